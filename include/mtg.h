@@ -1,0 +1,230 @@
+/*
+ * mtg.h - C ABI of the GB300 engine for MADDY's Brownian/Langevin hot path
+ * (6-DOF coarse-grained tubulin beads: forces, pair lists, Euler-Maruyama
+ * update with HybridTaus noise, energies, TEA hydrodynamics).
+ *
+ * Every function returns an int status: MTG_OK (0) or a negative MTG_E_*
+ * code; mtg_last_error_string() describes the last failure of the calling
+ * thread.  Host buffers are plain pointers owned by the caller; device
+ * buffers are owned by the engine.  One engine = one CUDA stream; an engine
+ * is not thread-safe, distinct engines are independent.
+ *
+ * Reference interfaces replaced (paths inside the klyshko/MT project):
+ *   compute(Coord*, Coord*, Parameters&, Topology&, Energies*)   src/compute_cuda.cuh:17
+ *   initIntegration / deleteIntegration                          src/compute_cuda.cuh:18-19
+ *   initTeaIntegrator / updateTea / integrateTea / deleteTea...  src/bdhitea.cuh:18-24
+ *   initRand(int seed, int Np)                                   src/ht.cuh:14
+ * The engine entry points below are what a compute() drop-in calls; see
+ * mt_gb300/host/mtg_compute.cpp for that drop-in.
+ */
+#ifndef MTG_H_
+#define MTG_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MTG_OK            0
+#define MTG_E_CUDA       -1  /* a CUDA runtime call failed (reference: checkCUDAError -> die, src/Cuda.h:120-135) */
+#define MTG_E_CONFIG     -2  /* invalid parameters, sizes or call arguments (reference: DIE, src/configreader.cpp:129) */
+#define MTG_E_OVERFLOW   -3  /* a neighbour list exceeded its capacity (reference: silent overflow, src/compute_cuda.cu:1076) */
+#define MTG_E_NONFINITE  -4  /* a non-finite energy total (reference: prints, src/updater.cpp:27-30) */
+#define MTG_E_TEA_EPS    -5  /* TEA epsilon > 1 in capricious mode, > epsmax, or a too-diagonal tensor (reference: exit(-1), src/bdhitea.cu:89-106) */
+#define MTG_E_TIMEOUT    -6  /* a bounded device-side wait gave up */
+#define MTG_E_STATE      -7  /* call out of sequence (e.g. surrogate not trained) */
+
+/* Coord as laid out by the reference (src/mt.h:63-71): 7 floats per bead in
+ * the order x, y, z, fi, theta, psi, w (w unused).  Host state buffers of
+ * this ABI use that AoS layout so a caller can pass its Coord* directly. */
+#define MTG_COORD_FLOATS 7
+
+/* Energies as laid out by the reference (src/mt.h:94-102): 7 doubles in the
+ * order U_harm, U_long, U_lat, U_psi, U_fi, U_teta, U_lj. */
+#define MTG_ENERGY_TERMS 7
+
+/* Scalar parameters of the hot path.  Each field carries the meaning (and
+ * units: nm, ps, kcal/mol, K) of the Parameters field of the same name,
+ * src/parameters.h:246-318; derived values (gammaR, gammaTheta, varR,
+ * varTheta) are computed by the caller exactly as src/preparator.cpp:209-221
+ * does, see mtg_derive_params(). */
+typedef struct {
+    float dt, Temp, viscosity;
+    float gammaR, gammaTheta, varR, varTheta;
+    float alpha, freeze_temp;
+    /* harmonic bond and bending (src/parameters.h:270-278) */
+    float C, B_psi, B_fi, B_theta, psi_0, fi_0, theta0_gtp, theta0_gdp;
+    /* Morse longitudinal / lateral (src/parameters.h:279-283) */
+    float A_lat, A_long, D_lat, D_long, seam_coeff;
+    /* Gaussian barriers (src/parameters.h:296-302); w_* already divided by 2*sqrt(-2 ln 0.5) */
+    int barrier;
+    float a_barr_long, r_barr_long, w_barr_long, a_barr_lat, r_barr_lat, w_barr_lat;
+    /* LJ repulsion and list (src/parameters.h:304-308) */
+    int lj_on;
+    float ljscale, ljsigma6, ljpairscutoff;
+    int ljpairsupdatefreq;
+    /* cylindrical walls (src/parameters.h:290-295); per-trajectory zs passed in the topology */
+    int is_wall;
+    float rep_r, rep_eps, rep_leftborder;
+    /* assembly mode: pair lists rebuilt on device (src/parameters.h:255) */
+    int is_assembly;
+    /* TEA hydrodynamics (Tea, src/mt.h:104-121; keys src/parameters.h:236-242) */
+    int hdi_on;
+    float tea_a;
+    int tea_epsilon_freq;
+    int tea_capricious;
+    float tea_epsmax;
+    /* HybridTaus seed (src/parameters.h:248) */
+    int rseed;
+} mtg_params;
+
+/* Topology of a uniform batch, in the reference's layout (Topology,
+ * src/mt.h:73-92): Ntr trajectories of Ntot beads; per-template arrays
+ * ([Ntot]) are shared by all trajectories, per-bead arrays are [Ntot*Ntr]
+ * with bead p = ind + traj*Ntot.  Longitudinal/lateral lists are read only
+ * when is_assembly == 0 (static lists, src/preparator.cpp:357-560). */
+typedef struct {
+    int Ntot, Ntr;
+    int maxHarmonicPerMonomer;
+    const int *harmonicCount;        /* [Ntot] */
+    const int *harmonic;             /* [maxHarmonicPerMonomer*Ntot], sign-encoded */
+    int maxLongitudinalPerMonomer;   /* list capacity (reference: 8, src/preparator.cpp:722) */
+    const int *longitudinalCount;    /* [Ntot*Ntr] or NULL */
+    const int *longitudinal;         /* [maxLong*Ntot*Ntr] or NULL */
+    int maxLateralPerMonomer;        /* list capacity (reference: 16, src/preparator.cpp:721) */
+    const int *lateralCount;
+    const int *lateral;
+    int maxLJPerMonomer;             /* list capacity (reference: 256, src/compute_cuda.cu:1076) */
+    const uint8_t *fixed;            /* [Ntot] */
+    const int *mon_type;             /* [Ntot] 0 = alpha, 1 = beta */
+    const uint8_t *extra;            /* [Ntot*Ntr] */
+    const int *gtp;                  /* [Ntot*Ntr] */
+    const int *on_tubule_cur;        /* [Ntot*Ntr] */
+    const float *zs;                 /* [Ntr] wall height per trajectory (Parameters::zs) */
+} mtg_topology;
+
+/* Topology of a ragged batch: trajectory t owns beads offsets[t] ..
+ * offsets[t+1]-1.  All per-bead arrays have offsets[ntraj] entries; list and
+ * harmonic indices are local to the bead's trajectory and use the reference's
+ * sign encoding.  No reference counterpart (the reference batches only
+ * uniform copies of one PDB, src/preparator.cpp:303-317). */
+typedef struct {
+    int ntraj;
+    const int *offsets;              /* [ntraj+1] */
+    int maxHarmonicPerMonomer;
+    const int *harmonicCount;        /* [nbeads] */
+    const int *harmonic;             /* [maxHarmonicPerMonomer*nbeads] bead-major */
+    int maxLongitudinalPerMonomer, maxLateralPerMonomer, maxLJPerMonomer;
+    const int *longitudinalCount;    /* [nbeads] or NULL (assembly mode) */
+    const int *longitudinal;         /* [maxLong*nbeads] bead-major or NULL */
+    const int *lateralCount;
+    const int *lateral;
+    const uint8_t *fixed;            /* [nbeads] */
+    const uint8_t *extra;            /* [nbeads] */
+    const int *mon_type;             /* [nbeads] */
+    const int *gtp;                  /* [nbeads] */
+    const int *on_tubule_cur;        /* [nbeads] */
+    const float *zs;                 /* [ntraj] */
+} mtg_batch_topology;
+
+typedef struct mtg_engine mtg_engine;
+
+/* Last error message of the calling thread (never NULL). */
+const char *mtg_last_error_string(void);
+
+/* Fills gammaR, gammaTheta, varR, varTheta from dt, Temp, viscosity, hdi_on
+ * and tea_a as src/preparator.cpp:209-219 does (k_B = 0.0019872041 kcal/mol/K,
+ * r_mon = 2 nm). */
+int mtg_derive_params(mtg_params *p);
+
+/* Creates an engine for a uniform batch (replaces initIntegration,
+ * src/compute_cuda.cu:977-1098, and initTeaIntegrator, src/bdhitea.cu:13-35).
+ * Seeds the HybridTaus streams from p->rseed as initRand(rseed, 2*Ntot*Ntr)
+ * does (src/HybridTaus.cu:21-48).  The state must be uploaded before stepping. */
+int mtg_create(const mtg_params *p, const mtg_topology *top, mtg_engine **out);
+
+/* Creates an engine for a ragged batch (no reference counterpart). */
+int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *top, mtg_engine **out);
+
+/* Frees every device buffer of the engine (replaces deleteIntegration,
+ * src/compute_cuda.cu:1100-1123, and deleteTeaIntegrator, src/bdhitea.cu:44-55). */
+int mtg_destroy(mtg_engine *e);
+
+int mtg_num_beads(const mtg_engine *e, int *nbeads, int *ntraj);
+
+/* Re-seeds all 2*nbeads HybridTaus streams with the reference's ran2-based
+ * generator (src/HybridTaus.cu:32-48, src/ran2.h:18-56). */
+int mtg_seed_rng(mtg_engine *e, int rseed);
+/* Reads / writes the raw HybridTaus states, 2*nbeads uint4 = 8*nbeads uint32
+ * (stream p drives xyz noise of bead p, stream p+nbeads its angle noise). */
+int mtg_download_rng(mtg_engine *e, uint32_t *seeds);
+int mtg_upload_rng(mtg_engine *e, const uint32_t *seeds);
+
+/* Host <-> device state, Coord AoS (MTG_COORD_FLOATS floats per bead).  The
+ * upload does not wrap angles; the reference wraps them once on the host in
+ * initIntegration (src/compute_cuda.cu:1004-1010) and so does the compute()
+ * drop-in.  Download writes r (may be NULL) and the forces of the last force
+ * evaluation f (may be NULL; zero where the reference's d_f would be zero). */
+int mtg_upload_state(mtg_engine *e, const float *r);
+int mtg_download_state(mtg_engine *e, float *r, float *f);
+/* Forces kept by plain (no-HI) steps: by default the fused step does not
+ * store them (the reference zeroes d_f after integrating, src/compute_cuda.cu:966-972);
+ * keep != 0 makes every step store the forces it integrated with. */
+int mtg_set_keep_forces(mtg_engine *e, int keep);
+
+/* Host-side topology changes made by the updater hooks (reference: H2D of
+ * gtp src/compute_cuda.cu:1157, on_tubule_cur :1190, extra :1202). */
+int mtg_set_gtp(mtg_engine *e, const int *gtp);
+int mtg_set_extra(mtg_engine *e, const uint8_t *extra);
+int mtg_set_on_tubule(mtg_engine *e, const int *on_tubule_cur);
+
+/* Rebuilds the LJ list (LJ_kernel, src/compute_cuda.cu:913-940) and, in
+ * assembly mode, the longitudinal and lateral lists (pairs_kernel,
+ * src/compute_cuda.cu:527-674) from the current state. */
+int mtg_rebuild_pairs(mtg_engine *e);
+/* Copies the lists to the host in the reference's layout: counts [nbeads],
+ * entries [cap*nbeads] bead-major (cap = the engine's list capacity).  Any
+ * pointer may be NULL. */
+int mtg_download_lists(mtg_engine *e, int *lj_count, int *lj, int *long_count, int *lon,
+                       int *lat_count, int *lat);
+int mtg_list_capacity(const mtg_engine *e, int *max_long, int *max_lat, int *max_lj);
+
+/* Evaluates the forces of the current state (compute_kernel,
+ * src/compute_cuda.cu:32-525) without integrating, and copies them to f
+ * (Coord AoS, may be NULL). */
+int mtg_compute_forces(mtg_engine *e, float *f);
+
+/* Runs steps first_step .. first_step+nsteps-1 of the reference step loop
+ * (src/compute_cuda.cu:1137-1238) without its host I/O: a pair-list rebuild
+ * when step % ljpairsupdatefreq == 0, the forces, then either the
+ * Euler-Maruyama update (integrate_kernel, :943-975) or, with hdi_on, the TEA
+ * update (updateTea + integrateTea, src/bdhitea.cu:37-118).  Launches are
+ * replayed from CUDA graphs; the call returns once they are enqueued and
+ * checks device error flags at the end. */
+int mtg_step(mtg_engine *e, long long first_step, int nsteps);
+/* Waits for the engine's stream and reports any device error flag. */
+int mtg_sync(mtg_engine *e);
+
+/* Energies of the current state (energy_kernel, src/compute_cuda.cu:676-911,
+ * each term halved per bead).  per_bead: [nbeads*7] doubles (may be NULL),
+ * per_traj: [ntraj*7] doubles summed on the device in FP64 (the reference
+ * sums on the host in double, src/updater.cpp:16-26).  Returns
+ * MTG_E_NONFINITE when a harm/long/lat/lj total is not finite (totals are
+ * still written). */
+int mtg_energies(mtg_engine *e, double *per_bead, double *per_traj);
+
+/* TEA: recomputes the per-bead coupling sums and, in FP64 on the device,
+ * epsilon and beta of every trajectory (integrateTea_epsilon_unlisted,
+ * src/bdhitea_kernel.cu:84-101, and the host reduction of updateTea,
+ * src/bdhitea.cu:57-118).  eps_out [ntraj] doubles and beta_out [ntraj]
+ * floats may be NULL.  ci_out [nbeads*4] floats (may be NULL): the per-bead
+ * row sums of squared normalised tensor entries (d_ci). */
+int mtg_tea_update(mtg_engine *e, double *eps_out, float *beta_out, float *ci_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MTG_H_ */

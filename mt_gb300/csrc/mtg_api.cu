@@ -1,0 +1,761 @@
+// mtg_api.cu - the engine object and the C ABI declared in include/mtg.h.
+//
+// Host orchestration of one batch on one GPU: device buffers owned by the
+// engine, one CUDA stream per engine, the step loop replayed from CUDA graphs
+// (one graph per pair-list period and frame-buffer parity), device error
+// words read back once per call instead of a device synchronisation after
+// every launch (the reference's checkCUDAError, src/Cuda.h:120-135).
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mtg.h"
+#include "mtg_internal.cuh"
+
+using namespace mtg;
+
+namespace {
+
+thread_local std::string g_last_error = "no error";
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return fail(MTG_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                       \
+    } while (0)
+
+// ran2 of the reference seeding (src/ran2.h:18-56) with its function statics
+// held in a struct that starts from their initial values.
+struct Ran2 {
+    int idum2 = 123456789, iy = 0, iv[32] = {0};
+    double next(int *idum) {
+        const int IM1 = 2147483563, IM2 = 2147483399, IMM1 = IM1 - 1;
+        const int IA1 = 40014, IA2 = 40692, IQ1 = 53668, IQ2 = 52774, IR1 = 12211, IR2 = 3791;
+        const int NTAB = 32, NDIV = 1 + IMM1 / NTAB;
+        int j, k;
+        if (*idum <= 0) {
+            *idum = (-(*idum) < 1) ? 1 : -(*idum);
+            idum2 = *idum;
+            for (j = NTAB + 7; j >= 0; j--) {
+                k = *idum / IQ1;
+                *idum = IA1 * (*idum - k * IQ1) - k * IR1;
+                if (*idum < 0) *idum += IM1;
+                if (j < NTAB) iv[j] = *idum;
+            }
+            iy = iv[0];
+        }
+        k = *idum / IQ1;
+        *idum = IA1 * (*idum - k * IQ1) - k * IR1;
+        if (*idum < 0) *idum += IM1;
+        k = idum2 / IQ2;
+        idum2 = IA2 * (idum2 - k * IQ2) - k * IR2;
+        if (idum2 < 0) idum2 += IM2;
+        j = iy / NDIV;
+        iy = iv[j] - idum2;
+        iv[j] = *idum;
+        if (iy < 1) iy += IMM1;
+        const double t = (1.0 / IM1) * iy;
+        return t > 1.0 - 1.2e-7 ? 1.0 - 1.2e-7 : t;
+    }
+};
+
+// generateSeeds (src/HybridTaus.cu:32-48): each component (unsigned)(ran2 *
+// UINT_MAX), redrawn while below 128.
+void make_seeds(int seed, size_t nstreams, std::vector<uint32_t> &out) {
+    Ran2 r;
+    out.resize(4 * nstreams);
+    for (size_t i = 0; i < 4 * nstreams; i++) {
+        uint32_t v;
+        do {
+            v = (uint32_t)(r.next(&seed) * (double)UINT_MAX);
+        } while (v < 128u);
+        out[i] = v;
+    }
+}
+
+template <class T>
+int dalloc(T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    CK(cudaMalloc((void **)p, n * sizeof(T)));
+    return MTG_OK;
+}
+
+}  // namespace
+
+struct mtg_engine {
+    mtg_params p{};
+    KParams kp{};
+    int nb = 0, nt = 0;
+    int cur = 0;            // frame buffer holding the current state
+    bool keep_forces = false;
+    bool have_state = false;
+    bool lists_valid = false;
+    cudaStream_t stream = nullptr;
+    std::vector<int> h_off;
+    // device
+    int *off = nullptr, *traj = nullptr, *flags = nullptr, *harm = nullptr;
+    float *zs = nullptr;
+    float4 *frame[2] = {nullptr, nullptr};
+    float4 *force = nullptr;
+    uint4 *seeds = nullptr;
+    int *ljc = nullptr, *lj = nullptr, *lonc = nullptr, *lon = nullptr, *latc = nullptr, *lat = nullptr;
+    int *err = nullptr;
+    int2 *work = nullptr;
+    int nwork = 0;
+    int *work_first = nullptr;
+    double *en_partials = nullptr, *en_traj = nullptr, *en_bead = nullptr;
+    float4 *tea_r = nullptr, *tea_ci = nullptr;
+    float *tea_eps = nullptr, *tea_beta = nullptr;
+    double *tea_eps_t = nullptr;
+    float *stage = nullptr;        // 7*nb floats for host <-> device Coord transfers
+    void *stage_host = nullptr;    // pinned mirror of stage
+    uint8_t *stage_u8 = nullptr;
+    int *stage_i = nullptr;
+    // graphs: [parity]
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_period = 0;
+
+    DevBuffers bufs() const {
+        DevBuffers b{};
+        b.off = off;
+        b.traj = traj;
+        b.flags = flags;
+        b.harm = harm;
+        b.zs = zs;
+        b.frame_in = frame[cur];
+        b.frame_out = frame[cur ^ 1];
+        b.force = force;
+        b.seeds = seeds;
+        b.ljc = ljc;
+        b.lj = lj;
+        b.lonc = lonc;
+        b.lon = lon;
+        b.latc = latc;
+        b.lat = lat;
+        b.err = err;
+        b.tea_r = tea_r;
+        b.tea_ci = tea_ci;
+        b.tea_eps = tea_eps;
+        b.tea_beta = tea_beta;
+        b.tea_eps_t = tea_eps_t;
+        return b;
+    }
+};
+
+namespace {
+
+KParams make_kparams(const mtg_params &p, int nb, int nt, int maxH, int maxLong, int maxLat, int maxLJ) {
+    KParams k{};
+    k.nb = nb;
+    k.nt = nt;
+    // integrate_kernel coefficients, evaluated in float as src/compute_cuda.cu:955-961 does
+    k.kr = p.dt / p.gammaR;
+    k.kfi = p.dt / (p.gammaTheta * p.alpha);
+    k.kth = p.dt / p.gammaTheta;
+    k.varR = p.varR;
+    k.nfi = p.varTheta * sqrtf(p.freeze_temp / p.alpha);
+    k.varTheta = p.varTheta;
+    k.C = p.C;
+    k.B_psi = p.B_psi;
+    k.B_fi = p.B_fi;
+    k.B_theta = p.B_theta;
+    k.psi_0 = p.psi_0;
+    k.fi_0 = p.fi_0;
+    k.th0_gtp = p.theta0_gtp;
+    k.th0_gdp = p.theta0_gdp;
+    k.A_long = p.A_long;
+    k.D_long = p.D_long;
+    k.A_lat = p.A_lat;
+    k.D_lat = p.D_lat;
+    k.D_lat_seam = p.D_lat / p.seam_coeff;
+    k.barrier = p.barrier;
+    k.a_bl = p.a_barr_long;
+    k.r_bl = p.r_barr_long;
+    k.w_bl = p.w_barr_long;
+    k.a_bt = p.a_barr_lat;
+    k.r_bt = p.r_barr_lat;
+    k.w_bt = p.w_barr_lat;
+    k.lj_on = p.lj_on;
+    k.lj_pref = p.ljscale * p.ljsigma6;
+    k.ljcut = p.ljpairscutoff;
+    k.is_wall = p.is_wall;
+    k.rep_r = p.rep_r;
+    k.rep_eps = p.rep_eps;
+    k.lb = p.rep_leftborder;
+    k.is_assembly = p.is_assembly;
+    // lateral binding sites (src/mt.h:44-50), float arithmetic as in the reference
+    const float c = cosf((float)(2.0 * M_PI / 13.0)), s = sinf((float)(2.0 * M_PI / 13.0));
+    k.p1x = 0.5f * 8.12f * (c - 1.0f);
+    k.p1y = 0.5f * 8.12f * s;
+    k.p1z = -3.0f * 2.0f / 13.0f;
+    k.p2x = k.p1x;
+    k.p2y = -k.p1y;
+    k.p2z = -k.p1z;
+    k.maxH = maxH;
+    k.maxLong = maxLong;
+    k.maxLat = maxLat;
+    k.maxLJ = maxLJ;
+    k.tea_a = p.tea_a;
+    k.tea_var = sqrtf(2.0f * 0.0019872041f * p.Temp * p.gammaR / p.dt);
+    return k;
+}
+
+int check_params(const mtg_params *p) {
+    if (!p) return fail(MTG_E_CONFIG, "params is NULL");
+    if (!(p->dt > 0) || !(p->gammaR > 0) || !(p->gammaTheta > 0) || !(p->alpha > 0))
+        return fail(MTG_E_CONFIG, "dt, gammaR, gammaTheta and alpha must be positive (call mtg_derive_params)");
+    if (p->ljpairsupdatefreq <= 0) return fail(MTG_E_CONFIG, "ljpairsupdatefreq must be positive");
+    if (p->hdi_on && p->tea_epsilon_freq <= 0)
+        return fail(MTG_E_CONFIG, "tea_epsilon_freq must be positive with tea_on (the reference divides by it)");
+    if (p->hdi_on && !(p->tea_a > 0)) return fail(MTG_E_CONFIG, "tea_a must be positive");
+    if (p->seam_coeff == 0.0f) return fail(MTG_E_CONFIG, "seam_coeff must be non-zero");
+    return MTG_OK;
+}
+
+int upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    return MTG_OK;
+}
+
+int check_errors(mtg_engine *e) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, e->err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    CK(cudaGetLastError());
+    if (h) {
+        CK(cudaMemsetAsync(e->err, 0, sizeof(int), e->stream));
+        if (h & kErrOverflow) return fail(MTG_E_OVERFLOW, "a neighbour list exceeded its capacity");
+        if (h & kErrTeaEps)
+            return fail(MTG_E_TEA_EPS, "TEA epsilon out of range (> 1 in capricious mode, > epsmax, or a too diagonal tensor)");
+        if (h & kErrNonFinite) return fail(MTG_E_NONFINITE, "non-finite energy total");
+    }
+    return MTG_OK;
+}
+
+void destroy_graphs(mtg_engine *e) {
+    for (auto &g : e->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+// Enqueues one step of the loop of compute() (src/compute_cuda.cu:1137-1238)
+// minus its host I/O.
+void enqueue_step(mtg_engine *e, long long step) {
+    const mtg_params &p = e->p;
+    if (step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
+        launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+        e->lists_valid = true;
+    }
+    if (p.hdi_on) {
+        launch_forces(e->kp, e->bufs(), true, e->stream);
+        if (step % p.tea_epsilon_freq == 0) {
+            launch_tea_eps(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+            launch_tea_beta(e->kp, e->bufs(), p.tea_capricious, p.tea_epsmax, e->stream);
+        }
+        launch_tea_step(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+    } else {
+        launch_step_plain(e->kp, e->bufs(), e->keep_forces, e->stream);
+    }
+    e->cur ^= 1;
+}
+
+long long lcm_ll(long long a, long long b) {
+    long long x = a, y = b;
+    while (y) {
+        const long long t = x % y;
+        x = y;
+        y = t;
+    }
+    return a / x * b;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mtg_last_error_string(void) { return g_last_error.c_str(); }
+
+int mtg_derive_params(mtg_params *p) {
+    if (!p) return fail(MTG_E_CONFIG, "params is NULL");
+    const float rmon = 2.0f;
+    // src/preparator.cpp:209-219 (M_PI in double, stored to float)
+    p->gammaR = (float)(6 * M_PI * p->viscosity * (p->hdi_on ? p->tea_a : rmon));
+    p->gammaTheta = (float)(8 * M_PI * p->viscosity * pow(rmon, 3));
+    p->varR = sqrtf(2.0f * 0.0019872041f * p->Temp * p->dt / p->gammaR);
+    p->varTheta = sqrtf(2.0f * 0.0019872041f * p->Temp * p->dt / p->gammaTheta);
+    return MTG_OK;
+}
+
+int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engine **out) {
+    if (!out) return fail(MTG_E_CONFIG, "out is NULL");
+    *out = nullptr;
+    int rc = check_params(p);
+    if (rc) return rc;
+    if (!t || t->ntraj <= 0 || !t->offsets) return fail(MTG_E_CONFIG, "topology needs ntraj > 0 and offsets");
+    const int nt = t->ntraj;
+    if (t->offsets[0] != 0) return fail(MTG_E_CONFIG, "offsets[0] must be 0");
+    for (int i = 0; i < nt; i++)
+        if (t->offsets[i + 1] <= t->offsets[i]) return fail(MTG_E_CONFIG, "trajectory %d is empty or offsets decrease", i);
+    const long long nbl = t->offsets[nt];
+    const int maxH = t->maxHarmonicPerMonomer > 0 ? t->maxHarmonicPerMonomer : 1;
+    const int maxLong = t->maxLongitudinalPerMonomer > 0 ? t->maxLongitudinalPerMonomer : 8;
+    const int maxLat = t->maxLateralPerMonomer > 0 ? t->maxLateralPerMonomer : 16;
+    const int maxLJ = t->maxLJPerMonomer > 0 ? t->maxLJPerMonomer : 256;
+    if (nbl * (long long)maxLJ >= INT_MAX || nbl * (long long)maxLat >= INT_MAX || 2 * nbl * 4 >= INT_MAX)
+        return fail(MTG_E_CONFIG, "batch too large for 32-bit list indexing");
+    if (maxH > 7) return fail(MTG_E_CONFIG, "at most 7 harmonic partners per bead");
+    if (!t->harmonicCount || !t->harmonic || !t->fixed || !t->mon_type)
+        return fail(MTG_E_CONFIG, "harmonicCount, harmonic, fixed and mon_type are required");
+    if (!p->is_assembly && (!t->longitudinalCount || !t->longitudinal || !t->lateralCount || !t->lateral))
+        return fail(MTG_E_CONFIG, "static (non-assembly) mode needs the longitudinal and lateral lists");
+    const int nb = (int)nbl;
+
+    auto *e = new mtg_engine();
+    e->p = *p;
+    e->nb = nb;
+    e->nt = nt;
+    e->h_off.assign(t->offsets, t->offsets + nt + 1);
+    e->kp = make_kparams(*p, nb, nt, maxH, maxLong, maxLat, maxLJ);
+
+    // host-side per-bead tables
+    std::vector<int> traj(nb), flags(nb), harm((size_t)maxH * nb);
+    for (int tr = 0; tr < nt; tr++)
+        for (int g = t->offsets[tr]; g < t->offsets[tr + 1]; g++) traj[g] = tr;
+    for (int g = 0; g < nb; g++) {
+        const int hc = t->harmonicCount[g];
+        if (hc < 0 || hc > maxH) {
+            delete e;
+            return fail(MTG_E_CONFIG, "bead %d: harmonicCount %d outside [0, %d]", g, hc, maxH);
+        }
+        const int n = t->offsets[traj[g] + 1] - t->offsets[traj[g]];
+        for (int k = 0; k < maxH; k++) {
+            const int v = t->harmonic[(size_t)maxH * g + k];
+            const int a = v < 0 ? -v : v;
+            if (k < hc && a >= n) {
+                delete e;
+                return fail(MTG_E_CONFIG, "bead %d: harmonic partner %d outside its trajectory", g, v);
+            }
+            harm[(size_t)maxH * g + k] = v;
+        }
+        int f = 0;
+        if (t->extra && t->extra[g]) f |= kFlagExtra;
+        if (t->fixed[g]) f |= kFlagFixed;
+        if (t->mon_type[g] != 0) f |= kFlagBeta;
+        if (!t->gtp || t->gtp[g] == 1) f |= kFlagGtp;
+        if (t->on_tubule_cur && t->on_tubule_cur[g] != 0) f |= kFlagOnTubule;
+        f |= hc << kHarmShift;
+        flags[g] = f;
+    }
+    // work items: chunks of kTile beads, never straddling a trajectory
+    std::vector<int2> work;
+    std::vector<int> work_first(nt + 1);
+    for (int tr = 0; tr < nt; tr++) {
+        work_first[tr] = (int)work.size();
+        for (int g = t->offsets[tr]; g < t->offsets[tr + 1]; g += kTile) work.push_back(make_int2(tr, g));
+    }
+    work_first[nt] = (int)work.size();
+    e->nwork = (int)work.size();
+
+#define ALLOC(ptr, n)                         \
+    do {                                      \
+        if ((rc = dalloc(&(ptr), (n))) != 0) { \
+            mtg_destroy(e);                   \
+            return rc;                        \
+        }                                     \
+    } while (0)
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete e;
+        return fail(MTG_E_CUDA, "cudaStreamCreate failed");
+    }
+    ALLOC(e->off, nt + 1);
+    ALLOC(e->traj, nb);
+    ALLOC(e->flags, nb);
+    ALLOC(e->harm, (size_t)maxH * nb);
+    ALLOC(e->zs, nt);
+    ALLOC(e->frame[0], 4 * (size_t)nb);
+    ALLOC(e->frame[1], 4 * (size_t)nb);
+    ALLOC(e->force, 2 * (size_t)nb);
+    ALLOC(e->seeds, 2 * (size_t)nb);
+    ALLOC(e->ljc, nb);
+    ALLOC(e->lj, (size_t)maxLJ * nb);
+    ALLOC(e->lonc, nb);
+    ALLOC(e->lon, (size_t)maxLong * nb);
+    ALLOC(e->latc, nb);
+    ALLOC(e->lat, (size_t)maxLat * nb);
+    ALLOC(e->err, 1);
+    ALLOC(e->work, e->nwork);
+    ALLOC(e->work_first, nt + 1);
+    ALLOC(e->en_partials, 7 * (size_t)e->nwork);
+    ALLOC(e->en_traj, 7 * (size_t)nt);
+    ALLOC(e->stage, 7 * (size_t)nb);
+    ALLOC(e->stage_u8, nb);
+    ALLOC(e->stage_i, nb);
+    if (p->hdi_on) {
+        ALLOC(e->tea_r, nb);
+        ALLOC(e->tea_ci, nb);
+        ALLOC(e->tea_eps, nb);
+        ALLOC(e->tea_beta, nt);
+        ALLOC(e->tea_eps_t, nt);
+    }
+#undef ALLOC
+    cudaStream_t s = e->stream;
+    std::vector<float> zs(nt, 0.f);
+    if (t->zs) zs.assign(t->zs, t->zs + nt);
+    if ((rc = upload(e->off, t->offsets, sizeof(int) * (nt + 1), s)) || (rc = upload(e->traj, traj.data(), sizeof(int) * nb, s)) ||
+        (rc = upload(e->flags, flags.data(), sizeof(int) * nb, s)) ||
+        (rc = upload(e->harm, harm.data(), sizeof(int) * harm.size(), s)) ||
+        (rc = upload(e->zs, zs.data(), sizeof(float) * nt, s)) ||
+        (rc = upload(e->work, work.data(), sizeof(int2) * work.size(), s)) ||
+        (rc = upload(e->work_first, work_first.data(), sizeof(int) * (nt + 1), s))) {
+        mtg_destroy(e);
+        return rc;
+    }
+    cudaMemsetAsync(e->err, 0, sizeof(int), s);
+    cudaMemsetAsync(e->ljc, 0, sizeof(int) * nb, s);
+    cudaMemsetAsync(e->lonc, 0, sizeof(int) * nb, s);
+    cudaMemsetAsync(e->latc, 0, sizeof(int) * nb, s);
+    cudaMemsetAsync(e->force, 0, sizeof(float4) * 2 * nb, s);
+    if (p->hdi_on) {
+        cudaMemsetAsync(e->tea_ci, 0, sizeof(float4) * nb, s);
+        cudaMemsetAsync(e->tea_beta, 0, sizeof(float) * nt, s);
+    }
+    // static (non-assembly) lists, transposed to k-major
+    if (!p->is_assembly) {
+        std::vector<int> cnt(nb), lon((size_t)maxLong * nb, 0), lat((size_t)maxLat * nb, 0), cnt2(nb);
+        for (int g = 0; g < nb; g++) {
+            cnt[g] = t->longitudinalCount[g];
+            cnt2[g] = t->lateralCount[g];
+            if (cnt[g] < 0 || cnt[g] > maxLong || cnt2[g] < 0 || cnt2[g] > maxLat) {
+                mtg_destroy(e);
+                return fail(MTG_E_OVERFLOW, "bead %d: static list count exceeds its capacity", g);
+            }
+            const int n = t->offsets[traj[g] + 1] - t->offsets[traj[g]];
+            for (int k = 0; k < cnt[g]; k++) {
+                const int v = t->longitudinal[(size_t)maxLong * g + k], a = v < 0 ? -v : v;
+                if (a >= n) {
+                    mtg_destroy(e);
+                    return fail(MTG_E_CONFIG, "bead %d: longitudinal partner %d outside its trajectory", g, v);
+                }
+                lon[(size_t)k * nb + g] = v;
+            }
+            for (int k = 0; k < cnt2[g]; k++) {
+                const int v = t->lateral[(size_t)maxLat * g + k];
+                int a = v < 0 ? -v : v;
+                if (a == kZeroCode) a = 0;
+                if (a >= n) {
+                    mtg_destroy(e);
+                    return fail(MTG_E_CONFIG, "bead %d: lateral partner %d outside its trajectory", g, v);
+                }
+                lat[(size_t)k * nb + g] = v;
+            }
+        }
+        if ((rc = upload(e->lonc, cnt.data(), sizeof(int) * nb, s)) ||
+            (rc = upload(e->lon, lon.data(), sizeof(int) * lon.size(), s)) ||
+            (rc = upload(e->latc, cnt2.data(), sizeof(int) * nb, s)) ||
+            (rc = upload(e->lat, lat.data(), sizeof(int) * lat.size(), s))) {
+            mtg_destroy(e);
+            return rc;
+        }
+        if (cudaStreamSynchronize(s) != cudaSuccess) {
+            mtg_destroy(e);
+            return fail(MTG_E_CUDA, "static list upload failed");
+        }
+    }
+    if ((rc = mtg_seed_rng(e, p->rseed)) != 0) {
+        mtg_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return MTG_OK;
+}
+
+int mtg_create(const mtg_params *p, const mtg_topology *t, mtg_engine **out) {
+    if (!out) return fail(MTG_E_CONFIG, "out is NULL");
+    *out = nullptr;
+    if (!t || t->Ntot <= 0 || t->Ntr <= 0) return fail(MTG_E_CONFIG, "topology needs Ntot > 0 and Ntr > 0");
+    if (!t->harmonicCount || !t->harmonic || !t->fixed || !t->mon_type)
+        return fail(MTG_E_CONFIG, "harmonicCount, harmonic, fixed and mon_type are required");
+    const int N = t->Ntot, R = t->Ntr;
+    const int maxH = t->maxHarmonicPerMonomer > 0 ? t->maxHarmonicPerMonomer : 1;
+    const size_t nb = (size_t)N * R;
+    // replicate the per-template arrays over the trajectories
+    std::vector<int> off(R + 1), hc(nb), hh((size_t)maxH * nb), mt(nb);
+    std::vector<uint8_t> fx(nb);
+    for (int r = 0; r <= R; r++) off[r] = r * N;
+    for (int r = 0; r < R; r++)
+        for (int i = 0; i < N; i++) {
+            const size_t g = (size_t)r * N + i;
+            hc[g] = t->harmonicCount[i];
+            for (int k = 0; k < maxH; k++) hh[(size_t)maxH * g + k] = t->harmonic[(size_t)maxH * i + k];
+            mt[g] = t->mon_type[i];
+            fx[g] = t->fixed[i];
+        }
+    mtg_batch_topology b{};
+    b.ntraj = R;
+    b.offsets = off.data();
+    b.maxHarmonicPerMonomer = maxH;
+    b.harmonicCount = hc.data();
+    b.harmonic = hh.data();
+    b.maxLongitudinalPerMonomer = t->maxLongitudinalPerMonomer;
+    b.maxLateralPerMonomer = t->maxLateralPerMonomer;
+    b.maxLJPerMonomer = t->maxLJPerMonomer;
+    b.longitudinalCount = t->longitudinalCount;
+    b.longitudinal = t->longitudinal;
+    b.lateralCount = t->lateralCount;
+    b.lateral = t->lateral;
+    b.fixed = fx.data();
+    b.extra = t->extra;
+    b.mon_type = mt.data();
+    b.gtp = t->gtp;
+    b.on_tubule_cur = t->on_tubule_cur;
+    b.zs = t->zs;
+    return mtg_create_batch(p, &b, out);
+}
+
+int mtg_destroy(mtg_engine *e) {
+    if (!e) return MTG_OK;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    destroy_graphs(e);
+    void *ptrs[] = {e->off, e->traj, e->flags, e->harm, e->zs, e->frame[0], e->frame[1], e->force, e->seeds,
+                    e->ljc, e->lj, e->lonc, e->lon, e->latc, e->lat, e->err, e->work, e->work_first,
+                    e->en_partials, e->en_traj, e->en_bead, e->tea_r, e->tea_ci, e->tea_eps, e->tea_beta,
+                    e->tea_eps_t, e->stage, e->stage_u8, e->stage_i};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (e->stage_host) cudaFreeHost(e->stage_host);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return MTG_OK;
+}
+
+int mtg_num_beads(const mtg_engine *e, int *nbeads, int *ntraj) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (nbeads) *nbeads = e->nb;
+    if (ntraj) *ntraj = e->nt;
+    return MTG_OK;
+}
+
+int mtg_list_capacity(const mtg_engine *e, int *max_long, int *max_lat, int *max_lj) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (max_long) *max_long = e->kp.maxLong;
+    if (max_lat) *max_lat = e->kp.maxLat;
+    if (max_lj) *max_lj = e->kp.maxLJ;
+    return MTG_OK;
+}
+
+int mtg_seed_rng(mtg_engine *e, int rseed) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    std::vector<uint32_t> s;
+    make_seeds(rseed, 2 * (size_t)e->nb, s);
+    return mtg_upload_rng(e, s.data());
+}
+
+int mtg_upload_rng(mtg_engine *e, const uint32_t *seeds) {
+    if (!e || !seeds) return fail(MTG_E_CONFIG, "engine or seeds is NULL");
+    CK(cudaMemcpyAsync(e->seeds, seeds, sizeof(uint4) * 2 * (size_t)e->nb, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return MTG_OK;
+}
+
+int mtg_download_rng(mtg_engine *e, uint32_t *seeds) {
+    if (!e || !seeds) return fail(MTG_E_CONFIG, "engine or seeds is NULL");
+    CK(cudaMemcpyAsync(seeds, e->seeds, sizeof(uint4) * 2 * (size_t)e->nb, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return MTG_OK;
+}
+
+int mtg_upload_state(mtg_engine *e, const float *r) {
+    if (!e || !r) return fail(MTG_E_CONFIG, "engine or r is NULL");
+    CK(cudaMemcpyAsync(e->stage, r, sizeof(float) * 7 * (size_t)e->nb, cudaMemcpyHostToDevice, e->stream));
+    launch_frames_from_coords(e->kp, e->stage, e->frame[e->cur], e->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e->stream));
+    e->have_state = true;
+    return MTG_OK;
+}
+
+int mtg_download_state(mtg_engine *e, float *r, float *f) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    const size_t bytes = sizeof(float) * 7 * (size_t)e->nb;
+    if (r) {
+        launch_coords_from_frames(e->kp, e->frame[e->cur], e->stage, e->stream);
+        CK(cudaMemcpyAsync(r, e->stage, bytes, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    if (f) {
+        launch_forces_to_coords(e->kp, e->force, e->stage, e->stream);
+        CK(cudaMemcpyAsync(f, e->stage, bytes, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    CK(cudaGetLastError());
+    return MTG_OK;
+}
+
+static int set_flag_array(mtg_engine *e, const uint8_t *extra, const int *gtp, const int *ontub) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    const size_t nb = e->nb;
+    if (extra) CK(cudaMemcpyAsync(e->stage_u8, extra, nb, cudaMemcpyHostToDevice, e->stream));
+    if (gtp || ontub) CK(cudaMemcpyAsync(e->stage_i, gtp ? gtp : ontub, sizeof(int) * nb, cudaMemcpyHostToDevice, e->stream));
+    launch_set_flags(e->nb, extra ? e->stage_u8 : nullptr, gtp ? e->stage_i : nullptr, ontub ? e->stage_i : nullptr,
+                     e->flags, e->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e->stream));
+    return MTG_OK;
+}
+
+int mtg_set_gtp(mtg_engine *e, const int *gtp) {
+    if (!gtp) return fail(MTG_E_CONFIG, "gtp is NULL");
+    return set_flag_array(e, nullptr, gtp, nullptr);
+}
+int mtg_set_extra(mtg_engine *e, const uint8_t *extra) {
+    if (!extra) return fail(MTG_E_CONFIG, "extra is NULL");
+    return set_flag_array(e, extra, nullptr, nullptr);
+}
+int mtg_set_on_tubule(mtg_engine *e, const int *on_tubule_cur) {
+    if (!on_tubule_cur) return fail(MTG_E_CONFIG, "on_tubule_cur is NULL");
+    return set_flag_array(e, nullptr, nullptr, on_tubule_cur);
+}
+
+int mtg_set_keep_forces(mtg_engine *e, int keep) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (e->keep_forces != (keep != 0)) destroy_graphs(e);
+    e->keep_forces = keep != 0;
+    return MTG_OK;
+}
+
+int mtg_rebuild_pairs(mtg_engine *e) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
+    if (e->p.lj_on || e->p.is_assembly) launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+    CK(cudaGetLastError());
+    e->lists_valid = true;
+    return check_errors(e);
+}
+
+int mtg_download_lists(mtg_engine *e, int *lj_count, int *lj, int *long_count, int *lon, int *lat_count, int *lat) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    const size_t nb = e->nb;
+    struct L {
+        int *cnt_dev, *arr_dev, cap;
+        int *cnt_host, *arr_host;
+    } ls[3] = {{e->ljc, e->lj, e->kp.maxLJ, lj_count, lj},
+               {e->lonc, e->lon, e->kp.maxLong, long_count, lon},
+               {e->latc, e->lat, e->kp.maxLat, lat_count, lat}};
+    for (auto &l : ls) {
+        if (!l.cnt_host && !l.arr_host) continue;
+        std::vector<int> cnt(nb), arr((size_t)l.cap * nb);
+        CK(cudaMemcpyAsync(cnt.data(), l.cnt_dev, sizeof(int) * nb, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaMemcpyAsync(arr.data(), l.arr_dev, sizeof(int) * arr.size(), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        if (l.cnt_host) std::memcpy(l.cnt_host, cnt.data(), sizeof(int) * nb);
+        if (l.arr_host) {
+            // k-major on the device -> bead-major (reference layout) on the host
+            for (size_t g = 0; g < nb; g++)
+                for (int k = 0; k < l.cap; k++) l.arr_host[(size_t)l.cap * g + k] = k < cnt[g] ? arr[(size_t)k * nb + g] : 0;
+        }
+    }
+    return MTG_OK;
+}
+
+int mtg_compute_forces(mtg_engine *e, float *f) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
+    launch_forces(e->kp, e->bufs(), false, e->stream);
+    CK(cudaGetLastError());
+    int rc = check_errors(e);
+    if (rc) return rc;
+    return f ? mtg_download_state(e, nullptr, f) : MTG_OK;
+}
+
+int mtg_step(mtg_engine *e, long long first_step, int nsteps) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
+    if (nsteps < 0 || first_step < 0) return fail(MTG_E_CONFIG, "negative step range");
+    const mtg_params &p = e->p;
+    long long period = p.ljpairsupdatefreq;
+    if (p.hdi_on) period = lcm_ll(period, p.tea_epsilon_freq);
+    const bool use_graphs = period <= 256;
+    if (e->graph_period != period) {
+        destroy_graphs(e);
+        e->graph_period = (int)period;
+    }
+    long long s = first_step;
+    const long long end = first_step + nsteps;
+    while (s < end) {
+        if (use_graphs && s % period == 0 && end - s >= period) {
+            cudaGraphExec_t &ge = e->graph[e->cur];
+            if (!ge) {
+                const int cur0 = e->cur;
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+                for (long long k = 0; k < period; k++) enqueue_step(e, k);
+                CK(cudaStreamEndCapture(e->stream, &g));
+                e->cur = cur0;
+                CK(cudaGraphInstantiate(&ge, g, 0));
+                cudaGraphDestroy(g);
+            }
+            CK(cudaGraphLaunch(ge, e->stream));
+            if (period & 1) e->cur ^= 1;
+            if (p.lj_on || p.is_assembly) e->lists_valid = true;
+            s += period;
+        } else {
+            enqueue_step(e, s);
+            s++;
+        }
+    }
+    CK(cudaGetLastError());
+    return check_errors(e);
+}
+
+int mtg_sync(mtg_engine *e) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    return check_errors(e);
+}
+
+int mtg_energies(mtg_engine *e, double *per_bead, double *per_traj) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
+    int rc;
+    if (per_bead && !e->en_bead && (rc = dalloc(&e->en_bead, 7 * (size_t)e->nb)) != 0) return rc;
+    launch_energy(e->kp, e->bufs(), per_bead ? e->en_bead : nullptr, e->en_partials, e->work, e->nwork, e->stream);
+    launch_energy_totals(e->kp, e->en_partials, e->work_first, e->en_traj, e->err, e->stream);
+    CK(cudaGetLastError());
+    if (per_traj)
+        CK(cudaMemcpyAsync(per_traj, e->en_traj, sizeof(double) * 7 * e->nt, cudaMemcpyDeviceToHost, e->stream));
+    if (per_bead)
+        CK(cudaMemcpyAsync(per_bead, e->en_bead, sizeof(double) * 7 * (size_t)e->nb, cudaMemcpyDeviceToHost, e->stream));
+    return check_errors(e);
+}
+
+int mtg_tea_update(mtg_engine *e, double *eps_out, float *beta_out, float *ci_out) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (!e->p.hdi_on) return fail(MTG_E_STATE, "engine created without hdi_on");
+    if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
+    launch_tea_eps(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+    launch_tea_beta(e->kp, e->bufs(), e->p.tea_capricious, e->p.tea_epsmax, e->stream);
+    CK(cudaGetLastError());
+    if (eps_out) CK(cudaMemcpyAsync(eps_out, e->tea_eps_t, sizeof(double) * e->nt, cudaMemcpyDeviceToHost, e->stream));
+    if (beta_out) CK(cudaMemcpyAsync(beta_out, e->tea_beta, sizeof(float) * e->nt, cudaMemcpyDeviceToHost, e->stream));
+    if (ci_out) CK(cudaMemcpyAsync(ci_out, e->tea_ci, sizeof(float4) * e->nb, cudaMemcpyDeviceToHost, e->stream));
+    return check_errors(e);
+}
+
+}  // extern "C"

@@ -1,0 +1,211 @@
+// mtg_internal.cuh - shared device helpers, kernel parameters and the engine
+// object of the GB300 engine.  Not part of the public ABI (include/mtg.h).
+//
+// HBM layout (nb beads over nt trajectories, CSR offsets):
+//   frame[2]   : two buffers of 4 planes x nb float4 (double-buffered state)
+//                plane 0 = (x, y, z, fi)
+//                plane 1 = (R e_z, psi)       axial site direction
+//                plane 2 = (R p1, theta)      lateral site p1 in the lab frame
+//                plane 3 = (R p2, 0)          lateral site p2 in the lab frame
+//                R = Rz(psi) Ry(theta) Rx(fi) is the bead's orientation; the
+//                planes are written by the kernel that moves the bead, so a
+//                neighbour's sites cost one 16 B gather instead of six sin/cos.
+//   flags[nb]  : bit 0 extra, 1 fixed, 2 mon_type, 3 gtp==1, 4 on_tubule!=0,
+//                bits 8..10 harmonic count
+//   harm[nb*maxH] : harmonic partners, local index, reference sign encoding
+//   lists      : counts [nb] + entries k-major [cap][nb] (coalesced per k)
+//   seeds[2nb] : HybridTaus uint4 states; stream g = xyz noise of bead g,
+//                stream g+nb = its angle noise
+//   force[2nb] : last generalised forces, (fx, fy, fz, 0), (ffi, ftheta, fpsi, 0)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mtg {
+
+constexpr int kFlagExtra = 1 << 0;
+constexpr int kFlagFixed = 1 << 1;
+constexpr int kFlagBeta = 1 << 2;
+constexpr int kFlagGtp = 1 << 3;
+constexpr int kFlagOnTubule = 1 << 4;
+constexpr int kHarmShift = 8;
+constexpr int kZeroCode = 999999;   // lateral encoding of bead 0 (src/mt.h:35)
+
+constexpr int kErrOverflow = 1;     // bit in the device error word
+constexpr int kErrTeaEps = 2;
+constexpr int kErrNonFinite = 4;
+
+// Scalars every kernel reads (passed by value: constant bank).
+struct KParams {
+    int nb, nt;
+    // Euler-Maruyama coefficients (integrate_kernel, src/compute_cuda.cu:955-963)
+    float kr, kfi, kth, varR, nfi, varTheta;
+    // harmonic + bending
+    float C, B_psi, B_fi, B_theta, psi_0, fi_0, th0_gtp, th0_gdp;
+    // Morse
+    float A_long, D_long, A_lat, D_lat, D_lat_seam;
+    // barriers
+    int barrier;
+    float a_bl, r_bl, w_bl, a_bt, r_bt, w_bt;
+    // LJ
+    int lj_on;
+    float lj_pref, ljcut;
+    // walls
+    int is_wall;
+    float rep_r, rep_eps, lb;
+    int is_assembly;
+    // lateral binding sites p1, p2 (src/mt.h:44-50)
+    float p1x, p1y, p1z, p2x, p2y, p2z;
+    int maxH, maxLong, maxLat, maxLJ;
+    // TEA
+    float tea_a, tea_var;
+};
+
+// Device buffers of one engine.
+struct DevBuffers {
+    const int *off;        // [nt+1]
+    const int *traj;       // [nb]
+    const int *flags;      // [nb]
+    const int *harm;       // [nb*maxH]
+    const float *zs;       // [nt]
+    float4 *frame_in;      // 4 planes
+    float4 *frame_out;     // 4 planes
+    float4 *force;         // 2 planes (may be null where unused)
+    uint4 *seeds;          // [2nb]
+    int *ljc, *lj, *lonc, *lon, *latc, *lat;
+    int *err;
+    // TEA
+    float4 *tea_r;         // random forces of all beads (xyz scaled, w raw)
+    float4 *tea_ci;        // row sums of squared normalised RPY entries
+    float *tea_eps;        // per-bead epsilon sums
+    float *tea_beta;       // [nt]
+    double *tea_eps_t;     // [nt]
+};
+
+// ------------------------------------------------------------------ RNG
+// HybridTaus (src/HybridTaus.cu:63-82): three Tausworthe steps and one LCG.
+__device__ __forceinline__ uint32_t taus_step(uint32_t &z, int s1, int s2, int s3, uint32_t m) {
+    const uint32_t b = ((z << s1) ^ z) >> s2;
+    z = ((z & m) << s3) ^ b;
+    return z;
+}
+__device__ __forceinline__ uint32_t hybrid_taus(uint4 &s) {
+    const uint32_t a = taus_step(s.x, 13, 19, 12, 4294967294u);
+    const uint32_t b = taus_step(s.y, 2, 25, 4, 4294967288u);
+    const uint32_t c = taus_step(s.z, 3, 11, 17, 4294967280u);
+    s.w = 1664525u * s.w + 1013904223u;
+    return a ^ b ^ c ^ s.w;
+}
+// uintToFloat (src/HybridTaus.cu:53-61): 23 mantissa bits -> [0,1), 0 -> 1e-8.
+__device__ __forceinline__ float uint_to_unit(uint32_t u) {
+    const float f = __uint_as_float(0x3f800000u | (0x007fffffu & u)) - 1.0f;
+    return f == 0.0f ? 1.0e-8f : f;
+}
+// rforce (src/HybridTaus.cu:85-98): four N(0,1) deviates by Box-Muller.
+__device__ __forceinline__ float4 gauss4(uint4 &s) {
+    float4 g;
+    float u1 = uint_to_unit(hybrid_taus(s));
+    float u2 = uint_to_unit(hybrid_taus(s));
+    float r = sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincosf(6.28318548f * u2, &sn, &cs);
+    g.x = r * sn;
+    g.y = r * cs;
+    u1 = uint_to_unit(hybrid_taus(s));
+    u2 = uint_to_unit(hybrid_taus(s));
+    r = sqrtf(-2.0f * logf(u1));
+    sincosf(6.28318548f * u2, &sn, &cs);
+    g.z = r * sn;
+    g.w = r * cs;
+    return g;
+}
+
+// --------------------------------------------------------------- frames
+struct Frame {
+    float4 p0, p1, p2, p3;
+};
+
+__device__ __forceinline__ float3 f3(const float4 &v) { return make_float3(v.x, v.y, v.z); }
+
+// Builds the four planes of a bead from its state.
+__device__ __forceinline__ Frame make_frame(const KParams &P, float x, float y, float z, float fi,
+                                            float theta, float psi) {
+    float sf, cf, st, ct, sp, cp;
+    sincosf(fi, &sf, &cf);
+    sincosf(theta, &st, &ct);
+    sincosf(psi, &sp, &cp);
+    const float m00 = cp * ct, m01 = cp * st * sf - sp * cf, m02 = cp * st * cf + sp * sf;
+    const float m10 = sp * ct, m11 = sp * st * sf + cp * cf, m12 = sp * st * cf - cp * sf;
+    const float m20 = -st, m21 = ct * sf, m22 = ct * cf;
+    Frame F;
+    F.p0 = make_float4(x, y, z, fi);
+    F.p1 = make_float4(m02, m12, m22, psi);
+    F.p2 = make_float4(m00 * P.p1x + m01 * P.p1y + m02 * P.p1z, m10 * P.p1x + m11 * P.p1y + m12 * P.p1z,
+                       m20 * P.p1x + m21 * P.p1y + m22 * P.p1z, theta);
+    F.p3 = make_float4(m00 * P.p2x + m01 * P.p2y + m02 * P.p2z, m10 * P.p2x + m11 * P.p2y + m12 * P.p2z,
+                       m20 * P.p2x + m21 * P.p2y + m22 * P.p2z, 0.0f);
+    return F;
+}
+
+__device__ __forceinline__ void store_frame(float4 *planes, int nb, int g, const Frame &F) {
+    planes[g] = F.p0;
+    planes[nb + g] = F.p1;
+    planes[2 * nb + g] = F.p2;
+    planes[3 * nb + g] = F.p3;
+}
+
+// ------------------------------------------------------------ potentials
+// Morse derivative / energy and Gaussian barrier (src/compute_cuda.cu:16-30).
+__device__ __forceinline__ float dmorse(float D, float a, float x) {
+    const float e = expf(-a * x);
+    return 2.0f * a * D * (1.0f - e) * e;
+}
+__device__ __forceinline__ float morse_en(float D, float a, float x) {
+    const float e = expf(-a * x);
+    return D * (1.0f - e) * (1.0f - e) - D;
+}
+__device__ __forceinline__ float dbarr(float a, float r, float w, float x) {
+    return -a * expf(-(x - r) * (x - r) / (2.0f * w * w)) * (x - r) / (w * w);
+}
+__device__ __forceinline__ float barr(float a, float r, float w, float x) {
+    return a * expf(-(x - r) * (x - r) / (2.0f * w * w));
+}
+
+// Centre distance in a fixed, contraction-free order shared with the CPU
+// oracle, so that LJ list membership is bit-identical for identical inputs.
+__device__ __forceinline__ float centre_dist(float4 a, float4 b) {
+    const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+}
+
+// Site-to-site vector d = (r_j + w_j) - (r_i + w_i), position difference first.
+__device__ __forceinline__ float3 site_delta(float4 ri, float4 rj, float3 wi, float3 wj) {
+    return make_float3(__fsub_rn(__fadd_rn(__fsub_rn(rj.x, ri.x), wj.x), wi.x),
+                       __fsub_rn(__fadd_rn(__fsub_rn(rj.y, ri.y), wj.y), wi.y),
+                       __fsub_rn(__fadd_rn(__fsub_rn(rj.z, ri.z), wj.z), wi.z));
+}
+__device__ __forceinline__ float norm3_rn(float3 d) {
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z)));
+}
+
+// ------------------------------------------------------ host entry points
+// (kernel launchers, defined in the .cu files)
+void launch_frames_from_coords(const KParams &P, const float *coords7, float4 *frame, cudaStream_t s);
+void launch_coords_from_frames(const KParams &P, const float4 *frame, float *coords7, cudaStream_t s);
+void launch_forces_to_coords(const KParams &P, const float4 *force, float *coords7, cudaStream_t s);
+void launch_rebuild(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
+void launch_step_plain(const KParams &P, const DevBuffers &B, bool keep_forces, cudaStream_t s);
+void launch_forces(const KParams &P, const DevBuffers &B, bool tea_prepare, cudaStream_t s);
+void launch_energy(const KParams &P, const DevBuffers &B, double *per_bead, double *partials,
+                   const int2 *work, int nwork, cudaStream_t s);
+void launch_energy_totals(const KParams &P, const double *partials, const int *work_first, double *per_traj,
+                          int *err, cudaStream_t s);
+void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
+void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s);
+void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
+void launch_set_flags(int nb, const uint8_t *extra, const int *gtp, const int *on_tubule, int *flags,
+                      cudaStream_t s);
+
+constexpr int kTile = 128;   // beads per CTA tile of the O(N^2) kernels
+
+}  // namespace mtg

@@ -1,0 +1,235 @@
+"""Python binding of the engine's C ABI (include/mtg.h) over ctypes.
+
+``Engine`` owns one ``mtg_engine`` handle.  Every call goes through
+mt_gb300/libmtg.so; there is no Python or CPU fallback: a missing library or a
+failed call raises ``MtgError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import MtgBatchTopology, MtgParams, MtgTopology, ptr
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmtg.so")
+
+EXPORTS = {
+    # name: (restype, argtypes)
+    "mtg_last_error_string": (C.c_char_p, []),
+    "mtg_derive_params": (C.c_int, [C.POINTER(MtgParams)]),
+    "mtg_create": (C.c_int, [C.POINTER(MtgParams), C.POINTER(MtgTopology), C.POINTER(C.c_void_p)]),
+    "mtg_create_batch": (C.c_int, [C.POINTER(MtgParams), C.POINTER(MtgBatchTopology), C.POINTER(C.c_void_p)]),
+    "mtg_destroy": (C.c_int, [C.c_void_p]),
+    "mtg_num_beads": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mtg_seed_rng": (C.c_int, [C.c_void_p, C.c_int]),
+    "mtg_download_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
+    "mtg_upload_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
+    "mtg_upload_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "mtg_download_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "mtg_set_keep_forces": (C.c_int, [C.c_void_p, C.c_int]),
+    "mtg_set_gtp": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "mtg_set_extra": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8)]),
+    "mtg_set_on_tubule": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "mtg_rebuild_pairs": (C.c_int, [C.c_void_p]),
+    "mtg_download_lists": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 6),
+    "mtg_list_capacity": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 3),
+    "mtg_compute_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "mtg_step": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int]),
+    "mtg_sync": (C.c_int, [C.c_void_p]),
+    "mtg_energies": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "mtg_tea_update": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+}
+
+_lib = None
+
+
+class MtgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Loads libmtg.so and declares every exported entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise MtgError(_abi.MTG_E_STATE, f"{path} is not built: run python -m mt_gb300.build")
+    lib = C.CDLL(path)
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code: int) -> int:
+    if code != 0:
+        raise MtgError(code, load().mtg_last_error_string().decode())
+    return code
+
+
+def derive_params(p: MtgParams) -> MtgParams:
+    check(load().mtg_derive_params(C.byref(p)))
+    return p
+
+
+class Engine:
+    """One batch on the GPU.  ``batch`` is a ``mt_gb300.synth.Batch``-like
+    object (CSR arrays); uniform batches go through ``mtg_create`` (the
+    reference layout), ragged ones through ``mtg_create_batch``."""
+
+    def __init__(self, batch, static_lists=None, force_ragged: bool = False):
+        self.lib = load()
+        self.batch = batch
+        self.params = batch.params
+        self._keep = []
+        h = C.c_void_p()
+        if batch.uniform_ntot and not force_ragged and static_lists is None:
+            n = batch.uniform_ntot
+            t = MtgTopology()
+            t.Ntot, t.Ntr = n, batch.ntraj
+            t.maxHarmonicPerMonomer = batch.max_h
+            hc = np.ascontiguousarray(batch.harmonic_count[:n])
+            hh = np.ascontiguousarray(batch.harmonic[:batch.max_h * n])
+            fx = np.ascontiguousarray(batch.fixed[:n])
+            mt = np.ascontiguousarray(batch.mon_type[:n])
+            self._keep += [hc, hh, fx, mt]
+            t.harmonicCount, t.harmonic = ptr(hc, C.c_int), ptr(hh, C.c_int)
+            t.maxLongitudinalPerMonomer, t.maxLateralPerMonomer = batch.max_long, batch.max_lat
+            t.maxLJPerMonomer = batch.max_lj
+            t.fixed, t.mon_type = ptr(fx, C.c_uint8), ptr(mt, C.c_int)
+            t.extra, t.gtp = ptr(batch.extra, C.c_uint8), ptr(batch.gtp, C.c_int)
+            t.on_tubule_cur, t.zs = ptr(batch.on_tubule, C.c_int), ptr(batch.zs, C.c_float)
+            check(self.lib.mtg_create(C.byref(batch.params), C.byref(t), C.byref(h)))
+        else:
+            t = MtgBatchTopology()
+            t.ntraj = batch.ntraj
+            t.offsets = ptr(batch.offsets, C.c_int)
+            t.maxHarmonicPerMonomer = batch.max_h
+            t.harmonicCount, t.harmonic = ptr(batch.harmonic_count, C.c_int), ptr(batch.harmonic, C.c_int)
+            t.maxLongitudinalPerMonomer, t.maxLateralPerMonomer = batch.max_long, batch.max_lat
+            t.maxLJPerMonomer = batch.max_lj
+            if static_lists is not None:
+                L = static_lists
+                self._keep += [L.long_count, L.lon, L.lat_count, L.lat]
+                t.longitudinalCount, t.longitudinal = ptr(L.long_count, C.c_int), ptr(L.lon, C.c_int)
+                t.lateralCount, t.lateral = ptr(L.lat_count, C.c_int), ptr(L.lat, C.c_int)
+            t.fixed, t.extra = ptr(batch.fixed, C.c_uint8), ptr(batch.extra, C.c_uint8)
+            t.mon_type, t.gtp = ptr(batch.mon_type, C.c_int), ptr(batch.gtp, C.c_int)
+            t.on_tubule_cur, t.zs = ptr(batch.on_tubule, C.c_int), ptr(batch.zs, C.c_float)
+            check(self.lib.mtg_create_batch(C.byref(batch.params), C.byref(t), C.byref(h)))
+        self.h = h
+        nb, nt = C.c_int(), C.c_int()
+        check(self.lib.mtg_num_beads(self.h, C.byref(nb), C.byref(nt)))
+        self.nb, self.nt = nb.value, nt.value
+
+    # ------------------------------------------------------------ lifecycle
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mtg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ----------------------------------------------------------------- state
+    def upload_state(self, coords: np.ndarray):
+        c = np.ascontiguousarray(coords, np.float32)
+        assert c.shape == (self.nb, 7)
+        check(self.lib.mtg_upload_state(self.h, ptr(c, C.c_float)))
+
+    def download_state(self, forces: bool = False):
+        r = np.zeros((self.nb, 7), np.float32)
+        f = np.zeros((self.nb, 7), np.float32) if forces else None
+        check(self.lib.mtg_download_state(self.h, ptr(r, C.c_float), ptr(f, C.c_float)))
+        return (r, f) if forces else r
+
+    def set_keep_forces(self, keep: bool = True):
+        check(self.lib.mtg_set_keep_forces(self.h, int(keep)))
+
+    def seed_rng(self, seed: int):
+        check(self.lib.mtg_seed_rng(self.h, seed))
+
+    def download_rng(self) -> np.ndarray:
+        s = np.zeros(8 * self.nb, np.uint32)
+        check(self.lib.mtg_download_rng(self.h, ptr(s, C.c_uint32)))
+        return s
+
+    def upload_rng(self, seeds: np.ndarray):
+        s = np.ascontiguousarray(seeds, np.uint32)
+        assert s.size == 8 * self.nb
+        check(self.lib.mtg_upload_rng(self.h, ptr(s, C.c_uint32)))
+
+    def set_gtp(self, gtp):
+        a = np.ascontiguousarray(gtp, np.int32)
+        check(self.lib.mtg_set_gtp(self.h, ptr(a, C.c_int)))
+
+    def set_extra(self, extra):
+        a = np.ascontiguousarray(extra, np.uint8)
+        check(self.lib.mtg_set_extra(self.h, ptr(a, C.c_uint8)))
+
+    def set_on_tubule(self, on):
+        a = np.ascontiguousarray(on, np.int32)
+        check(self.lib.mtg_set_on_tubule(self.h, ptr(a, C.c_int)))
+
+    # ---------------------------------------------------------------- compute
+    def rebuild_pairs(self):
+        check(self.lib.mtg_rebuild_pairs(self.h))
+
+    def lists(self):
+        """(counts, entries) per kind in the reference layout (bead-major, cap per bead)."""
+        ml, mt, mj = C.c_int(), C.c_int(), C.c_int()
+        check(self.lib.mtg_list_capacity(self.h, C.byref(ml), C.byref(mt), C.byref(mj)))
+        out = {}
+        a = [np.zeros(self.nb, np.int32), np.zeros(self.nb * mj.value, np.int32),
+             np.zeros(self.nb, np.int32), np.zeros(self.nb * ml.value, np.int32),
+             np.zeros(self.nb, np.int32), np.zeros(self.nb * mt.value, np.int32)]
+        check(self.lib.mtg_download_lists(self.h, *[ptr(x, C.c_int) for x in a]))
+        out["lj"] = (a[0], a[1], mj.value)
+        out["long"] = (a[2], a[3], ml.value)
+        out["lat"] = (a[4], a[5], mt.value)
+        return out
+
+    def list_of_lists(self, kind: str):
+        cnt, arr, cap = self.lists()[kind]
+        return [arr[cap * i: cap * i + cnt[i]].tolist() for i in range(self.nb)]
+
+    def compute_forces(self) -> np.ndarray:
+        f = np.zeros((self.nb, 7), np.float32)
+        check(self.lib.mtg_compute_forces(self.h, ptr(f, C.c_float)))
+        return f
+
+    def step(self, first_step: int, nsteps: int):
+        check(self.lib.mtg_step(self.h, C.c_longlong(first_step), C.c_int(nsteps)))
+
+    def step_raw(self, first_step: int, nsteps: int) -> int:
+        """mtg_step returning its status instead of raising."""
+        return self.lib.mtg_step(self.h, C.c_longlong(first_step), C.c_int(nsteps))
+
+    def energies(self, per_bead: bool = False):
+        pt = np.zeros((self.nt, 7), np.float64)
+        pb = np.zeros((self.nb, 7), np.float64) if per_bead else None
+        check(self.lib.mtg_energies(self.h, ptr(pb, C.c_double), ptr(pt, C.c_double)))
+        return (pt, pb) if per_bead else pt
+
+    def tea_update(self):
+        eps = np.zeros(self.nt, np.float64)
+        beta = np.zeros(self.nt, np.float32)
+        ci = np.zeros((self.nb, 4), np.float32)
+        rc = self.lib.mtg_tea_update(self.h, ptr(eps, C.c_double), ptr(beta, C.c_float), ptr(ci, C.c_float))
+        return eps, beta, ci, rc

@@ -1,0 +1,202 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle on
+identical inputs and seeds.
+
+Bars: integer/index work bit-exact (HybridTaus streams, ran2 seeds, pair
+lists on states whose list decisions sit > 2e-4 nm from every cutoff);
+forces and energies within 1e-5 relative (norm over the array, per
+component) in FP32; multi-step states within the FP32 drift stated per test.
+"""
+import numpy as np
+import pytest
+
+from helpers import rel_norm, small_system, system_with_margin
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-5
+
+
+def make_engine(engine_mod, b, **kw):
+    e = engine_mod.Engine(b, **kw)
+    e.upload_state(b.coords)
+    return e
+
+
+def test_seeds_match_reference_ran2(engine_mod, oracle_lib):
+    b = small_system(seed=2)
+    e = make_engine(engine_mod, b)
+    o = oracle_lib.Oracle("orc")
+    assert np.array_equal(e.download_rng(), o.generate_seeds(b.params.rseed, 2 * b.nbeads))
+    e.close()
+
+
+@pytest.mark.parametrize("ragged", [False, True])
+def test_lists_bit_exact(engine_mod, oracle_lib, ragged):
+    b = system_with_margin(seed=5, ntr=3)
+    e = make_engine(engine_mod, b, force_ragged=ragged)
+    e.rebuild_pairs()
+    L = oracle_lib.Oracle("orc").lists(b, b.coords)
+    for k in ("lj", "long", "lat"):
+        assert e.list_of_lists(k) == L.as_lists(k), k
+    e.close()
+
+
+def test_lists_golden(engine_mod):
+    """Lists of the fixture written from the reference's own pairs/LJ kernels."""
+    from helpers import golden_batch
+    d = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "plain.npz"))
+    b = golden_batch(d)
+    e = make_engine(engine_mod, b)
+    e.rebuild_pairs()
+    got = e.lists()
+    for kind, kc, ka in (("lj", "lj_count", "lj"), ("long", "long_count", "lon"), ("lat", "lat_count", "lat")):
+        cnt, arr, cap = got[kind]
+        assert np.array_equal(cnt, d[kc]), kind
+        for i in range(b.nbeads):
+            assert np.array_equal(arr[cap * i:cap * i + cnt[i]], d[ka][cap * i:cap * i + cnt[i]]), (kind, i)
+    e.close()
+
+
+@pytest.mark.parametrize("case", ["default", "walls_barrier_seam", "gdp_ontubule", "static_lists"])
+def test_forces_and_energies(engine_mod, oracle_lib, case):
+    over = {}
+    if case == "walls_barrier_seam":
+        over = dict(is_wall=1, rep_r=9.0, barrier=1, seam_coeff=1.7)
+    b = system_with_margin(seed=8, **over)
+    if case == "gdp_ontubule":
+        rng = np.random.default_rng(4)
+        b.gtp[:] = rng.integers(0, 2, b.nbeads)
+        b.on_tubule[:] = rng.integers(0, 2, b.nbeads)
+        b.params.barrier = 1
+    o32, o64 = oracle_lib.Oracle("orc", "f32"), oracle_lib.Oracle("orc", "f64")
+    L = o32.lists(b, b.coords)
+    if case == "static_lists":
+        b.params.is_assembly = 0
+        e = make_engine(engine_mod, b, static_lists=L)
+        e.rebuild_pairs()   # LJ only; the static lists stay
+    else:
+        e = make_engine(engine_mod, b)
+        e.rebuild_pairs()
+    f = e.compute_forces()
+    fo, f64 = o32.forces(b, b.coords, L), o64.forces(b, b.coords, L)
+    for c in range(6):
+        err = rel_norm(f[:, c], fo[:, c])
+        assert err < FORCE_RTOL, (c, err, rel_norm(f[:, c], f64[:, c]))
+    tot, per = e.energies(per_bead=True)
+    eo = o32.energies(b, b.coords, L)
+    for t in range(b.ntraj):
+        sl = slice(int(b.offsets[t]), int(b.offsets[t + 1]))
+        np.testing.assert_allclose(tot[t], eo[sl].sum(0), rtol=1e-5, atol=1e-3)
+    assert rel_norm(per, eo) < 1e-5
+    e.close()
+
+
+def test_one_step_matches_oracle(engine_mod, oracle_lib):
+    b = system_with_margin(seed=11)
+    o = oracle_lib.Oracle("orc")
+    seeds = o.generate_seeds(b.params.rseed, 2 * b.nbeads)
+    e = make_engine(engine_mod, b)
+    e.step(0, 1)
+    x = e.download_state()
+    xo, _, so, _, st, _, _ = o.run(b, b.coords, seeds, 0, 1)
+    assert st == 0
+    assert np.array_equal(e.download_rng(), so)          # streams consumed by moving beads only
+    np.testing.assert_allclose(x[:, :6], xo[:, :6], rtol=0, atol=5e-5)
+
+
+def test_zero_temperature_trajectory(engine_mod, oracle_lib):
+    """Temp = 0 makes the update deterministic (varR = varTheta = 0); 30 steps
+    with three list rebuilds stay within FP32 drift of the oracle."""
+    b = system_with_margin(seed=12, Temp=0.0)
+    o = oracle_lib.Oracle("orc")
+    seeds = o.generate_seeds(b.params.rseed, 2 * b.nbeads)
+    e = make_engine(engine_mod, b)
+    e.step(0, 30)
+    x = e.download_state()
+    xo = o.run(b, b.coords, seeds, 0, 30)[0]
+    np.testing.assert_allclose(x[:, :3], xo[:, :3], rtol=0, atol=2e-3)
+    np.testing.assert_allclose(x[:, 3:6], xo[:, 3:6], rtol=0, atol=2e-3)
+
+
+def test_graph_replay_equals_single_steps(engine_mod):
+    b = small_system(seed=13)
+    e1 = make_engine(engine_mod, b)
+    e1.step(0, 25)                       # two graph replays + tail
+    e2 = make_engine(engine_mod, b)
+    for s in range(25):
+        e2.step(s, 1)
+    assert np.array_equal(e1.download_state(), e2.download_state())
+    assert np.array_equal(e1.download_rng(), e2.download_rng())
+
+
+def test_ragged_batch_forces(engine_mod, oracle_lib):
+    from mt_gb300 import synth
+    p = synth.default_params(seed=3)
+    b = synth.ragged_batch(p, 5, seed=3, pf_range=(4, 14), free_range=(0, 60), cube=50.0, radius=8.12,
+                           psi_mode="make_mt", thermal=0.05)
+    e = make_engine(engine_mod, b)
+    e.rebuild_pairs()
+    o = oracle_lib.Oracle("orc")
+    L = o.lists(b, b.coords)
+    f = e.compute_forces()
+    fo = o.forces(b, b.coords, L)
+    for c in range(6):
+        assert rel_norm(f[:, c], fo[:, c]) < FORCE_RTOL
+    tot = e.energies()
+    eo = o.energies(b, b.coords, L)
+    for t in range(b.ntraj):
+        sl = slice(int(b.offsets[t]), int(b.offsets[t + 1]))
+        np.testing.assert_allclose(tot[t], eo[sl].sum(0), rtol=1e-5, atol=1e-3)
+
+
+def test_tea_update_and_step(engine_mod, oracle_lib):
+    b = system_with_margin(seed=14, tea=True, tea_epsilon_freq=1)
+    o32, o64 = oracle_lib.Oracle("orc", "f32"), oracle_lib.Oracle("orc", "f64")
+    e = make_engine(engine_mod, b)
+    eps, beta, ci, rc = e.tea_update()
+    assert rc == 0
+    ci_o, eps_o = o32.tea_epsilon(b, b.coords)
+    eps_t, beta_o, st = o32.tea_beta(b, eps_o)
+    assert rel_norm(ci[:, :3], ci_o[:, :3]) < 1e-5
+    np.testing.assert_allclose(eps, eps_t, rtol=1e-5)
+    np.testing.assert_allclose(beta, beta_o, rtol=1e-5)
+    # one TEA step from identical state and seeds
+    seeds = o32.generate_seeds(b.params.rseed, 2 * b.nbeads)
+    e2 = make_engine(engine_mod, b)
+    e2.step(0, 1)
+    x = e2.download_state()
+    xo, _, so, _, st, _, _ = o32.run(b, b.coords, seeds, 0, 1)
+    assert st == 0
+    assert np.array_equal(e2.download_rng(), so)         # TEA draws both streams of every bead
+    np.testing.assert_allclose(x[:, :6], xo[:, :6], rtol=0, atol=1e-4)
+
+
+def test_overflow_reported(engine_mod):
+    b = small_system(seed=15)
+    b.max_lj = 4
+    e = make_engine(engine_mod, b)
+    with pytest.raises(engine_mod.MtgError) as ex:
+        e.rebuild_pairs()
+    assert ex.value.code == -3
+
+
+def test_nonfinite_energy_reported(engine_mod):
+    b = small_system(seed=16)
+    c = b.coords.copy()
+    c[5, 0] = np.nan
+    e = engine_mod.Engine(b)
+    e.upload_state(c)
+    e.rebuild_pairs()
+    with pytest.raises(engine_mod.MtgError) as ex:
+        e.energies()
+    assert ex.value.code == -4
+    # the context stays usable
+    e.upload_state(b.coords)
+    e.rebuild_pairs()
+    assert np.all(np.isfinite(e.energies()))
+
+
+def test_tea_epsmax_reported(engine_mod):
+    b = small_system(seed=17, tea=True, tea_epsilon_freq=1, tea_epsmax=1e-6)
+    e = make_engine(engine_mod, b)
+    assert e.step_raw(0, 1) == -5
