@@ -20,6 +20,7 @@
 #ifndef MTG_H_
 #define MTG_H_
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -78,6 +79,9 @@ typedef struct {
     float tea_epsmax;
     /* HybridTaus seed (src/parameters.h:248) */
     int rseed;
+    /* CUDA device of the engine (Parameters::device, src/parameters.h:263;
+     * the reference calls cudaSetDevice(par.device) in initIntegration) */
+    int device;
 } mtg_params;
 
 /* Topology of a uniform batch, in the reference's layout (Topology,
@@ -222,6 +226,27 @@ int mtg_energies(mtg_engine *e, double *per_bead, double *per_traj);
  * floats may be NULL.  ci_out [nbeads*4] floats (may be NULL): the per-bead
  * row sums of squared normalised tensor entries (d_ci). */
 int mtg_tea_update(mtg_engine *e, double *eps_out, float *beta_out, float *ci_out);
+
+/* ---- measurement ------------------------------------------------------- */
+/* mtg_step bracketed by CUDA events recorded on the engine's stream;
+ * *device_ms = the device time between them.  No reference counterpart (the
+ * reference reports CPU clock() steps/s, src/timer.cpp:24-34). */
+int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *device_ms);
+
+/* Per-kernel timing: while enabled, every kernel launch of mtg_step is
+ * bracketed by its own pair of CUDA events; after each mtg_step call the
+ * durations of that call's launches are added to per-kind totals.  (When a
+ * call replays a pair-list period graph more than once only its last replay
+ * is counted; the call count below says how many launches were timed.)
+ * Kinds: 0 pair-list rebuild, 1 fused plain step, 2 forces (+ TEA random
+ * forces), 3 TEA epsilon pass, 4 TEA beta reduction, 5 TEA mobility step. */
+#define MTG_KERNEL_KINDS 6
+int mtg_set_kernel_timing(mtg_engine *e, int on);
+int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int reset);
+
+/* Page-locked host buffers for fast state transfers (cudaHostAlloc). */
+int mtg_host_alloc(void **ptr, size_t bytes);
+int mtg_host_free(void *ptr);
 
 #ifdef __cplusplus
 }

@@ -56,6 +56,7 @@ class MtgParams(C.Structure):
         ("hdi_on", _i), ("tea_a", _f), ("tea_epsilon_freq", _i), ("tea_capricious", _i),
         ("tea_epsmax", _f),
         ("rseed", _i),
+        ("device", _i),
     ]
 
     def as_dict(self):

@@ -127,9 +127,21 @@ struct mtg_engine {
     void *stage_host = nullptr;    // pinned mirror of stage
     uint8_t *stage_u8 = nullptr;
     int *stage_i = nullptr;
+    int device = 0;
     // graphs: [parity]
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_period = 0;
+    // per-kernel timing (see mtg_set_kernel_timing)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_a, ev_b;
+    std::vector<int> ev_kind;
+    int graph_slot_base[2] = {0, 0}, graph_slot_count[2] = {0, 0};
+    int direct_base = 0, direct_next = 0, capture_next = 0;
+    bool capturing = false;
+    std::vector<int> used_slots;
+    double kt_total[MTG_KERNEL_KINDS] = {0};
+    long long kt_count[MTG_KERNEL_KINDS] = {0};
+    cudaEvent_t call_a = nullptr, call_b = nullptr;
 
     DevBuffers bufs() const {
         DevBuffers b{};
@@ -254,6 +266,37 @@ void destroy_graphs(mtg_engine *e) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+    e->direct_base = 0;
+    e->graph_slot_count[0] = e->graph_slot_count[1] = 0;
+}
+
+// Event slot for one timed launch (created outside any stream capture).
+int timing_slot(mtg_engine *e, int kind) {
+    int &next = e->capturing ? e->capture_next : e->direct_next;
+    const int s = next++;
+    while ((int)e->ev_a.size() <= s) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        e->ev_a.push_back(a);
+        e->ev_b.push_back(b);
+        e->ev_kind.push_back(0);
+    }
+    e->ev_kind[s] = kind;
+    if (!e->capturing) e->used_slots.push_back(s);
+    return s;
+}
+
+template <class F>
+void timed_launch(mtg_engine *e, int kind, F &&launch) {
+    if (!e->timing) {
+        launch();
+        return;
+    }
+    const int s = timing_slot(e, kind);
+    cudaEventRecord(e->ev_a[s], e->stream);
+    launch();
+    cudaEventRecord(e->ev_b[s], e->stream);
 }
 
 // Enqueues one step of the loop of compute() (src/compute_cuda.cu:1137-1238)
@@ -261,20 +304,43 @@ void destroy_graphs(mtg_engine *e) {
 void enqueue_step(mtg_engine *e, long long step) {
     const mtg_params &p = e->p;
     if (step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
-        launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+        timed_launch(e, 0, [&] { launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream); });
         e->lists_valid = true;
     }
     if (p.hdi_on) {
-        launch_forces(e->kp, e->bufs(), true, e->stream);
+        timed_launch(e, 2, [&] { launch_forces(e->kp, e->bufs(), true, e->stream); });
         if (step % p.tea_epsilon_freq == 0) {
-            launch_tea_eps(e->kp, e->bufs(), e->work, e->nwork, e->stream);
-            launch_tea_beta(e->kp, e->bufs(), p.tea_capricious, p.tea_epsmax, e->stream);
+            timed_launch(e, 3, [&] { launch_tea_eps(e->kp, e->bufs(), e->work, e->nwork, e->stream); });
+            timed_launch(e, 4, [&] { launch_tea_beta(e->kp, e->bufs(), p.tea_capricious, p.tea_epsmax, e->stream); });
         }
-        launch_tea_step(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+        timed_launch(e, 5, [&] { launch_tea_step(e->kp, e->bufs(), e->work, e->nwork, e->stream); });
     } else {
-        launch_step_plain(e->kp, e->bufs(), e->keep_forces, e->stream);
+        timed_launch(e, 1, [&] { launch_step_plain(e->kp, e->bufs(), e->keep_forces, e->stream); });
     }
     e->cur ^= 1;
+}
+
+// Creates event pairs up to slot `upto` (never called during a capture).
+void reserve_slots(mtg_engine *e, int upto) {
+    while ((int)e->ev_a.size() < upto) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        e->ev_a.push_back(a);
+        e->ev_b.push_back(b);
+        e->ev_kind.push_back(0);
+    }
+}
+
+void collect_timing(mtg_engine *e) {
+    for (int s : e->used_slots) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e->ev_a[s], e->ev_b[s]) == cudaSuccess) {
+            e->kt_total[e->ev_kind[s]] += ms;
+            e->kt_count[e->ev_kind[s]]++;
+        }
+    }
+    e->used_slots.clear();
 }
 
 long long lcm_ll(long long a, long long b) {
@@ -328,8 +394,10 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
         return fail(MTG_E_CONFIG, "static (non-assembly) mode needs the longitudinal and lateral lists");
     const int nb = (int)nbl;
 
+    if (cudaSetDevice(p->device) != cudaSuccess) return fail(MTG_E_CUDA, "cudaSetDevice(%d) failed", p->device);
     auto *e = new mtg_engine();
     e->p = *p;
+    e->device = p->device;
     e->nb = nb;
     e->nt = nt;
     e->h_off.assign(t->offsets, t->offsets + nt + 1);
@@ -532,6 +600,7 @@ int mtg_create(const mtg_params *p, const mtg_topology *t, mtg_engine **out) {
 
 int mtg_destroy(mtg_engine *e) {
     if (!e) return MTG_OK;
+    cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     destroy_graphs(e);
     void *ptrs[] = {e->off, e->traj, e->flags, e->harm, e->zs, e->frame[0], e->frame[1], e->force, e->seeds,
@@ -541,6 +610,10 @@ int mtg_destroy(mtg_engine *e) {
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (e->stage_host) cudaFreeHost(e->stage_host);
+    for (auto ev : e->ev_a) cudaEventDestroy(ev);
+    for (auto ev : e->ev_b) cudaEventDestroy(ev);
+    if (e->call_a) cudaEventDestroy(e->call_a);
+    if (e->call_b) cudaEventDestroy(e->call_b);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
     return MTG_OK;
@@ -548,6 +621,7 @@ int mtg_destroy(mtg_engine *e) {
 
 int mtg_num_beads(const mtg_engine *e, int *nbeads, int *ntraj) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     if (nbeads) *nbeads = e->nb;
     if (ntraj) *ntraj = e->nt;
     return MTG_OK;
@@ -555,6 +629,7 @@ int mtg_num_beads(const mtg_engine *e, int *nbeads, int *ntraj) {
 
 int mtg_list_capacity(const mtg_engine *e, int *max_long, int *max_lat, int *max_lj) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     if (max_long) *max_long = e->kp.maxLong;
     if (max_lat) *max_lat = e->kp.maxLat;
     if (max_lj) *max_lj = e->kp.maxLJ;
@@ -563,6 +638,7 @@ int mtg_list_capacity(const mtg_engine *e, int *max_long, int *max_lat, int *max
 
 int mtg_seed_rng(mtg_engine *e, int rseed) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     std::vector<uint32_t> s;
     make_seeds(rseed, 2 * (size_t)e->nb, s);
     return mtg_upload_rng(e, s.data());
@@ -570,6 +646,7 @@ int mtg_seed_rng(mtg_engine *e, int rseed) {
 
 int mtg_upload_rng(mtg_engine *e, const uint32_t *seeds) {
     if (!e || !seeds) return fail(MTG_E_CONFIG, "engine or seeds is NULL");
+    cudaSetDevice(e->device);
     CK(cudaMemcpyAsync(e->seeds, seeds, sizeof(uint4) * 2 * (size_t)e->nb, cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return MTG_OK;
@@ -577,6 +654,7 @@ int mtg_upload_rng(mtg_engine *e, const uint32_t *seeds) {
 
 int mtg_download_rng(mtg_engine *e, uint32_t *seeds) {
     if (!e || !seeds) return fail(MTG_E_CONFIG, "engine or seeds is NULL");
+    cudaSetDevice(e->device);
     CK(cudaMemcpyAsync(seeds, e->seeds, sizeof(uint4) * 2 * (size_t)e->nb, cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return MTG_OK;
@@ -584,6 +662,7 @@ int mtg_download_rng(mtg_engine *e, uint32_t *seeds) {
 
 int mtg_upload_state(mtg_engine *e, const float *r) {
     if (!e || !r) return fail(MTG_E_CONFIG, "engine or r is NULL");
+    cudaSetDevice(e->device);
     CK(cudaMemcpyAsync(e->stage, r, sizeof(float) * 7 * (size_t)e->nb, cudaMemcpyHostToDevice, e->stream));
     launch_frames_from_coords(e->kp, e->stage, e->frame[e->cur], e->stream);
     CK(cudaGetLastError());
@@ -594,6 +673,7 @@ int mtg_upload_state(mtg_engine *e, const float *r) {
 
 int mtg_download_state(mtg_engine *e, float *r, float *f) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     const size_t bytes = sizeof(float) * 7 * (size_t)e->nb;
     if (r) {
         launch_coords_from_frames(e->kp, e->frame[e->cur], e->stage, e->stream);
@@ -611,6 +691,7 @@ int mtg_download_state(mtg_engine *e, float *r, float *f) {
 
 static int set_flag_array(mtg_engine *e, const uint8_t *extra, const int *gtp, const int *ontub) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     const size_t nb = e->nb;
     if (extra) CK(cudaMemcpyAsync(e->stage_u8, extra, nb, cudaMemcpyHostToDevice, e->stream));
     if (gtp || ontub) CK(cudaMemcpyAsync(e->stage_i, gtp ? gtp : ontub, sizeof(int) * nb, cudaMemcpyHostToDevice, e->stream));
@@ -636,6 +717,7 @@ int mtg_set_on_tubule(mtg_engine *e, const int *on_tubule_cur) {
 
 int mtg_set_keep_forces(mtg_engine *e, int keep) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     if (e->keep_forces != (keep != 0)) destroy_graphs(e);
     e->keep_forces = keep != 0;
     return MTG_OK;
@@ -643,6 +725,7 @@ int mtg_set_keep_forces(mtg_engine *e, int keep) {
 
 int mtg_rebuild_pairs(mtg_engine *e) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
     if (e->p.lj_on || e->p.is_assembly) launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream);
     CK(cudaGetLastError());
@@ -652,6 +735,7 @@ int mtg_rebuild_pairs(mtg_engine *e) {
 
 int mtg_download_lists(mtg_engine *e, int *lj_count, int *lj, int *long_count, int *lon, int *lat_count, int *lat) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     const size_t nb = e->nb;
     struct L {
         int *cnt_dev, *arr_dev, cap;
@@ -677,6 +761,7 @@ int mtg_download_lists(mtg_engine *e, int *lj_count, int *lj, int *long_count, i
 
 int mtg_compute_forces(mtg_engine *e, float *f) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
     launch_forces(e->kp, e->bufs(), false, e->stream);
     CK(cudaGetLastError());
@@ -685,8 +770,9 @@ int mtg_compute_forces(mtg_engine *e, float *f) {
     return f ? mtg_download_state(e, nullptr, f) : MTG_OK;
 }
 
-int mtg_step(mtg_engine *e, long long first_step, int nsteps) {
+static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
     if (nsteps < 0 || first_step < 0) return fail(MTG_E_CONFIG, "negative step range");
     const mtg_params &p = e->p;
@@ -697,6 +783,9 @@ int mtg_step(mtg_engine *e, long long first_step, int nsteps) {
         destroy_graphs(e);
         e->graph_period = (int)period;
     }
+    const int max_launch_per_step = 5;
+    e->direct_next = e->direct_base;
+    e->used_slots.clear();
     long long s = first_step;
     const long long end = first_step + nsteps;
     while (s < end) {
@@ -704,14 +793,38 @@ int mtg_step(mtg_engine *e, long long first_step, int nsteps) {
             cudaGraphExec_t &ge = e->graph[e->cur];
             if (!ge) {
                 const int cur0 = e->cur;
+                if (e->timing) {
+                    // graph slots live below direct_base; direct launches above it
+                    const int base = e->direct_base;
+                    const int count = (int)period * max_launch_per_step;
+                    reserve_slots(e, base + count);
+                    e->graph_slot_base[cur0] = base;
+                    e->graph_slot_count[cur0] = 0;
+                    e->direct_base = base + count;
+                    e->direct_next = e->direct_base;
+                    e->capture_next = base;
+                }
                 cudaGraph_t g;
-                CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-                for (long long k = 0; k < period; k++) enqueue_step(e, k);
-                CK(cudaStreamEndCapture(e->stream, &g));
+                e->capturing = true;
+                cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+                if (ce == cudaSuccess) {
+                    for (long long k = 0; k < period; k++) enqueue_step(e, k);
+                    ce = cudaStreamEndCapture(e->stream, &g);
+                }
+                e->capturing = false;
+                if (ce != cudaSuccess) return fail(MTG_E_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+                if (e->timing) e->graph_slot_count[cur0] = e->capture_next - e->graph_slot_base[cur0];
                 e->cur = cur0;
                 CK(cudaGraphInstantiate(&ge, g, 0));
                 cudaGraphDestroy(g);
             }
+            if (e->timing)
+                for (int k = 0; k < e->graph_slot_count[e->cur]; k++) {
+                    const int slot = e->graph_slot_base[e->cur] + k;
+                    bool seen = false;
+                    for (int u : e->used_slots) seen |= (u == slot);
+                    if (!seen) e->used_slots.push_back(slot);
+                }
             CK(cudaGraphLaunch(ge, e->stream));
             if (period & 1) e->cur ^= 1;
             if (p.lj_on || p.is_assembly) e->lists_valid = true;
@@ -722,16 +835,77 @@ int mtg_step(mtg_engine *e, long long first_step, int nsteps) {
         }
     }
     CK(cudaGetLastError());
-    return check_errors(e);
+    return MTG_OK;
+}
+
+int mtg_step(mtg_engine *e, long long first_step, int nsteps) {
+    if (e) cudaSetDevice(e->device);
+    int rc = enqueue_range(e, first_step, nsteps);
+    if (rc) return rc;
+    rc = check_errors(e);
+    if (e->timing) collect_timing(e);
+    return rc;
+}
+
+int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *device_ms) {
+    if (!e || !device_ms) return fail(MTG_E_CONFIG, "engine or device_ms is NULL");
+    cudaSetDevice(e->device);
+    if (!e->call_a) {
+        CK(cudaEventCreate(&e->call_a));
+        CK(cudaEventCreate(&e->call_b));
+    }
+    CK(cudaEventRecord(e->call_a, e->stream));
+    int rc = enqueue_range(e, first_step, nsteps);
+    if (rc) return rc;
+    CK(cudaEventRecord(e->call_b, e->stream));
+    rc = check_errors(e);
+    if (e->timing) collect_timing(e);
+    CK(cudaEventElapsedTime(device_ms, e->call_a, e->call_b));
+    return rc;
+}
+
+int mtg_set_kernel_timing(mtg_engine *e, int on) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
+    if (e->timing != (on != 0)) destroy_graphs(e);
+    e->timing = on != 0;
+    return MTG_OK;
+}
+
+int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int reset) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
+    for (int k = 0; k < MTG_KERNEL_KINDS; k++) {
+        if (total_ms) total_ms[k] = e->kt_total[k];
+        if (launches) launches[k] = e->kt_count[k];
+        if (reset) {
+            e->kt_total[k] = 0;
+            e->kt_count[k] = 0;
+        }
+    }
+    return MTG_OK;
+}
+
+int mtg_host_alloc(void **ptr, size_t bytes) {
+    if (!ptr) return fail(MTG_E_CONFIG, "ptr is NULL");
+    CK(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocPortable));
+    return MTG_OK;
+}
+
+int mtg_host_free(void *ptr) {
+    if (ptr) CK(cudaFreeHost(ptr));
+    return MTG_OK;
 }
 
 int mtg_sync(mtg_engine *e) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     return check_errors(e);
 }
 
 int mtg_energies(mtg_engine *e, double *per_bead, double *per_traj) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
     int rc;
     if (per_bead && !e->en_bead && (rc = dalloc(&e->en_bead, 7 * (size_t)e->nb)) != 0) return rc;
@@ -747,6 +921,7 @@ int mtg_energies(mtg_engine *e, double *per_bead, double *per_traj) {
 
 int mtg_tea_update(mtg_engine *e, double *eps_out, float *beta_out, float *ci_out) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    cudaSetDevice(e->device);
     if (!e->p.hdi_on) return fail(MTG_E_STATE, "engine created without hdi_on");
     if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
     launch_tea_eps(e->kp, e->bufs(), e->work, e->nwork, e->stream);

@@ -41,7 +41,14 @@ EXPORTS = {
     "mtg_sync": (C.c_int, [C.c_void_p]),
     "mtg_energies": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mtg_tea_update": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "mtg_step_timed": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_float)]),
+    "mtg_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "mtg_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
+    "mtg_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
+    "mtg_host_free": (C.c_int, [C.c_void_p]),
 }
+
+KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step")
 
 _lib = None
 
@@ -72,6 +79,24 @@ def check(code: int) -> int:
     if code != 0:
         raise MtgError(code, load().mtg_last_error_string().decode())
     return code
+
+
+class PinnedArray:
+    """numpy view of a page-locked host buffer from mtg_host_alloc."""
+
+    def __init__(self, shape, dtype):
+        self.lib = load()
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.ptr = C.c_void_p()
+        check(self.lib.mtg_host_alloc(C.byref(self.ptr), n))
+        buf = (C.c_char * n).from_address(self.ptr.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            self.lib.mtg_host_free(self.ptr)
+            self.ptr = None
 
 
 def derive_params(p: MtgParams) -> MtgParams:
@@ -220,6 +245,22 @@ class Engine:
     def step_raw(self, first_step: int, nsteps: int) -> int:
         """mtg_step returning its status instead of raising."""
         return self.lib.mtg_step(self.h, C.c_longlong(first_step), C.c_int(nsteps))
+
+    def step_timed(self, first_step: int, nsteps: int) -> float:
+        """mtg_step between two CUDA events on the engine's stream; returns device ms."""
+        ms = C.c_float()
+        check(self.lib.mtg_step_timed(self.h, C.c_longlong(first_step), C.c_int(nsteps), C.byref(ms)))
+        return ms.value
+
+    def set_kernel_timing(self, on: bool = True):
+        check(self.lib.mtg_set_kernel_timing(self.h, int(on)))
+
+    def kernel_times(self, reset: bool = False):
+        """{kind: (total_ms, launches)} of the timed kernel launches."""
+        t = (C.c_double * len(KERNEL_KINDS))()
+        n = (C.c_longlong * len(KERNEL_KINDS))()
+        check(self.lib.mtg_kernel_times(self.h, t, n, int(reset)))
+        return {k: (t[i], n[i]) for i, k in enumerate(KERNEL_KINDS)}
 
     def energies(self, per_bead: bool = False):
         pt = np.zeros((self.nt, 7), np.float64)

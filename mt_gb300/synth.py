@@ -159,46 +159,53 @@ def make_lattice(n_mon: int, radius: float = 12.0, psi_mode: str = "zero", tail:
 
 
 def place_free_dimers(rng, existing: np.ndarray, n_dimers: int, lo, hi, spacing: float = 4.0):
-    """Seeded rejection placement of CA/CB dimers keeping >= spacing between all centres."""
+    """Seeded rejection placement of CA/CB dimers keeping >= spacing between all centres.
+
+    Candidates are drawn in batches; a candidate is rejected when either bead
+    is closer than ``spacing`` to an accepted bead, and conflicts inside a
+    batch are resolved in draw order."""
     from scipy.spatial import cKDTree
 
-    pts = [existing.astype(np.float64)] if len(existing) else []
-    placed_ca, placed_ang = [], []
     lo = np.asarray(lo, np.float64)
     hi = np.asarray(hi, np.float64)
-    tries = 0
+    acc_pts = existing.astype(np.float64).reshape(-1, 3)
+    placed_ca = np.zeros((0, 3))
+    placed_ang = np.zeros((0, 3))
+    rounds = 0
     while len(placed_ca) < n_dimers:
-        tries += 1
-        if tries > 10000:
+        rounds += 1
+        if rounds > 200:
             raise RuntimeError("free tubulin placement failed: box too dense")
-        allpts = np.concatenate(pts) if pts else np.zeros((0, 3))
-        tree = cKDTree(allpts) if len(allpts) else None
-        k = max(64, 2 * (n_dimers - len(placed_ca)))
+        need = n_dimers - len(placed_ca)
+        k = max(64, int(need * 1.5))
         ca = rng.uniform(lo, hi, size=(k, 3))
         ang = rng.uniform(-math.pi, math.pi, size=(k, 3))
         cb = ca + 2 * R_MON * _rot_z_axis(ang[:, 0], ang[:, 1], ang[:, 2])
         ok = np.ones(k, bool)
-        if tree is not None:
+        if len(acc_pts):
+            tree = cKDTree(acc_pts)
             d1, _ = tree.query(ca)
             d2, _ = tree.query(cb)
             ok &= (d1 >= spacing) & (d2 >= spacing)
-        batch = []
-        for idx in np.nonzero(ok)[0]:
-            if len(placed_ca) + len(batch) >= n_dimers:
+        idx = np.nonzero(ok)[0]
+        pts = np.concatenate([ca[idx], cb[idx]])
+        owner = np.concatenate([np.arange(len(idx)), np.arange(len(idx))])
+        pairs = cKDTree(pts).query_pairs(spacing, output_type="ndarray") if len(pts) else np.zeros((0, 2), int)
+        conflict = [[] for _ in range(len(idx))]
+        for a, b in pairs:
+            oa, ob = owner[a], owner[b]
+            if oa != ob:
+                conflict[max(oa, ob)].append(min(oa, ob))
+        take = np.zeros(len(idx), bool)
+        for c in range(len(idx)):
+            if take.sum() >= need:
                 break
-            good = True
-            for j in batch:
-                for u in (ca[idx], cb[idx]):
-                    for v in (ca[j], cb[j]):
-                        if np.sum((u - v) ** 2) < spacing * spacing:
-                            good = False
-            if good:
-                batch.append(idx)
-        for idx in batch:
-            placed_ca.append(ca[idx])
-            placed_ang.append(ang[idx])
-            pts.append(np.stack([ca[idx], cb[idx]]))
-    return np.array(placed_ca).reshape(-1, 3), np.array(placed_ang).reshape(-1, 3)
+            take[c] = not any(take[o] for o in conflict[c])
+        sel = idx[take]
+        placed_ca = np.concatenate([placed_ca, ca[sel]])
+        placed_ang = np.concatenate([placed_ang, ang[sel]])
+        acc_pts = np.concatenate([acc_pts, ca[sel], cb[sel]])
+    return placed_ca[:n_dimers], placed_ang[:n_dimers]
 
 
 def make_trajectory(n_mon: int, n_free: int, seed: int, radius: float = 12.0, psi_mode: str = "zero",

@@ -16,6 +16,16 @@
 #define M_PI 3.14159265358979323846
 #endif
 
+/* Each bead's outputs depend only on its own inputs, so the per-bead loops
+ * run in parallel (OpenMP) with results independent of the thread count. */
+#ifdef _OPENMP
+#define ORC_PAR_FOR _Pragma("omp parallel for schedule(dynamic, 16)")
+#define ORC_SET_FLAG(x) do { _Pragma("omp atomic write") (x) = 1; } while (0)
+#else
+#define ORC_PAR_FOR
+#define ORC_SET_FLAG(x) ((x) = 1)
+#endif
+
 /* ------------------------------------------------------------------ ran2 */
 /* Numerical Recipes ran2 (L'Ecuyer with Bays-Durham shuffle) as used by the
  * reference seeding, src/ran2.h:18-56.  The reference keeps idum2, iy and

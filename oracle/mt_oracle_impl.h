@@ -160,9 +160,12 @@ void FN(orc_forces)(const mtg_params *P, const mtg_topology *T, const REAL *r, i
     V3 P1, P2;
     FN(lateral_sites)(&P1, &P2);
     const REAL lj_pref = (REAL)P->ljscale * (REAL)P->ljsigma6;
-    for (int traj = 0; traj < Ntr; traj++) {
-        for (int ind = 0; ind < N; ind++) {
-            const size_t p = (size_t)ind + (size_t)traj * N;
+    const long long NN = (long long)N * Ntr;
+    ORC_PAR_FOR
+    for (long long pp = 0; pp < NN; pp++) {
+        {
+            const size_t p = (size_t)pp;
+            const int traj = (int)(pp / N), ind = (int)(pp % N);
             if (T->extra[p]) continue; /* d_f[p] left untouched (:55) */
             ACC A = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             const FRAME Fi = FN(bead_frame)(r, p);
@@ -298,9 +301,12 @@ void FN(orc_energies)(const mtg_params *P, const mtg_topology *T, const REAL *r,
     const int N = T->Ntot, Ntr = T->Ntr;
     V3 P1, P2;
     FN(lateral_sites)(&P1, &P2);
-    for (int traj = 0; traj < Ntr; traj++) {
-        for (int ind = 0; ind < N; ind++) {
-            const size_t p = (size_t)ind + (size_t)traj * N;
+    const long long NN = (long long)N * Ntr;
+    ORC_PAR_FOR
+    for (long long pp = 0; pp < NN; pp++) {
+        {
+            const size_t p = (size_t)pp;
+            const int traj = (int)(pp / N), ind = (int)(pp % N);
             REAL Uh = 0, Ulong = 0, Ulat = 0, Upsi = 0, Ufi = 0, Uth = 0, Ulj = 0;
             if (!T->extra[p]) {
                 const FRAME Fi = FN(bead_frame)(r, p);
@@ -392,9 +398,12 @@ void FN(orc_lj_list)(const mtg_params *P, const mtg_topology *T, const REAL *r, 
                      int *LJCount, int *LJ, int *overflow) {
     const int N = T->Ntot, Ntr = T->Ntr;
     const REAL cut = (REAL)P->ljpairscutoff;
-    for (int tr = 0; tr < Ntr; tr++) {
-        for (int i = 0; i < N; i++) {
-            const size_t p = (size_t)i + (size_t)tr * N;
+    const long long NN = (long long)N * Ntr;
+    ORC_PAR_FOR
+    for (long long pp = 0; pp < NN; pp++) {
+        {
+            const size_t p = (size_t)pp;
+            const int tr = (int)(pp / N), i = (int)(pp % N);
             int cnt = 0;
             if (!T->extra[p]) {
                 for (int j = 0; j < N; j++) {
@@ -403,7 +412,7 @@ void FN(orc_lj_list)(const mtg_params *P, const mtg_topology *T, const REAL *r, 
                         if (cnt < maxLJ)
                             LJ[(size_t)maxLJ * p + cnt] = j;
                         else if (overflow)
-                            *overflow = 1;
+                            ORC_SET_FLAG(*overflow);
                         cnt++;
                     }
                 }
@@ -422,9 +431,12 @@ void FN(orc_pairs_list)(const mtg_params *P, const mtg_topology *T, const REAL *
     FN(lateral_sites)(&P1, &P2);
     const V3 ez = {0, 0, 1};
     const REAL cut = (REAL)2.5f;
-    for (int tr = 0; tr < Ntr; tr++) {
-        for (int i = 0; i < N; i++) {
-            const size_t p = (size_t)i + (size_t)tr * N;
+    const long long NN = (long long)N * Ntr;
+    ORC_PAR_FOR
+    for (long long pp = 0; pp < NN; pp++) {
+        {
+            const size_t p = (size_t)pp;
+            const int tr = (int)(pp / N), i = (int)(pp % N);
             int nl = 0, nt = 0;
             if (!T->extra[p]) {
                 /* harmonic[max*i] < 0 (partner above, or no partner: -1) -> R_MON = -r_mon */
@@ -443,7 +455,7 @@ void FN(orc_pairs_list)(const mtg_params *P, const mtg_topology *T, const REAL *
                         if (nl < maxLong)
                             lon[(size_t)maxLong * p + nl] = h0 < 0 ? j : -j;
                         else if (overflow)
-                            *overflow = 1;
+                            ORC_SET_FLAG(*overflow);
                         nl++;
                     }
                 }
@@ -460,7 +472,7 @@ void FN(orc_pairs_list)(const mtg_params *P, const mtg_topology *T, const REAL *
                             if (nt < maxLat)
                                 lat[(size_t)maxLat * p + nt] = o == 0 ? -code : code;
                             else if (overflow)
-                                *overflow = 1;
+                                ORC_SET_FLAG(*overflow);
                             nt++;
                         }
                     }
@@ -495,6 +507,7 @@ void FN(orc_integrate)(const mtg_params *P, const mtg_topology *T, REAL *r, REAL
     const REAL kfi = (REAL)P->dt / ((REAL)P->gammaTheta * (REAL)P->alpha);
     const REAL kth = (REAL)P->dt / (REAL)P->gammaTheta;
     const REAL nfi = (REAL)P->varTheta * MSQRT((REAL)P->freeze_temp / (REAL)P->alpha);
+    ORC_PAR_FOR
     for (size_t p = 0; p < NN; p++) {
         if (!T->fixed[p % T->Ntot] && !T->extra[p]) {
             REAL a[4], b[4];
@@ -541,6 +554,7 @@ void FN(orc_tea_prepare)(const mtg_params *P, const mtg_topology *T, REAL *f, co
                          uint32_t *seeds, REAL *rforce, REAL *mforce, REAL *coords) {
     const size_t NN = (size_t)T->Ntot * T->Ntr;
     const REAL var = MSQRT((REAL)2 * (REAL)0.0019872041f * (REAL)P->Temp * (REAL)P->gammaR / (REAL)P->dt);
+    ORC_PAR_FOR
     for (size_t p = 0; p < NN; p++) {
         REAL g[4];
         FN(orc_rforce)(seeds + 4 * p, 1, g);
@@ -566,6 +580,7 @@ void FN(orc_tea_prepare)(const mtg_params *P, const mtg_topology *T, REAL *f, co
 void FN(orc_tea_epsilon)(const mtg_params *P, const mtg_topology *T, const REAL *r, REAL *ci, REAL *eps) {
     const int N = T->Ntot;
     const size_t NN = (size_t)N * T->Ntr;
+    ORC_PAR_FOR
     for (size_t p = 0; p < NN; p++) {
         const size_t i0 = (p / N) * N;
         REAL sx = 0, sy = 0, sz = 0, sw = 0;
@@ -634,6 +649,7 @@ void FN(orc_tea_integrate)(const mtg_params *P, const mtg_topology *T, REAL *f, 
     const REAL kfi = (REAL)P->dt / ((REAL)P->gammaTheta * (REAL)P->alpha);
     const REAL kth = (REAL)P->dt / (REAL)P->gammaTheta;
     const REAL nfi = (REAL)P->varTheta * MSQRT((REAL)P->freeze_temp / (REAL)P->alpha);
+    ORC_PAR_FOR
     for (size_t p = 0; p < NN; p++) {
         const size_t tr = p / N, i0 = tr * N;
         const REAL b = beta[tr], b2 = b * b;
