@@ -1,0 +1,374 @@
+"""Benchmark of the Brownian/Langevin hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl mtg|reference]
+
+One bench step = one pair-list period (``ljpairsupdatefreq`` = 10 MD steps:
+one list rebuild + 10 force/update steps) over the whole batch.  The metric
+is monomer-steps/s = active (non-extra) beads x MD steps / seconds.
+
+value     device time of the K timed bench steps (CUDA events on the engine's
+          stream), inputs resident in HBM; L2 is flushed (256 MB write)
+          before every timed bench step, outside the timed interval.
+e2e       the same steps through the C ABI with host buffers: every step
+          uploads the state from pinned host memory, runs, and downloads the
+          state (wall clock around each step).
+roofline  the dominant kernel's algorithmic bytes per launch / its average
+          CUDA-event duration in the timed region, against the measured HBM
+          copy bandwidth.
+cpu_baseline  the CPU oracle (the reference's algorithm restated in C, all
+          host threads) on a bounded sample of the same workload.
+
+--impl reference times that CPU implementation alone (the reference's own
+code path is CUDA-only and does not compile on the GPU host).
+
+Multi-GPU (torchrun): each rank runs an independent copy of the workload
+(trajectories are independent: replicas, no collective); value = all
+ranks' monomer-steps / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = json.load(open(os.path.join(ROOT, "BASELINE.json")))["metric"] if os.path.exists(
+    os.path.join(ROOT, "BASELINE.json")) else "monomer-steps/s"
+UNIT = "monomer-steps/s"
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    # 256 trajectories of a 13 PF x 40 monomer lattice (520 beads) + 1000 free
+    # tubulin monomers (500 dimers, GDP) in a 100 nm cube; Morse, 8 nm LJ list
+    # rebuilt every 10 steps; no hydrodynamics.
+    "batched_plain_256x1520": dict(kind="plain", ntraj=256, n_mon=40, n_free=1000, cube=100.0),
+    # small case for quick checks
+    "plain_16x1520": dict(kind="plain", ntraj=16, n_mon=40, n_free=1000, cube=100.0),
+}
+DEFAULT_WORKLOAD = "batched_plain_256x1520"
+
+
+# ---------------------------------------------------------------- helpers
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Host-side barrier and max-reduction over ranks (gloo); no data-path collective."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def make_batch(spec: dict, seed: int):
+    from mt_gb300 import synth
+    p = synth.default_params(seed=seed)
+    b = synth.uniform_batch(p, spec["ntraj"], spec["n_mon"], spec["n_free"], seed=seed, cube=spec["cube"])
+    return b
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` recorded by an ncu capture summary under profiles/."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    d = json.load(open(path))
+    return d.get(workload, {}).get(kernel)
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_sample(spec: dict, seed: int, max_seconds: float = 20.0):
+    """Times the CPU oracle (all host threads) on a bounded sample: the first
+    trajectories of the workload for one pair-list period (10 MD steps),
+    doubling the sample until it takes a few seconds."""
+    from mt_gb300 import synth
+    from oracle import oracle
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
+    o = oracle.Oracle("orc", "f32")
+    ntr = 1
+    best = None
+    while True:
+        p = synth.default_params(seed=seed)
+        b = synth.uniform_batch(p, ntr, spec["n_mon"], spec["n_free"], seed=seed, cube=spec["cube"])
+        seeds = o.generate_seeds(p.rseed, 2 * b.nbeads)
+        period = int(p.ljpairsupdatefreq)
+        t0 = time.perf_counter()
+        o.run(b, b.coords, seeds, 0, period)
+        dt = time.perf_counter() - t0
+        best = (b.active_beads() * period / dt, ntr, dt, b.nbeads)
+        if dt > 2.0 or ntr >= spec["ntraj"] or dt * 2 > max_seconds:
+            break
+        ntr *= 2
+    cores = os.cpu_count() or 1
+    rate, ntr, dt, nb = best
+    return {"value": rate, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", cores)), "kind": "port",
+            "sample": f"{ntr} of {spec['ntraj']} trajectories ({nb} beads) x {10} MD steps (one list period), "
+                      f"{dt:.2f} s"}
+
+
+def run_reference(args, spec, dist):
+    if dist.rank != 0:
+        return
+    seed = 1
+    from mt_gb300 import synth
+    from oracle import oracle
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
+    o = oracle.Oracle("orc", "f32")
+    # bounded per-step sample: as many trajectories as take ~1 s per period
+    probe = cpu_sample(spec, seed, max_seconds=4.0)
+    ntr = int(probe["sample"].split(" ")[0])
+    p = synth.default_params(seed=seed)
+    b = synth.uniform_batch(p, ntr, spec["n_mon"], spec["n_free"], seed=seed, cube=spec["cube"])
+    seeds = o.generate_seeds(p.rseed, 2 * b.nbeads)
+    period = int(p.ljpairsupdatefreq)
+    x = b.coords
+    for w in range(args.warmup):
+        x, _, seeds, _, _, _, _ = o.run(b, x, seeds, w * period, period)
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        x, _, seeds, _, _, _, _ = o.run(b, x, seeds, (args.warmup + k) * period, period)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = b.active_beads() * period * args.steps / tot
+    cores = os.cpu_count() or 1
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": args.workload, "sample_trajectories": ntr, "md_steps_per_bench_step": period},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
+                            "kind": "port",
+                            "sample": f"{ntr} of {spec['ntraj']} trajectories x {period} MD steps per bench step"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ------------------------------------------------------------------ main
+def run_gpu(args, spec, dist):
+    import torch
+
+    from mt_gb300 import build as mbuild
+    from mt_gb300 import engine
+
+    mbuild.build()
+    torch.cuda.set_device(dist.local)
+    seed = 1 + dist.rank
+    b = make_batch(spec, seed)
+    b.params.device = dist.local
+    e = engine.Engine(b)
+    e.upload_state(b.coords)
+    period = int(b.params.ljpairsupdatefreq)
+    active = b.active_beads()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dist.local}")
+
+    step = 0
+    for _ in range(args.warmup):
+        e.step(step, period)
+        step += period
+    e.set_kernel_timing(True)
+    e.step(step, period)          # capture the timed graph outside the timed region
+    step += period
+    e.kernel_times(reset=True)
+
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    dist.barrier()
+    ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms.append(e.step_timed(step, period))
+        step += period
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    kt = e.kernel_times(reset=True)
+    e.set_kernel_timing(False)
+    total_ms = sum(ms)
+    t_max = dist.max(total_ms)
+    total_units = dist.sum(active * period * args.steps)
+    value = total_units / (t_max / 1e3)
+
+    # list statistics for the roofline's algorithmic bytes
+    L = e.lists()
+    n_i = (L["lj"][0].astype(np.int64) + L["long"][0] + L["lat"][0] + b.harmonic_count).astype(np.int64)
+    act = b.extra == 0
+    step_bytes = float(np.sum((48 + 64 + 16 + 4 * n_i)[act]))
+    kt_ms = {k: v[0] for k, v in kt.items()}
+    launches = {k: v[1] for k, v in kt.items()}
+    dominant = max(kt_ms, key=lambda k: kt_ms[k])
+    avg_step_ms = kt_ms["step_plain"] / max(1, launches["step_plain"])
+    peak, peak_kind = measured_peaks()
+    achieved = step_bytes / (avg_step_ms / 1e3) / 1e9
+    traffic = ncu_traffic("k_step_plain", args.workload)
+
+    # end to end through the C ABI with pinned host buffers
+    pin = engine.PinnedArray((e.nb, 7), np.float32)
+    pin.array[:] = e.download_state()
+    lib = engine.load()
+    import ctypes as C
+    fptr = pin.array.ctypes.data_as(C.POINTER(C.c_float))
+    e2e_t = []
+    for _ in range(max(3, args.steps)):
+        t0 = time.perf_counter()
+        engine.check(lib.mtg_upload_state(e.h, fptr))
+        engine.check(lib.mtg_step(e.h, C.c_longlong(step), C.c_int(period)))
+        engine.check(lib.mtg_download_state(e.h, fptr, C.cast(None, C.POINTER(C.c_float))))
+        e2e_t.append(time.perf_counter() - t0)
+        step += period
+    e2e_max = dist.max(sum(e2e_t))
+    e2e_value = dist.sum(active * period * len(e2e_t)) / e2e_max
+    pin.free()
+
+    out = None
+    if dist.rank == 0:
+        cpu = cpu_sample(spec, seed) if dist.ws == 1 and not args.no_cpu_baseline else None
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "trajectories_per_gpu": b.ntraj, "beads_per_gpu": b.nbeads,
+                       "active_beads_per_gpu": active, "md_steps_per_bench_step": period,
+                       "l2": "flushed (256 MB write) before every timed step",
+                       "parallelism": f"replicas x{dist.ws} (independent trajectories)"},
+            "roofline": {"bound": "hbm", "kernel": "k_step_plain", "achieved": achieved, "peak": peak,
+                         "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": step_bytes, "avg_launch_ms": avg_step_ms},
+            "kernel_ms": {k: (kt_ms[k] / launches[k] if launches[k] else None) for k in kt_ms},
+            "kernel_share": {k: kt_ms[k] / max(1e-12, sum(kt_ms.values())) for k in kt_ms},
+            "dominant_kernel": dominant,
+            "gpu_launches": int(sum(launches.values())),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 28 * e.nb, "d2h_bytes_per_step": 28 * e.nb},
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+    e.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="mtg", choices=["mtg", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU-oracle sample (profiling runs)")
+    args = ap.parse_args()
+    spec = WORKLOADS[args.workload]
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, spec, dist)
+        else:
+            out = run_gpu(args, spec, dist)
+            if out is not None:
+                print(json.dumps(out))
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()
