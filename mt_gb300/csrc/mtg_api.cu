@@ -294,9 +294,12 @@ void timed_launch(mtg_engine *e, int kind, F &&launch) {
         return;
     }
     const int s = timing_slot(e, kind);
-    cudaEventRecord(e->ev_a[s], e->stream);
+    // inside a stream capture a plain record only orders the capture; the
+    // External flag makes it an event-record node of the graph
+    const unsigned fl = e->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    cudaEventRecordWithFlags(e->ev_a[s], e->stream, fl);
     launch();
-    cudaEventRecord(e->ev_b[s], e->stream);
+    cudaEventRecordWithFlags(e->ev_b[s], e->stream, fl);
 }
 
 // Enqueues one step of the loop of compute() (src/compute_cuda.cu:1137-1238)
@@ -338,6 +341,8 @@ void collect_timing(mtg_engine *e) {
         if (cudaEventElapsedTime(&ms, e->ev_a[s], e->ev_b[s]) == cudaSuccess) {
             e->kt_total[e->ev_kind[s]] += ms;
             e->kt_count[e->ev_kind[s]]++;
+        } else {
+            cudaGetLastError();  // a slot without a completed record is skipped
         }
     }
     e->used_slots.clear();

@@ -200,3 +200,18 @@ def test_tea_epsmax_reported(engine_mod):
     b = small_system(seed=17, tea=True, tea_epsilon_freq=1, tea_epsmax=1e-6)
     e = make_engine(engine_mod, b)
     assert e.step_raw(0, 1) == -5
+
+
+def test_kernel_timing_in_graphs(engine_mod):
+    """Per-kernel events recorded inside the replayed graphs are readable."""
+    b = small_system(seed=18)
+    e = make_engine(engine_mod, b)
+    e.set_kernel_timing(True)
+    e.step(0, 10)                 # capture + one replay
+    e.kernel_times(reset=True)
+    ms = e.step_timed(10, 10)
+    kt = e.kernel_times()
+    assert kt["rebuild"][1] == 1 and kt["step_plain"][1] == 10
+    assert 0 < kt["step_plain"][0] <= ms
+    e.set_kernel_timing(False)
+    assert e.step_timed(20, 15) > 0   # graph + direct launches without timing
