@@ -204,9 +204,12 @@ int mtg_compute_forces(mtg_engine *e, float *f);
  * (src/compute_cuda.cu:1137-1238) without its host I/O: a pair-list rebuild
  * when step % ljpairsupdatefreq == 0, the forces, then either the
  * Euler-Maruyama update (integrate_kernel, :943-975) or, with hdi_on, the TEA
- * update (updateTea + integrateTea, src/bdhitea.cu:37-118).  Launches are
- * replayed from CUDA graphs; the call returns once they are enqueued and
- * checks device error flags at the end. */
+ * update (updateTea + integrateTea, src/bdhitea.cu:37-118).  When
+ * mtg_rebuild_pairs() was called after the last step, the rebuild due at
+ * first_step is not repeated, so a caller can rebuild, run its host hooks and
+ * then step: the reference's order within a step (src/compute_cuda.cu:1140-1228).
+ * Launches are replayed from CUDA graphs (one per pair-list period); the call
+ * waits for them and reports device error flags. */
 int mtg_step(mtg_engine *e, long long first_step, int nsteps);
 /* Waits for the engine's stream and reports any device error flag. */
 int mtg_sync(mtg_engine *e);

@@ -106,6 +106,7 @@ struct mtg_engine {
     bool keep_forces = false;
     bool have_state = false;
     bool lists_valid = false;
+    bool lists_fresh = false;   // mtg_rebuild_pairs ran after the last step
     cudaStream_t stream = nullptr;
     std::vector<int> h_off;
     // device
@@ -304,9 +305,9 @@ void timed_launch(mtg_engine *e, int kind, F &&launch) {
 
 // Enqueues one step of the loop of compute() (src/compute_cuda.cu:1137-1238)
 // minus its host I/O.
-void enqueue_step(mtg_engine *e, long long step) {
+void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
     const mtg_params &p = e->p;
-    if (step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
+    if (allow_rebuild && step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
         timed_launch(e, 0, [&] { launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream); });
         e->lists_valid = true;
     }
@@ -735,6 +736,7 @@ int mtg_rebuild_pairs(mtg_engine *e) {
     if (e->p.lj_on || e->p.is_assembly) launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream);
     CK(cudaGetLastError());
     e->lists_valid = true;
+    e->lists_fresh = true;
     return check_errors(e);
 }
 
@@ -793,6 +795,13 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
     e->used_slots.clear();
     long long s = first_step;
     const long long end = first_step + nsteps;
+    if (e->lists_fresh && s < end && s % p.ljpairsupdatefreq == 0) {
+        // the caller rebuilt the lists for this step already (reference order:
+        // rebuild, host hooks, forces; src/compute_cuda.cu:1140-1228)
+        enqueue_step(e, s, false);
+        s++;
+    }
+    if (nsteps > 0) e->lists_fresh = false;
     while (s < end) {
         if (use_graphs && s % period == 0 && end - s >= period) {
             cudaGraphExec_t &ge = e->graph[e->cur];
