@@ -230,6 +230,25 @@ int mtg_energies(mtg_engine *e, double *per_bead, double *per_traj);
  * row sums of squared normalised tensor entries (d_ci). */
 int mtg_tea_update(mtg_engine *e, double *eps_out, float *beta_out, float *ci_out);
 
+/* Per-trajectory energy totals written to device memory, allocating nothing.
+ * No counterpart in the reference.  For callers that must not allocate at
+ * the moment they ask for energies: analysis hooks running while other
+ * engines on the same GPU have work in flight (cudaMalloc/cudaFree may
+ * synchronise the whole device and stall that work), and processes whose
+ * device memory is reserved up front by a pool allocator, where a new
+ * cudaMalloc can fail.  d_per_traj: device memory for [ntraj*7] doubles
+ * (the totals of mtg_energies).  The block partial sums live in a fixed
+ * device array of 16384 x 7 doubles (917,504 bytes, held by every GPU that
+ * loads the library until the process exits), so a batch may span at most
+ * 16384 chunks of 128 beads (each trajectory is chunked separately; up to
+ * 2,097,152 beads); larger batches get MTG_E_CONFIG.  The first call on a
+ * device looks up that array's device address (make it before any stream
+ * capture).  Every call on a device shares the array: calls whose work
+ * overlaps on the GPU (engines on different streams of the same device)
+ * race and must be serialised by the caller.  Work is enqueued on the
+ * engine's stream; mtg_sync() waits for it and reports a non-finite total. */
+int mtg_energies_noalloc(mtg_engine *e, double *d_per_traj);
+
 /* ---- measurement ------------------------------------------------------- */
 /* mtg_step bracketed by CUDA events recorded on the engine's stream;
  * *device_ms = the device time between them.  No reference counterpart (the

@@ -1,0 +1,66 @@
+// energy_noalloc.cu - per-trajectory energy totals without any allocation.
+//
+// mtg_energies() reduces the per-bead energies through block partial sums
+// kept in a buffer the engine allocated.  This file offers the same
+// reduction for callers that must not allocate device memory at the moment
+// they ask for energies: analysis hooks that run while other engines on the
+// same GPU have work in flight (cudaMalloc and cudaFree may synchronise the
+// whole device and stall that work), and processes whose device memory is
+// reserved up front by a pool allocator, where a fresh cudaMalloc can fail.
+// Its scratch (the block partials) lives in a fixed, file-scope device array
+// instead, so the call itself allocates nothing.
+#include <mutex>
+
+#include "mtg_engine.cuh"
+
+namespace {
+
+// Block partials: 7 doubles per 128-bead chunk; 16384 chunks = up to
+// 2,097,152 beads per call, 917,504 bytes held on every GPU that loads the
+// library, until the process exits.
+constexpr int kMaxChunks = 16384;
+static __device__ __align__(256) double g_energy_scratch[kMaxChunks * MTG_ENERGY_TERMS];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+double *g_scratch_addr[kMaxDevices] = {nullptr};
+
+// Device address of g_energy_scratch on `device` (which must be current).
+// The host-side symbol is only a stand-in; a kernel needs this address.
+int scratch_address(int device, double **out) {
+    if (device < 0 || device >= kMaxDevices)
+        return mtg_internal_fail(MTG_E_CONFIG, "mtg_energies_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_scratch_addr[device]) {
+        void *p = nullptr;
+        const cudaError_t err = cudaGetSymbolAddress(&p, g_energy_scratch);
+        if (err != cudaSuccess)
+            return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: cudaGetSymbolAddress of the scratch failed");
+        g_scratch_addr[device] = static_cast<double *>(p);
+    }
+    *out = g_scratch_addr[device];
+    return MTG_OK;
+}
+
+}  // namespace
+
+extern "C" int mtg_energies_noalloc(mtg_engine *e, double *d_per_traj) {
+    if (!e || !d_per_traj) return mtg_internal_fail(MTG_E_CONFIG, "mtg_energies_noalloc: engine or output is NULL");
+    if (!e->have_state) return mtg_internal_fail(MTG_E_STATE, "mtg_energies_noalloc: no state uploaded");
+    if (e->nwork > kMaxChunks)
+        return mtg_internal_fail(MTG_E_CONFIG,
+                                 "mtg_energies_noalloc: the batch needs more than 16384 chunks of 128 beads "
+                                 "(trajectories are chunked separately); use mtg_energies");
+    if (cudaSetDevice(e->device) != cudaSuccess)
+        return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: cudaSetDevice failed");
+    double *scratch = nullptr;
+    const int rc = scratch_address(e->device, &scratch);
+    if (rc != MTG_OK) return rc;
+    // every chunk's partials are overwritten by the energy kernel before the
+    // totals kernel reads them, so nothing needs clearing between calls
+    mtg::launch_energy(e->kp, e->bufs(), nullptr, scratch, e->work, e->nwork, e->stream);
+    mtg::launch_energy_totals(e->kp, scratch, e->work_first, d_per_traj, e->err, e->stream);
+    if (cudaGetLastError() != cudaSuccess)
+        return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: kernel launch failed");
+    return MTG_OK;
+}

@@ -1,0 +1,88 @@
+// mtg_engine.cuh - the engine object behind the opaque mtg_engine handle.
+// Internal to the library; shared by the .cu files that implement the ABI.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/mtg.h"
+#include "mtg_internal.cuh"
+
+struct mtg_engine {
+    using KParams = mtg::KParams;
+    using DevBuffers = mtg::DevBuffers;
+    mtg_params p{};
+    KParams kp{};
+    int nb = 0, nt = 0;
+    int cur = 0;            // frame buffer holding the current state
+    bool keep_forces = false;
+    bool have_state = false;
+    bool lists_valid = false;
+    bool lists_fresh = false;   // mtg_rebuild_pairs ran after the last step
+    cudaStream_t stream = nullptr;
+    std::vector<int> h_off;
+    // device
+    int *off = nullptr, *traj = nullptr, *flags = nullptr, *harm = nullptr;
+    float *zs = nullptr;
+    float4 *frame[2] = {nullptr, nullptr};
+    float4 *force = nullptr;
+    uint4 *seeds = nullptr;
+    int *ljc = nullptr, *lj = nullptr, *lonc = nullptr, *lon = nullptr, *latc = nullptr, *lat = nullptr;
+    int *err = nullptr;
+    int2 *work = nullptr;
+    int nwork = 0;
+    int *work_first = nullptr;
+    double *en_partials = nullptr, *en_traj = nullptr, *en_bead = nullptr;
+    float4 *tea_r = nullptr, *tea_ci = nullptr;
+    float *tea_eps = nullptr, *tea_beta = nullptr;
+    double *tea_eps_t = nullptr;
+    float *stage = nullptr;        // 7*nb floats for host <-> device Coord transfers
+    void *stage_host = nullptr;    // pinned mirror of stage
+    uint8_t *stage_u8 = nullptr;
+    int *stage_i = nullptr;
+    int device = 0;
+    // graphs: [parity]
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_period = 0;
+    // per-kernel timing (see mtg_set_kernel_timing)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_a, ev_b;
+    std::vector<int> ev_kind;
+    int graph_slot_base[2] = {0, 0}, graph_slot_count[2] = {0, 0};
+    int direct_base = 0, direct_next = 0, capture_next = 0;
+    bool capturing = false;
+    std::vector<int> used_slots;
+    double kt_total[MTG_KERNEL_KINDS] = {0};
+    long long kt_count[MTG_KERNEL_KINDS] = {0};
+    cudaEvent_t call_a = nullptr, call_b = nullptr;
+
+    DevBuffers bufs() const {
+        DevBuffers b{};
+        b.off = off;
+        b.traj = traj;
+        b.flags = flags;
+        b.harm = harm;
+        b.zs = zs;
+        b.frame_in = frame[cur];
+        b.frame_out = frame[cur ^ 1];
+        b.force = force;
+        b.seeds = seeds;
+        b.ljc = ljc;
+        b.lj = lj;
+        b.lonc = lonc;
+        b.lon = lon;
+        b.latc = latc;
+        b.lat = lat;
+        b.err = err;
+        b.tea_r = tea_r;
+        b.tea_ci = tea_ci;
+        b.tea_eps = tea_eps;
+        b.tea_beta = tea_beta;
+        b.tea_eps_t = tea_eps_t;
+        return b;
+    }
+};
+
+
+// Records msg as the calling thread's last error (mtg_last_error_string) and
+// returns code.
+int mtg_internal_fail(int code, const char *msg);

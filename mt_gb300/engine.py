@@ -46,6 +46,7 @@ EXPORTS = {
     "mtg_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
     "mtg_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "mtg_host_free": (C.c_int, [C.c_void_p]),
+    "mtg_energies_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step")
