@@ -52,6 +52,12 @@ WORKLOADS = {
     "batched_plain_256x1520": dict(kind="plain", ntraj=256, n_mon=40, n_free=1000, cube=100.0),
     # small case for quick checks
     "plain_16x1520": dict(kind="plain", ntraj=16, n_mon=40, n_free=1000, cube=100.0),
+    # exact TEA hydrodynamics: 16 trajectories of a 13 PF x 100 monomer lattice
+    # (1300 beads) + 2000 free monomers; RPY radius 2 nm, epsilon/beta every
+    # 10 steps (FP64 reduction on the device)
+    "tea_exact_16x3300": dict(kind="tea", ntraj=16, n_mon=100, n_free=2000, cube=100.0),
+    # exact TEA at the size of the learned-TEA comparison: 64 x (13 PF x 200 + 3000)
+    "tea_exact_64x5600": dict(kind="tea", ntraj=64, n_mon=200, n_free=3000, cube=150.0),
 }
 DEFAULT_WORKLOAD = "batched_plain_256x1520"
 
@@ -162,11 +168,27 @@ def measured_peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def make_batch(spec: dict, seed: int):
+def workload_params(spec: dict, seed: int):
     from mt_gb300 import synth
-    p = synth.default_params(seed=seed)
-    b = synth.uniform_batch(p, spec["ntraj"], spec["n_mon"], spec["n_free"], seed=seed, cube=spec["cube"])
-    return b
+    if spec["kind"] == "tea":
+        return synth.default_params(seed=seed, hdi_on=1, tea_a=2.0, tea_epsilon_freq=10)
+    return synth.default_params(seed=seed)
+
+
+def make_batch(spec: dict, seed: int, ntraj: int | None = None):
+    from mt_gb300 import synth
+    p = workload_params(spec, seed)
+    return synth.uniform_batch(p, ntraj or spec["ntraj"], spec["n_mon"], spec["n_free"], seed=seed,
+                               cube=spec["cube"])
+
+
+def tea_pairs(b) -> int:
+    """Ordered non-extra pairs i != j per trajectory, summed: the TEA mobility product's units."""
+    tot = 0
+    for t in range(b.ntraj):
+        n = int(np.count_nonzero(b.extra[b.offsets[t]:b.offsets[t + 1]] == 0))
+        tot += n * (n - 1)
+    return tot
 
 
 def ncu_traffic(kernel: str, workload: str):
@@ -190,8 +212,8 @@ def cpu_sample(spec: dict, seed: int, max_seconds: float = 20.0):
     ntr = 1
     best = None
     while True:
-        p = synth.default_params(seed=seed)
-        b = synth.uniform_batch(p, ntr, spec["n_mon"], spec["n_free"], seed=seed, cube=spec["cube"])
+        b = make_batch(spec, seed, ntr)
+        p = b.params
         seeds = o.generate_seeds(p.rseed, 2 * b.nbeads)
         period = int(p.ljpairsupdatefreq)
         t0 = time.perf_counter()
@@ -219,17 +241,19 @@ def run_reference(args, spec, dist):
     # bounded per-step sample: as many trajectories as take ~1 s per period
     probe = cpu_sample(spec, seed, max_seconds=4.0)
     ntr = int(probe["sample"].split(" ")[0])
-    p = synth.default_params(seed=seed)
-    b = synth.uniform_batch(p, ntr, spec["n_mon"], spec["n_free"], seed=seed, cube=spec["cube"])
+    b = make_batch(spec, seed, ntr)
+    p = b.params
     seeds = o.generate_seeds(p.rseed, 2 * b.nbeads)
     period = int(p.ljpairsupdatefreq)
     x = b.coords
+    ci = beta = None
     for w in range(args.warmup):
-        x, _, seeds, _, _, _, _ = o.run(b, x, seeds, w * period, period)
+        x, _, seeds, _, _, ci, beta = o.run(b, x, seeds, w * period, period, tea_ci=ci, tea_beta=beta)
     times = []
     for k in range(args.steps):
         t0 = time.perf_counter()
-        x, _, seeds, _, _, _, _ = o.run(b, x, seeds, (args.warmup + k) * period, period)
+        x, _, seeds, _, _, ci, beta = o.run(b, x, seeds, (args.warmup + k) * period, period, tea_ci=ci,
+                                            tea_beta=beta)
         times.append(time.perf_counter() - t0)
     tot = sum(times)
     value = b.active_beads() * period * args.steps / tot
@@ -291,18 +315,33 @@ def run_gpu(args, spec, dist):
     total_units = dist.sum(active * period * args.steps)
     value = total_units / (t_max / 1e3)
 
-    # list statistics for the roofline's algorithmic bytes
-    L = e.lists()
-    n_i = (L["lj"][0].astype(np.int64) + L["long"][0] + L["lat"][0] + b.harmonic_count).astype(np.int64)
-    act = b.extra == 0
-    step_bytes = float(np.sum((48 + 64 + 16 + 4 * n_i)[act]))
     kt_ms = {k: v[0] for k, v in kt.items()}
     launches = {k: v[1] for k, v in kt.items()}
     dominant = max(kt_ms, key=lambda k: kt_ms[k])
-    avg_step_ms = kt_ms["step_plain"] / max(1, launches["step_plain"])
-    peak, peak_kind = measured_peaks()
-    achieved = step_bytes / (avg_step_ms / 1e3) / 1e9
-    traffic = ncu_traffic("k_step_plain", args.workload)
+    if spec["kind"] == "plain":
+        # list statistics for the algorithmic bytes of the fused step
+        L = e.lists()
+        n_i = (L["lj"][0].astype(np.int64) + L["long"][0] + L["lat"][0] + b.harmonic_count).astype(np.int64)
+        act = b.extra == 0
+        work = float(np.sum((48 + 64 + 16 + 4 * n_i)[act]))
+        avg_ms = kt_ms["step_plain"] / max(1, launches["step_plain"])
+        peak, peak_kind = measured_peaks()
+        achieved = work / (avg_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": "k_step_plain", "achieved": achieved, "peak": peak,
+                "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": ncu_traffic("k_step_plain", args.workload), "algorithmic_bytes_per_launch": work,
+                "avg_launch_ms": avg_ms}
+    else:
+        import ctypes as C
+        work = 45.0 * tea_pairs(b)
+        avg_ms = kt_ms["tea_step"] / max(1, launches["tea_step"])
+        tf = C.c_double()
+        engine.check(engine.load().mtg_measure_fp32_tflops(dist.local, C.byref(tf)))
+        achieved = work / (avg_ms / 1e3) / 1e12
+        roof = {"bound": "fp32", "kernel": "k_tea_step", "achieved": achieved, "peak": tf.value,
+                "peak_source": "measured FP32 FMA rate (mtg_measure_fp32_tflops)", "unit": "TFLOP/s",
+                "frac": achieved / tf.value, "traffic": ncu_traffic("k_tea_step", args.workload),
+                "algorithmic_flop_per_launch": work, "avg_launch_ms": avg_ms}
 
     # end to end through the C ABI with pinned host buffers
     pin = engine.PinnedArray((e.nb, 7), np.float32)
@@ -333,9 +372,7 @@ def run_gpu(args, spec, dist):
                        "active_beads_per_gpu": active, "md_steps_per_bench_step": period,
                        "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{dist.ws} (independent trajectories)"},
-            "roofline": {"bound": "hbm", "kernel": "k_step_plain", "achieved": achieved, "peak": peak,
-                         "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": step_bytes, "avg_launch_ms": avg_step_ms},
+            "roofline": roof,
             "kernel_ms": {k: (kt_ms[k] / launches[k] if launches[k] else None) for k in kt_ms},
             "kernel_share": {k: kt_ms[k] / max(1e-12, sum(kt_ms.values())) for k in kt_ms},
             "dominant_kernel": dominant,

@@ -1,0 +1,55 @@
+// peak_probe.cu - measured FP32 FMA throughput of the current GPU, the
+// denominator of the roofline of the FP32-pipe-bound TEA kernels.
+#include <cuda_runtime.h>
+
+#include "../../include/mtg.h"
+
+namespace {
+
+// 8 independent FMA chains per thread, 2 FLOP each per iteration.
+__global__ void __launch_bounds__(256) k_fma_chain(float *out, int iters, float a, float b) {
+    float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    const float s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == 12345.678f) out[0] = s;  // keeps the chains live
+}
+
+}  // namespace
+
+extern "C" int mtg_measure_fp32_tflops(int device, double *tflops) {
+    if (!tflops) return MTG_E_CONFIG;
+    if (cudaSetDevice(device) != cudaSuccess) return MTG_E_CUDA;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    float *out = nullptr;
+    if (cudaMalloc(&out, sizeof(float)) != cudaSuccess) return MTG_E_CUDA;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    k_fma_chain<<<blocks, threads>>>(out, 64, 0.999f, 1e-3f);  // warm-up
+    double best = 0.0;
+    for (int rep = 0; rep < 5; rep++) {
+        cudaEventRecord(a);
+        k_fma_chain<<<blocks, threads>>>(out, iters, 0.999f, 1e-3f);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        const double flop = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+        if (ms > 0) best = flop / (ms * 1e-3) / 1e12 > best ? flop / (ms * 1e-3) / 1e12 : best;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    if (cudaGetLastError() != cudaSuccess) return MTG_E_CUDA;
+    *tflops = best;
+    return MTG_OK;
+}

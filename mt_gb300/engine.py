@@ -47,6 +47,7 @@ EXPORTS = {
     "mtg_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "mtg_host_free": (C.c_int, [C.c_void_p]),
     "mtg_energies_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mtg_measure_fp32_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
 }
 
 KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step")
