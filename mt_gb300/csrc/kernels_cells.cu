@@ -1,0 +1,257 @@
+// kernels_cells.cu - neighbour-list rebuild through a per-trajectory spatial
+// hash (cell list), producing the same lists as the brute-force kernel.
+//
+// Cells are cubes of edge `reach` (the largest list cutoff, or the 6.6 nm
+// prefilter of the assembly lists), so every partner lies in the 27 cells
+// around a bead.  Each trajectory owns a hash table of next_pow2(max(32, N))
+// buckets; colliding cells share a bucket and only add candidates.
+//   1. k_cell_count : bucket of every bead, bucket populations
+//   2. k_cell_scan  : one CTA per trajectory, exclusive scan of its table
+//   3. k_cell_fill  : beads scattered into bucket order
+//   4. k_cell_lists : per bead, candidates from the 27 cells' buckets (each
+//      bucket visited once), the reference's list tests, then an insertion
+//      sort so each list is in ascending j (orientation 0 before 1 for the
+//      lateral list), exactly the order of the reference's j loops
+//      (src/compute_cuda.cu:564-661, :927-936).
+#include "mtg_internal.cuh"
+
+namespace mtg {
+
+namespace {
+
+constexpr float kPairReach = 6.6f;  // see kPairPrefilter in kernels_lists.cu
+constexpr int kLocalLJ = 64;        // LJ entries sorted in local memory; more -> sorted in place
+
+__device__ __forceinline__ int cell_coord(float x, float inv) {
+    float c = floorf(x * inv);
+    c = fminf(fmaxf(c, -1048576.0f), 1048576.0f);  // NaN -> -2^20 (fmaxf drops NaN)
+    return (int)c;
+}
+
+__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz) {
+    return ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ ((uint32_t)cz * 83492791u);
+}
+
+__global__ void k_cell_count(KParams P, const float4 *pos, const int *traj, const int *tbase, const int *tmask,
+                             float inv_cell, int *key, int *cnt) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= P.nb) return;
+    const float4 p = pos[g];
+    const int t = traj[g];
+    const uint32_t h = cell_hash(cell_coord(p.x, inv_cell), cell_coord(p.y, inv_cell), cell_coord(p.z, inv_cell));
+    const int k = tbase[t] + (int)(h & (uint32_t)tmask[t]);
+    key[g] = k;
+    atomicAdd(&cnt[k], 1);
+}
+
+// Exclusive scan of each trajectory's table; start and cursor get the result.
+__global__ void __launch_bounds__(1024) k_cell_scan(const int *tbase, const int *cnt, int *start, int *cursor) {
+    const int t = blockIdx.x;
+    const int b0 = tbase[t], n = tbase[t + 1] - tbase[t];
+    __shared__ int s_part[1024];
+    __shared__ int s_warp[32];
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
+    int local = 0;
+    for (int i = lo; i < hi; i++) local += cnt[b0 + i];
+    // block exclusive scan of `local`
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int v = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) s_warp[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    int run = (v - local) + (wid > 0 ? s_warp[wid - 1] : 0);
+    s_part[threadIdx.x] = run;
+    for (int i = lo; i < hi; i++) {
+        start[b0 + i] = run;
+        cursor[b0 + i] = run;
+        run += cnt[b0 + i];
+    }
+}
+
+// Bucket-ordered bead lists; positions are relative to the trajectory's
+// first bead, so slots of trajectory t start at off[t].
+__global__ void k_cell_fill(int nb, const int *traj, const int *off, const int *key, int *cursor, int *cell_bead) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nb) return;
+    const int slot = atomicAdd(&cursor[key[g]], 1);
+    cell_bead[off[traj[g]] + slot] = g;
+}
+
+__device__ __forceinline__ void isort(int *a, int n) {
+    for (int i = 1; i < n; i++) {
+        const int v = a[i];
+        int j = i - 1;
+        while (j >= 0 && a[j] > v) {
+            a[j + 1] = a[j];
+            j--;
+        }
+        a[j + 1] = v;
+    }
+}
+
+// In-place insertion sort of a k-major list (rare path: > kLocalLJ entries).
+__device__ void isort_strided(int *a, int n, int stride) {
+    for (int i = 1; i < n; i++) {
+        const int v = a[(size_t)i * stride];
+        int j = i - 1;
+        while (j >= 0 && a[(size_t)j * stride] > v) {
+            a[(size_t)(j + 1) * stride] = a[(size_t)j * stride];
+            j--;
+        }
+        a[(size_t)(j + 1) * stride] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kTile) k_cell_lists(KParams P, DevBuffers B, const int2 *work, const int *tbase,
+                                                      const int *tmask, const int *start, const int *cnt,
+                                                      const int *cell_bead, float inv_cell) {
+    const int2 w = work[blockIdx.x];
+    const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
+    const int g = w.y + threadIdx.x;
+    if (g >= end) return;
+    const int nb = P.nb;
+    const float4 *fr = B.frame_in;
+    const int flags = B.flags[g];
+    const bool extra_i = (flags & kFlagExtra) != 0;
+    const bool do_lj = P.lj_on && !extra_i;
+    const bool do_pairs = P.is_assembly && !extra_i;
+    if (!do_lj && !do_pairs) {
+        if (P.lj_on) B.ljc[g] = 0;
+        if (P.is_assembly) {
+            B.lonc[g] = 0;
+            B.latc[g] = 0;
+        }
+        return;
+    }
+    const float4 pi = fr[g], ui = fr[nb + g], li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
+    const int il = g - base;
+    const int h0 = B.harm[g * P.maxH];
+    const float rmon = h0 < 0 ? -2.0f : 2.0f;
+    const int hpart = h0 < 0 ? -h0 : h0;
+    const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
+    const int cx = cell_coord(pi.x, inv_cell), cy = cell_coord(pi.y, inv_cell), cz = cell_coord(pi.z, inv_cell);
+    const int tb = tbase[traj];
+    const uint32_t mask = (uint32_t)tmask[traj];
+
+    int lj_buf[kLocalLJ];
+    int lo_buf[kCellMaxLong], la_buf[kCellMaxLat];
+    int nlj = 0, nlo = 0, nla = 0;
+    bool overflow = false;
+    int visited[27];
+    int nvis = 0;
+    for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+                const int bkt = tb + (int)(cell_hash(cx + dx, cy + dy, cz + dz) & mask);
+                bool seen = false;
+                for (int v = 0; v < nvis; v++) seen |= (visited[v] == bkt);
+                if (seen) continue;
+                visited[nvis++] = bkt;
+                const int s0 = base + start[bkt], s1 = s0 + cnt[bkt];
+                for (int s = s0; s < s1; s++) {
+                    const int jg = cell_bead[s];
+                    const int jl = jg - base;
+                    const float4 q = fr[jg];
+                    const float cd = centre_dist(pi, q);
+                    if (do_lj && jl != il && cd < P.ljcut) {
+                        if (nlj >= P.maxLJ) {
+                            overflow = true;
+                        } else if (nlj < kLocalLJ) {
+                            lj_buf[nlj] = jl;
+                        } else {
+                            if (nlj == kLocalLJ)  // spill the local part first
+                                for (int k = 0; k < kLocalLJ; k++) B.lj[k * nb + g] = lj_buf[k];
+                            B.lj[nlj * nb + g] = jl;
+                        }
+                        nlj++;
+                    }
+                    if (do_pairs && cd < kPairReach && jl != hpart) {
+                        const int fj = B.flags[jg];
+                        if (((flags ^ fj) & kFlagBeta) != 0) {
+                            const float4 uj = fr[nb + jg];
+                            const float3 d = site_delta(pi, q, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon));
+                            if (norm3_rn(d) < 2.5f) {
+                                if (nlo < P.maxLong)
+                                    lo_buf[nlo] = jl;
+                                else
+                                    overflow = true;
+                                nlo++;
+                            }
+                        }
+                        if (jl != il) {
+                            const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
+                            if (norm3_rn(site_delta(pi, q, f3(li1), f3(l2))) < 2.5f) {
+                                if (nla < P.maxLat)
+                                    la_buf[nla] = 2 * jl;       // orientation 0 -> -j
+                                else
+                                    overflow = true;
+                                nla++;
+                            }
+                            if (norm3_rn(site_delta(pi, q, f3(li2), f3(l1))) < 2.5f) {
+                                if (nla < P.maxLat)
+                                    la_buf[nla] = 2 * jl + 1;   // orientation 1 -> +j
+                                else
+                                    overflow = true;
+                                nla++;
+                            }
+                        }
+                    }
+                }
+            }
+    if (P.lj_on) {
+        const int n = min(nlj, P.maxLJ);
+        if (n <= kLocalLJ) {
+            isort(lj_buf, n);
+            for (int k = 0; k < n; k++) B.lj[k * nb + g] = lj_buf[k];
+        } else {
+            isort_strided(B.lj + g, n, nb);
+        }
+        B.ljc[g] = n;
+    }
+    if (P.is_assembly) {
+        const int n1 = min(nlo, P.maxLong), n2 = min(nla, P.maxLat);
+        isort(lo_buf, n1);
+        isort(la_buf, n2);
+        for (int k = 0; k < n1; k++) B.lon[k * nb + g] = h0 < 0 ? lo_buf[k] : -lo_buf[k];
+        for (int k = 0; k < n2; k++) {
+            const int j = la_buf[k] >> 1;
+            const int code = j != 0 ? j : kZeroCode;
+            B.lat[k * nb + g] = (la_buf[k] & 1) ? code : -code;
+        }
+        B.lonc[g] = n1;
+        B.latc[g] = n2;
+    }
+    if (overflow) atomicOr(B.err, kErrOverflow);
+}
+
+inline int nblk(int n, int t) { return (n + t - 1) / t; }
+
+}  // namespace
+
+void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffers &C, const int2 *work, int nwork,
+                          cudaStream_t s) {
+    // cells slightly larger than the reach, so that rounding of x / edge can
+    // never put two beads closer than the reach two cells apart
+    const float reach = fmaxf(P.lj_on ? P.ljcut : 0.f, P.is_assembly ? kPairReach : 0.f);
+    const float inv = 1.0f / (reach * 1.001f + 1e-3f);
+    cudaMemsetAsync(C.cnt, 0, sizeof(int) * C.nbuckets, s);
+    k_cell_count<<<nblk(P.nb, 256), 256, 0, s>>>(P, B.frame_in, B.traj, C.tbase, C.tmask, inv, C.key, C.cnt);
+    k_cell_scan<<<P.nt, 1024, 0, s>>>(C.tbase, C.cnt, C.start, C.cursor);
+    k_cell_fill<<<nblk(P.nb, 256), 256, 0, s>>>(P.nb, B.traj, B.off, C.key, C.cursor, C.cell_bead);
+    k_cell_lists<<<nwork, kTile, 0, s>>>(P, B, work, C.tbase, C.tmask, C.start, C.cnt, C.cell_bead, inv);
+}
+
+}  // namespace mtg

@@ -2,40 +2,51 @@
 // epsilon / C_i pass, the FP64 epsilon -> beta reduction, and the all-pairs
 // RPY mobility product fused with the position update.
 //
-// Both O(N^2) kernels run one CTA per (trajectory, chunk of kTile beads) and
-// stream the trajectory through shared memory in tiles; every thread keeps
-// its bead i in registers and reads the tile by broadcast.  They are bound by
-// the FP32 pipe (about 45 FLOP per ordered pair).
+// Both O(N^2) kernels run one CTA per (trajectory, chunk of kTeaChunk beads)
+// and stream the trajectory through shared memory in tiles; each bead i is
+// served by `tea_slices` threads that take interleaved j of every tile, so
+// small batches still fill the GPU, and the partial sums meet in shared
+// memory.  Every thread reads the tile by broadcast.  They are bound by the
+// FP32 pipe (about 45 FLOP per ordered pair).
 #include "mtg_internal.cuh"
 
 namespace mtg {
 
-// Normalised RPY block D_ij/D_ii (integrateTea_RPY, src/bdhitea_kernel.cu:38-58)
-// as (cii, crr): T = cii I + crr u u^T, from the squared distance r2.
-__device__ __forceinline__ void rpy_coeffs(float r2, float inv_a, float a, float &cii, float &crr, float &rinv) {
+// Normalised RPY block D_ij/D_ii (integrateTea_RPY, src/bdhitea_kernel.cu:38-58):
+// T = cii I + crr u u^T with ra = r/a; ra > 2: crr = 0.75/ra (1 - 2/ra^2),
+// cii = 0.75/ra (1 + 2/(3 ra^2)); otherwise crr = 3 ra/32, cii = 1 - 9 ra/32.
+// RPY coefficients from the squared distance (branch-free): cii, and
+// crr / r^2 so that T g = cii g + (crr / r^2) d (d . g) with d = r_j - r_i.
+__device__ __forceinline__ void rpy_pair(float r2, float a, float inv_a, float &cii, float &crr_r2, float &rinv) {
+    r2 = fmaxf(r2, 1e-6f);                  // coincident beads stay finite (masked by the caller)
     rinv = rsqrtf(r2);
-    const float r = r2 * rinv;
-    const float ra = r * inv_a;
-    if (ra > 2.0f) {
-        const float ira = a * rinv;         // 1 / ra
-        const float ira2 = ira * ira;
-        crr = 0.75f * ira * (1.0f - 2.0f * ira2);
-        cii = 0.75f * ira * (1.0f + (2.0f / 3.0f) * ira2);
-    } else {
-        crr = (3.0f / 32.0f) * ra;
-        cii = 1.0f - (9.0f / 32.0f) * ra;
-    }
+    const float ra = r2 * rinv * inv_a;
+    const float ira = a * rinv, ira2 = ira * ira;
+    const float far_rr = 0.75f * ira * (1.0f - 2.0f * ira2);
+    const float far_ii = 0.75f * ira * (1.0f + (2.0f / 3.0f) * ira2);
+    const bool far = ra > 2.0f;
+    crr_r2 = (far ? far_rr : (3.0f / 32.0f) * ra) * rinv * rinv;
+    cii = far ? far_ii : 1.0f - (9.0f / 32.0f) * ra;
 }
+
+// Work split of the all-pairs TEA kernels: a CTA holds kTeaI beads i, each
+// served by `slices` threads that cover interleaved j of every tile; the
+// partial sums meet in shared memory.  slices = blockDim.x / kTeaI.
+constexpr int kTeaI = kTeaChunk;
+constexpr int kTeaTile = 256;
 
 // integrateTea_epsilon_unlisted (src/bdhitea_kernel.cu:84-101): per bead i,
 // sum over non-extra j != i of the row sums of squared entries (-> tea_ci)
 // and of all nine entries (-> tea_eps).
-__global__ void __launch_bounds__(kTile) k_tea_eps(KParams P, DevBuffers B, const int2 *work) {
+__global__ void __launch_bounds__(512) k_tea_eps(KParams P, DevBuffers B, const int2 *work) {
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
-    const int g = w.y + threadIdx.x;
+    const int slices = blockDim.x / kTeaI;
+    const int il = threadIdx.x % kTeaI, sl = threadIdx.x / kTeaI;
+    const int g = w.y + il;
     const bool valid = g < end;
-    __shared__ float4 s_pos[kTile];
+    __shared__ float4 s_pos[kTeaTile];
+    __shared__ float4 s_red[512];
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
     bool extra_i = true;
     if (valid) {
@@ -44,26 +55,31 @@ __global__ void __launch_bounds__(kTile) k_tea_eps(KParams P, DevBuffers B, cons
     }
     const float a = P.tea_a, inv_a = 1.0f / P.tea_a;
     float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
-    for (int j0 = base; j0 < end; j0 += kTile) {
-        const int jg = j0 + threadIdx.x;
-        if (jg < end) {
-            float4 q = B.frame_in[jg];
-            q.w = (B.flags[jg] & kFlagExtra) ? 1.0f : 0.0f;
-            s_pos[threadIdx.x] = q;
+    for (int j0 = base; j0 < end; j0 += kTeaTile) {
+        for (int k = threadIdx.x; k < kTeaTile; k += blockDim.x) {
+            const int jg = j0 + k;
+            if (jg < end) {
+                float4 q = B.frame_in[jg];
+                q.w = (B.flags[jg] & kFlagExtra) ? 0.0f : 1.0f;
+                s_pos[k] = q;
+            }
         }
         __syncthreads();
         if (valid && !extra_i) {
-            const int n = min(kTile, end - j0);
-            for (int t = 0; t < n; t++) {
+            const int n = min(kTeaTile, end - j0);
+#pragma unroll 4
+            for (int t = sl; t < n; t += slices) {
                 const float4 q = s_pos[t];
-                if (j0 + t == g || q.w != 0.0f) continue;
+                const float m = (j0 + t == g) ? 0.0f : q.w;
                 const float dx = q.x - pi.x, dy = q.y - pi.y, dz = q.z - pi.z;
-                float cii, crr, rinv;
-                rpy_coeffs(dx * dx + dy * dy + dz * dz, inv_a, a, cii, crr, rinv);
-                const float ux = dx * rinv, uy = dy * rinv, uz = dz * rinv;
-                const float xx = ux * ux * crr + cii, yy = uy * uy * crr + cii, zz = uz * uz * crr + cii;
-                const float xy = ux * uy * crr, xz = ux * uz * crr, yz = uy * uz * crr;
-                sw += xx + yy + zz + 2.0f * (xy + xz + yz);
+                float cii, crr_r2, rinv;
+                rpy_pair(dx * dx + dy * dy + dz * dz, a, inv_a, cii, crr_r2, rinv);
+                cii *= m;
+                crr_r2 *= m;
+                const float xx = fmaf(dx * dx, crr_r2, cii), yy = fmaf(dy * dy, crr_r2, cii),
+                            zz = fmaf(dz * dz, crr_r2, cii);
+                const float xy = dx * dy * crr_r2, xz = dx * dz * crr_r2, yz = dy * dz * crr_r2;
+                sw += (xx + yy + zz) + 2.0f * (xy + xz + yz);
                 sx += xx * xx + xy * xy + xz * xz;
                 sy += xy * xy + yy * yy + yz * yz;
                 sz += xz * xz + yz * yz + zz * zz;
@@ -71,9 +87,19 @@ __global__ void __launch_bounds__(kTile) k_tea_eps(KParams P, DevBuffers B, cons
         }
         __syncthreads();
     }
-    if (valid) {
-        B.tea_ci[g] = make_float4(sx, sy, sz, 0.f);
-        B.tea_eps[g] = sw;
+    s_red[threadIdx.x] = make_float4(sx, sy, sz, sw);
+    __syncthreads();
+    if (sl == 0 && valid) {
+        float4 acc = s_red[il];
+        for (int k = 1; k < slices; k++) {
+            const float4 v = s_red[k * kTeaI + il];
+            acc.x += v.x;
+            acc.y += v.y;
+            acc.z += v.z;
+            acc.w += v.w;
+        }
+        B.tea_ci[g] = make_float4(acc.x, acc.y, acc.z, 0.f);
+        B.tea_eps[g] = acc.w;
     }
 }
 
@@ -135,13 +161,16 @@ __global__ void __launch_bounds__(256) k_tea_beta(KParams P, DevBuffers B, int c
 // f_i = F_i + C_i o R_i + sum_{j != i, non-extra} T_ij (F_j + beta C_i o R_j),
 // x_i += dt/gammaR f_i; angles by Euler-Maruyama from stream i + nb, which is
 // drawn for every bead.  Reads the current frame, writes the next one.
-__global__ void __launch_bounds__(kTile) k_tea_step(KParams P, DevBuffers B, const int2 *work) {
+__global__ void __launch_bounds__(512) k_tea_step(KParams P, DevBuffers B, const int2 *work) {
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
-    const int g = w.y + threadIdx.x;
+    const int slices = blockDim.x / kTeaI;
+    const int il = threadIdx.x % kTeaI, sl = threadIdx.x / kTeaI;
+    const int g = w.y + il;
     const bool valid = g < end;
     const int nb = P.nb;
-    __shared__ float4 s_pos[kTile], s_f[kTile], s_r[kTile];
+    __shared__ float4 s_pos[kTeaTile], s_f[kTeaTile], s_r[kTeaTile];
+    __shared__ float4 s_red[512];
 
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
     int flags = kFlagExtra;
@@ -150,50 +179,63 @@ __global__ void __launch_bounds__(kTile) k_tea_step(KParams P, DevBuffers B, con
         pi = B.frame_in[g];
         flags = B.flags[g];
         const float beta = B.tea_beta[traj], b2 = beta * beta;
-        const float4 ci = B.tea_ci[g], Fi = B.force[g], Ri = B.tea_r[g];
+        const float4 ci = B.tea_ci[g];
         const float cx = 1.0f / sqrtf(1.0f + b2 * ci.x);
         const float cy = 1.0f / sqrtf(1.0f + b2 * ci.y);
         const float cz = 1.0f / sqrtf(1.0f + b2 * ci.z);
-        fx = Fi.x + Ri.x * cx;
-        fy = Fi.y + Ri.y * cy;
-        fz = Fi.z + Ri.z * cz;
+        if (sl == 0) {
+            const float4 Fi = B.force[g], Ri = B.tea_r[g];
+            fx = Fi.x + Ri.x * cx;
+            fy = Fi.y + Ri.y * cy;
+            fz = Fi.z + Ri.z * cz;
+        }
         cbx = cx * beta;
         cby = cy * beta;
         cbz = cz * beta;
     }
     const bool extra_i = (flags & kFlagExtra) != 0;
     const float a = P.tea_a, inv_a = 1.0f / P.tea_a;
-    for (int j0 = base; j0 < end; j0 += kTile) {
-        const int jg = j0 + threadIdx.x;
-        if (jg < end) {
-            float4 q = B.frame_in[jg];
-            q.w = (B.flags[jg] & kFlagExtra) ? 1.0f : 0.0f;
-            s_pos[threadIdx.x] = q;
-            s_f[threadIdx.x] = B.force[jg];
-            s_r[threadIdx.x] = B.tea_r[jg];
+    for (int j0 = base; j0 < end; j0 += kTeaTile) {
+        for (int k = threadIdx.x; k < kTeaTile; k += blockDim.x) {
+            const int jg = j0 + k;
+            if (jg < end) {
+                float4 q = B.frame_in[jg];
+                q.w = (B.flags[jg] & kFlagExtra) ? 0.0f : 1.0f;
+                s_pos[k] = q;
+                s_f[k] = B.force[jg];
+                s_r[k] = B.tea_r[jg];
+            }
         }
         __syncthreads();
         if (valid && !extra_i) {
-            const int n = min(kTile, end - j0);
+            const int n = min(kTeaTile, end - j0);
 #pragma unroll 4
-            for (int t = 0; t < n; t++) {
+            for (int t = sl; t < n; t += slices) {
                 const float4 q = s_pos[t];
-                if (j0 + t == g || q.w != 0.0f) continue;
+                const float m = (j0 + t == g) ? 0.0f : q.w;
                 const float4 Fj = s_f[t], Rj = s_r[t];
                 const float dx = q.x - pi.x, dy = q.y - pi.y, dz = q.z - pi.z;
-                float cii, crr, rinv;
-                rpy_coeffs(dx * dx + dy * dy + dz * dz, inv_a, a, cii, crr, rinv);
-                const float ux = dx * rinv, uy = dy * rinv, uz = dz * rinv;
-                const float gx = Fj.x + Rj.x * cbx, gy = Fj.y + Rj.y * cby, gz = Fj.z + Rj.z * cbz;
-                const float ug = crr * (ux * gx + uy * gy + uz * gz);
-                fx += cii * gx + ug * ux;
-                fy += cii * gy + ug * uy;
-                fz += cii * gz + ug * uz;
+                float cii, crr_r2, rinv;
+                rpy_pair(dx * dx + dy * dy + dz * dz, a, inv_a, cii, crr_r2, rinv);
+                cii *= m;
+                const float gx = fmaf(Rj.x, cbx, Fj.x), gy = fmaf(Rj.y, cby, Fj.y), gz = fmaf(Rj.z, cbz, Fj.z);
+                const float s = m * crr_r2 * (dx * gx + dy * gy + dz * gz);
+                fx = fmaf(cii, gx, fmaf(s, dx, fx));
+                fy = fmaf(cii, gy, fmaf(s, dy, fy));
+                fz = fmaf(cii, gz, fmaf(s, dz, fz));
             }
         }
         __syncthreads();
     }
-    if (!valid) return;
+    s_red[threadIdx.x] = make_float4(fx, fy, fz, 0.f);
+    __syncthreads();
+    if (sl != 0 || !valid) return;
+    for (int k = 1; k < slices; k++) {
+        const float4 v = s_red[k * kTeaI + il];
+        fx += v.x;
+        fy += v.y;
+        fz += v.z;
+    }
     Frame Fr;
     Fr.p0 = pi;
     Fr.p1 = B.frame_in[nb + g];
@@ -214,13 +256,13 @@ __global__ void __launch_bounds__(kTile) k_tea_step(KParams P, DevBuffers B, con
 }
 
 void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
-    k_tea_eps<<<nwork, kTile, 0, s>>>(P, B, work);
+    k_tea_eps<<<nwork, kTeaI * P.tea_slices, 0, s>>>(P, B, work);
 }
 void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s) {
     k_tea_beta<<<P.nt, 256, 0, s>>>(P, B, capricious, epsmax);
 }
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
-    k_tea_step<<<nwork, kTile, 0, s>>>(P, B, work);
+    k_tea_step<<<nwork, kTeaI * P.tea_slices, 0, s>>>(P, B, work);
 }
 
 }  // namespace mtg

@@ -200,6 +200,24 @@ void destroy_graphs(mtg_engine *e) {
     e->graph_slot_count[0] = e->graph_slot_count[1] = 0;
 }
 
+// The list rebuild with the engine's method.
+void launch_lists(mtg_engine *e) {
+    if (e->use_cells)
+        launch_rebuild_cells(e->kp, e->bufs(), e->cells(), e->work, e->nwork, e->stream);
+    else
+        launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+}
+
+void choose_list_method(mtg_engine *e) {
+    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat && e->cell_tbase;
+    if (e->list_method == 1 || !cells_ok)
+        e->use_cells = false;
+    else if (e->list_method == 2)
+        e->use_cells = true;
+    else
+        e->use_cells = e->max_traj_beads >= 512;
+}
+
 // Event slot for one timed launch (created outside any stream capture).
 int timing_slot(mtg_engine *e, int kind) {
     int &next = e->capturing ? e->capture_next : e->direct_next;
@@ -237,16 +255,16 @@ void timed_launch(mtg_engine *e, int kind, F &&launch) {
 void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
     const mtg_params &p = e->p;
     if (allow_rebuild && step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
-        timed_launch(e, 0, [&] { launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream); });
+        timed_launch(e, 0, [&] { launch_lists(e); });
         e->lists_valid = true;
     }
     if (p.hdi_on) {
         timed_launch(e, 2, [&] { launch_forces(e->kp, e->bufs(), true, e->stream); });
         if (step % p.tea_epsilon_freq == 0) {
-            timed_launch(e, 3, [&] { launch_tea_eps(e->kp, e->bufs(), e->work, e->nwork, e->stream); });
+            timed_launch(e, 3, [&] { launch_tea_eps(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
             timed_launch(e, 4, [&] { launch_tea_beta(e->kp, e->bufs(), p.tea_capricious, p.tea_epsmax, e->stream); });
         }
-        timed_launch(e, 5, [&] { launch_tea_step(e->kp, e->bufs(), e->work, e->nwork, e->stream); });
+        timed_launch(e, 5, [&] { launch_tea_step(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
     } else {
         timed_launch(e, 1, [&] { launch_step_plain(e->kp, e->bufs(), e->keep_forces, e->stream); });
     }
@@ -376,6 +394,19 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
     }
     work_first[nt] = (int)work.size();
     e->nwork = (int)work.size();
+    std::vector<int2> tea_work;
+    for (int tr = 0; tr < nt; tr++)
+        for (int g = t->offsets[tr]; g < t->offsets[tr + 1]; g += kTeaChunk) tea_work.push_back(make_int2(tr, g));
+    e->tea_nwork = (int)tea_work.size();
+    // threads per bead in the all-pairs TEA kernels: enough to fill the GPU
+    {
+        int dev = p->device, sms = 148;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const double target = (double)sms * 2048.0 * 2.0;
+        int sl = 1;
+        while (sl < 8 && (double)nb * sl < target) sl <<= 1;
+        e->kp.tea_slices = sl;
+    }
 
 #define ALLOC(ptr, n)                         \
     do {                                      \
@@ -412,14 +443,39 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
     ALLOC(e->stage_u8, nb);
     ALLOC(e->stage_i, nb);
     if (p->hdi_on) {
+        ALLOC(e->tea_work, e->tea_nwork);
         ALLOC(e->tea_r, nb);
         ALLOC(e->tea_ci, nb);
         ALLOC(e->tea_eps, nb);
         ALLOC(e->tea_beta, nt);
         ALLOC(e->tea_eps_t, nt);
     }
+    // spatial-hash tables of the cell-list rebuild
+    std::vector<int> tbase(nt + 1, 0), tmask(nt, 0);
+    for (int tr = 0; tr < nt; tr++) {
+        const int n = t->offsets[tr + 1] - t->offsets[tr];
+        e->max_traj_beads = n > e->max_traj_beads ? n : e->max_traj_beads;
+        int size = 32;
+        while (size < n) size <<= 1;
+        tbase[tr + 1] = tbase[tr] + size;
+        tmask[tr] = size - 1;
+    }
+    e->cell_nbuckets = tbase[nt];
+    ALLOC(e->cell_tbase, nt + 1);
+    ALLOC(e->cell_tmask, nt);
+    ALLOC(e->cell_key, nb);
+    ALLOC(e->cell_bead, nb);
+    ALLOC(e->cell_cnt, e->cell_nbuckets);
+    ALLOC(e->cell_start, e->cell_nbuckets);
+    ALLOC(e->cell_cursor, e->cell_nbuckets);
 #undef ALLOC
     cudaStream_t s = e->stream;
+    if ((rc = upload(e->cell_tbase, tbase.data(), sizeof(int) * (nt + 1), s)) ||
+        (rc = upload(e->cell_tmask, tmask.data(), sizeof(int) * nt, s))) {
+        mtg_destroy(e);
+        return rc;
+    }
+    choose_list_method(e);
     std::vector<float> zs(nt, 0.f);
     if (t->zs) zs.assign(t->zs, t->zs + nt);
     if ((rc = upload(e->off, t->offsets, sizeof(int) * (nt + 1), s)) || (rc = upload(e->traj, traj.data(), sizeof(int) * nb, s)) ||
@@ -437,6 +493,10 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
     cudaMemsetAsync(e->latc, 0, sizeof(int) * nb, s);
     cudaMemsetAsync(e->force, 0, sizeof(float4) * 2 * nb, s);
     if (p->hdi_on) {
+        if ((rc = upload(e->tea_work, tea_work.data(), sizeof(int2) * tea_work.size(), s)) != 0) {
+            mtg_destroy(e);
+            return rc;
+        }
         cudaMemsetAsync(e->tea_ci, 0, sizeof(float4) * nb, s);
         cudaMemsetAsync(e->tea_beta, 0, sizeof(float) * nt, s);
     }
@@ -541,7 +601,8 @@ int mtg_destroy(mtg_engine *e) {
     void *ptrs[] = {e->off, e->traj, e->flags, e->harm, e->zs, e->frame[0], e->frame[1], e->force, e->seeds,
                     e->ljc, e->lj, e->lonc, e->lon, e->latc, e->lat, e->err, e->work, e->work_first,
                     e->en_partials, e->en_traj, e->en_bead, e->tea_r, e->tea_ci, e->tea_eps, e->tea_beta,
-                    e->tea_eps_t, e->stage, e->stage_u8, e->stage_i};
+                    e->tea_eps_t, e->stage, e->stage_u8, e->stage_i, e->cell_tbase, e->cell_tmask,
+                    e->cell_key, e->cell_bead, e->cell_cnt, e->cell_start, e->cell_cursor, e->tea_work};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (e->stage_host) cudaFreeHost(e->stage_host);
@@ -662,7 +723,7 @@ int mtg_rebuild_pairs(mtg_engine *e) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
     cudaSetDevice(e->device);
     if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
-    if (e->p.lj_on || e->p.is_assembly) launch_rebuild(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+    if (e->p.lj_on || e->p.is_assembly) launch_lists(e);
     CK(cudaGetLastError());
     e->lists_valid = true;
     e->lists_fresh = true;
@@ -807,6 +868,23 @@ int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *devic
     return rc;
 }
 
+int mtg_set_list_method(mtg_engine *e, int method) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (method < 0 || method > 2) return fail(MTG_E_CONFIG, "list method must be 0 (auto), 1 (tiles) or 2 (cells)");
+    e->list_method = method;
+    choose_list_method(e);
+    if (method == 2 && !e->use_cells)
+        return fail(MTG_E_CONFIG, "the cell-list rebuild supports list capacities up to %d/%d", kCellMaxLong, kCellMaxLat);
+    destroy_graphs(e);
+    return MTG_OK;
+}
+
+int mtg_get_list_method(mtg_engine *e, int *method) {
+    if (!e || !method) return fail(MTG_E_CONFIG, "engine or method is NULL");
+    *method = e->use_cells ? 2 : 1;
+    return MTG_OK;
+}
+
 int mtg_set_kernel_timing(mtg_engine *e, int on) {
     if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
     cudaSetDevice(e->device);
@@ -867,7 +945,7 @@ int mtg_tea_update(mtg_engine *e, double *eps_out, float *beta_out, float *ci_ou
     cudaSetDevice(e->device);
     if (!e->p.hdi_on) return fail(MTG_E_STATE, "engine created without hdi_on");
     if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
-    launch_tea_eps(e->kp, e->bufs(), e->work, e->nwork, e->stream);
+    launch_tea_eps(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream);
     launch_tea_beta(e->kp, e->bufs(), e->p.tea_capricious, e->p.tea_epsmax, e->stream);
     CK(cudaGetLastError());
     if (eps_out) CK(cudaMemcpyAsync(eps_out, e->tea_eps_t, sizeof(double) * e->nt, cudaMemcpyDeviceToHost, e->stream));

@@ -30,6 +30,8 @@ struct mtg_engine {
     int *err = nullptr;
     int2 *work = nullptr;
     int nwork = 0;
+    int2 *tea_work = nullptr;   // chunks of kTeaChunk beads for the TEA kernels
+    int tea_nwork = 0;
     int *work_first = nullptr;
     double *en_partials = nullptr, *en_traj = nullptr, *en_bead = nullptr;
     float4 *tea_r = nullptr, *tea_ci = nullptr;
@@ -54,6 +56,26 @@ struct mtg_engine {
     double kt_total[MTG_KERNEL_KINDS] = {0};
     long long kt_count[MTG_KERNEL_KINDS] = {0};
     cudaEvent_t call_a = nullptr, call_b = nullptr;
+    // list rebuild method: 0 auto, 1 brute-force tiles, 2 cell list
+    int list_method = 0;
+    bool use_cells = false;
+    int max_traj_beads = 0;
+    int *cell_tbase = nullptr, *cell_tmask = nullptr, *cell_key = nullptr, *cell_cnt = nullptr;
+    int *cell_start = nullptr, *cell_cursor = nullptr, *cell_bead = nullptr;
+    int cell_nbuckets = 0;
+
+    mtg::CellBuffers cells() const {
+        mtg::CellBuffers c{};
+        c.nbuckets = cell_nbuckets;
+        c.tbase = cell_tbase;
+        c.tmask = cell_tmask;
+        c.key = cell_key;
+        c.cnt = cell_cnt;
+        c.start = cell_start;
+        c.cursor = cell_cursor;
+        c.cell_bead = cell_bead;
+        return c;
+    }
 
     DevBuffers bufs() const {
         DevBuffers b{};

@@ -59,6 +59,7 @@ struct KParams {
     int maxH, maxLong, maxLat, maxLJ;
     // TEA
     float tea_a, tea_var;
+    int tea_slices;        // threads per bead i in the all-pairs TEA kernels (1, 2, 4 or 8)
 };
 
 // Device buffers of one engine.
@@ -188,18 +189,34 @@ __device__ __forceinline__ float norm3_rn(float3 d) {
     return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z)));
 }
 
+// Spatial-hash buffers of the cell-list rebuild (kernels_cells.cu).
+struct CellBuffers {
+    int nbuckets;          // sum over trajectories of their table sizes
+    const int *tbase;      // [nt+1] first bucket of each trajectory's table
+    const int *tmask;      // [nt] table size - 1 (power of two)
+    int *key;              // [nb] bucket of each bead
+    int *cnt, *start, *cursor;  // [nbuckets]
+    int *cell_bead;        // [nb] beads in bucket order
+};
+constexpr int kCellMaxLong = 16;   // largest list capacities the cell rebuild buffers locally
+constexpr int kCellMaxLat = 32;
+
 // ------------------------------------------------------ host entry points
 // (kernel launchers, defined in the .cu files)
 void launch_frames_from_coords(const KParams &P, const float *coords7, float4 *frame, cudaStream_t s);
 void launch_coords_from_frames(const KParams &P, const float4 *frame, float *coords7, cudaStream_t s);
 void launch_forces_to_coords(const KParams &P, const float4 *force, float *coords7, cudaStream_t s);
 void launch_rebuild(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
+void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffers &C, const int2 *work, int nwork,
+                          cudaStream_t s);
 void launch_step_plain(const KParams &P, const DevBuffers &B, bool keep_forces, cudaStream_t s);
 void launch_forces(const KParams &P, const DevBuffers &B, bool tea_prepare, cudaStream_t s);
 void launch_energy(const KParams &P, const DevBuffers &B, double *per_bead, double *partials,
                    const int2 *work, int nwork, cudaStream_t s);
 void launch_energy_totals(const KParams &P, const double *partials, const int *work_first, double *per_traj,
                           int *err, cudaStream_t s);
+// TEA kernels run over their own work list: chunks of kTeaChunk beads.
+constexpr int kTeaChunk = 64;
 void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
 void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s);
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);

@@ -48,6 +48,8 @@ EXPORTS = {
     "mtg_host_free": (C.c_int, [C.c_void_p]),
     "mtg_energies_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mtg_measure_fp32_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "mtg_set_list_method": (C.c_int, [C.c_void_p, C.c_int]),
+    "mtg_get_list_method": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
 }
 
 KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step")
@@ -217,6 +219,15 @@ class Engine:
     # ---------------------------------------------------------------- compute
     def rebuild_pairs(self):
         check(self.lib.mtg_rebuild_pairs(self.h))
+
+    def set_list_method(self, method: int):
+        """0 auto, 1 brute-force tiles, 2 cell list."""
+        check(self.lib.mtg_set_list_method(self.h, method))
+
+    def list_method(self) -> int:
+        m = C.c_int()
+        check(self.lib.mtg_get_list_method(self.h, C.byref(m)))
+        return m.value
 
     def lists(self):
         """(counts, entries) per kind in the reference layout (bead-major, cap per bead)."""

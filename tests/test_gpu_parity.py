@@ -31,9 +31,11 @@ def test_seeds_match_reference_ran2(engine_mod, oracle_lib):
 
 
 @pytest.mark.parametrize("ragged", [False, True])
-def test_lists_bit_exact(engine_mod, oracle_lib, ragged):
+@pytest.mark.parametrize("method", [1, 2])
+def test_lists_bit_exact(engine_mod, oracle_lib, ragged, method):
     b = system_with_margin(seed=5, ntr=3)
     e = make_engine(engine_mod, b, force_ragged=ragged)
+    e.set_list_method(method)
     e.rebuild_pairs()
     L = oracle_lib.Oracle("orc").lists(b, b.coords)
     for k in ("lj", "long", "lat"):
@@ -215,3 +217,24 @@ def test_kernel_timing_in_graphs(engine_mod):
     assert 0 < kt["step_plain"][0] <= ms
     e.set_kernel_timing(False)
     assert e.step_timed(20, 15) > 0   # graph + direct launches without timing
+
+
+def test_cell_lists_equal_tile_lists_on_a_large_batch(engine_mod):
+    """The cell-list and the tiled rebuild evaluate identical FP32 expressions,
+    so their lists agree exactly on any state (no cutoff margin needed)."""
+    from mt_gb300 import synth
+    p = synth.default_params(seed=4)
+    b = synth.uniform_batch(p, 8, 40, 1000, seed=4, cube=100.0)
+    e = make_engine(engine_mod, b)
+    e.step(0, 20)                      # move off the generated geometry
+    e.set_list_method(1)
+    e.rebuild_pairs()
+    tiles = e.lists()
+    e.set_list_method(2)
+    e.rebuild_pairs()
+    cells = e.lists()
+    for k in ("lj", "long", "lat"):
+        assert np.array_equal(tiles[k][0], cells[k][0]), k
+        cnt, arr, cap = cells[k]
+        for i in range(e.nb):
+            assert np.array_equal(arr[cap * i:cap * i + cnt[i]], tiles[k][1][cap * i:cap * i + cnt[i]]), (k, i)
