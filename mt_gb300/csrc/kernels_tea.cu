@@ -37,69 +37,94 @@ constexpr int kTeaTile = 256;
 
 // integrateTea_epsilon_unlisted (src/bdhitea_kernel.cu:84-101): per bead i,
 // sum over non-extra j != i of the row sums of squared entries (-> tea_ci)
-// and of all nine entries (-> tea_eps).
-__global__ void __launch_bounds__(512) k_tea_eps(KParams P, DevBuffers B, const int2 *work) {
+// and of all nine entries (-> tea_eps).  With T = cii I + crr u u^T the row
+// sums of squares are cii^2 + (2 cii + crr) crr u_c^2 and the sum of all
+// entries is 3 cii + crr (u_x + u_y + u_z)^2.  Two beads i per thread, like
+// k_tea_step; extra j enter the tile flagged and are skipped.
+template <int SLICES>
+__global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work) {
+    constexpr int kHalf = kTeaI / 2;
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
-    const int slices = blockDim.x / kTeaI;
-    const int il = threadIdx.x % kTeaI, sl = threadIdx.x / kTeaI;
-    const int g = w.y + il;
-    const bool valid = g < end;
+    const int il = threadIdx.x % kHalf, sl = threadIdx.x / kHalf;
     __shared__ float4 s_pos[kTeaTile];
-    __shared__ float4 s_red[512];
-    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool extra_i = true;
-    if (valid) {
-        pi = B.frame_in[g];
-        extra_i = (B.flags[g] & kFlagExtra) != 0;
+    __shared__ float4 s_red[kTeaI * SLICES];
+    int gi[2];
+    bool act[2];
+    float4 pi[2];
+    float sx[2] = {0.f, 0.f}, sy[2] = {0.f, 0.f}, sz[2] = {0.f, 0.f}, sw[2] = {0.f, 0.f};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        gi[h] = w.y + il + h * kHalf;
+        act[h] = false;
+        pi[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (gi[h] < end) {
+            pi[h] = B.frame_in[gi[h]];
+            act[h] = (B.flags[gi[h]] & kFlagExtra) == 0;
+        }
     }
     const float a = P.tea_a, inv_a = 1.0f / P.tea_a;
-    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+    const float c075a = 0.75f * a, c05a3 = 0.5f * a * a * a, c15a3 = 1.5f * a * a * a, four_a2 = 4.0f * a * a;
+    const bool any_act = act[0] || act[1];
     for (int j0 = base; j0 < end; j0 += kTeaTile) {
-        for (int k = threadIdx.x; k < kTeaTile; k += blockDim.x) {
+        for (int k = threadIdx.x; k < kTeaTile; k += kHalf * SLICES) {
             const int jg = j0 + k;
             if (jg < end) {
                 float4 q = B.frame_in[jg];
-                q.w = (B.flags[jg] & kFlagExtra) ? 0.0f : 1.0f;
+                q.w = (B.flags[jg] & kFlagExtra) ? 1.0f : 0.0f;
                 s_pos[k] = q;
             }
         }
         __syncthreads();
-        if (valid && !extra_i) {
+        if (any_act) {
             const int n = min(kTeaTile, end - j0);
-#pragma unroll 4
-            for (int t = sl; t < n; t += slices) {
+#pragma unroll 2
+            for (int t = sl; t < n; t += SLICES) {
                 const float4 q = s_pos[t];
-                const float m = (j0 + t == g) ? 0.0f : q.w;
-                const float dx = q.x - pi.x, dy = q.y - pi.y, dz = q.z - pi.z;
-                float cii, crr_r2, rinv;
-                rpy_pair(dx * dx + dy * dy + dz * dz, a, inv_a, cii, crr_r2, rinv);
-                cii *= m;
-                crr_r2 *= m;
-                const float xx = fmaf(dx * dx, crr_r2, cii), yy = fmaf(dy * dy, crr_r2, cii),
-                            zz = fmaf(dz * dz, crr_r2, cii);
-                const float xy = dx * dy * crr_r2, xz = dx * dz * crr_r2, yz = dy * dz * crr_r2;
-                sw += (xx + yy + zz) + 2.0f * (xy + xz + yz);
-                sx += xx * xx + xy * xy + xz * xz;
-                sy += xy * xy + yy * yy + yz * yz;
-                sz += xz * xz + yz * yz + zz * zz;
+                if (q.w != 0.0f) continue;   // extra j
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    if (j0 + t == gi[h]) continue;
+                    const float dx = q.x - pi[h].x, dy = q.y - pi[h].y, dz = q.z - pi[h].z;
+                    const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1e-6f);
+                    const float rinv = rsqrtf(r2);
+                    const float qq = rinv * rinv;
+                    float cii = rinv * fmaf(c05a3, qq, c075a);
+                    float crr = rinv * fmaf(-c15a3, qq, c075a);
+                    if (r2 <= four_a2) {
+                        const float ra = r2 * rinv * inv_a;
+                        cii = 1.0f - (9.0f / 32.0f) * ra;
+                        crr = (3.0f / 32.0f) * ra;
+                    }
+                    const float A = cii * cii, Bc = fmaf(2.0f, cii, crr) * crr * qq;
+                    sx[h] = fmaf(Bc, dx * dx, sx[h] + A);
+                    sy[h] = fmaf(Bc, dy * dy, sy[h] + A);
+                    sz[h] = fmaf(Bc, dz * dz, sz[h] + A);
+                    const float us = dx + dy + dz;
+                    sw[h] = fmaf(crr * qq, us * us, fmaf(3.0f, cii, sw[h]));
+                }
             }
         }
         __syncthreads();
     }
-    s_red[threadIdx.x] = make_float4(sx, sy, sz, sw);
+#pragma unroll
+    for (int h = 0; h < 2; h++) s_red[(sl * 2 + h) * kHalf + il] = make_float4(sx[h], sy[h], sz[h], sw[h]);
     __syncthreads();
-    if (sl == 0 && valid) {
-        float4 acc = s_red[il];
-        for (int k = 1; k < slices; k++) {
-            const float4 v = s_red[k * kTeaI + il];
+    if (sl != 0) return;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        if (gi[h] >= end) continue;
+        float4 acc = s_red[h * kHalf + il];
+        for (int k = 1; k < SLICES; k++) {
+            const float4 v = s_red[(k * 2 + h) * kHalf + il];
             acc.x += v.x;
             acc.y += v.y;
             acc.z += v.z;
             acc.w += v.w;
         }
-        B.tea_ci[g] = make_float4(acc.x, acc.y, acc.z, 0.f);
-        B.tea_eps[g] = acc.w;
+        if (!act[h]) acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        B.tea_ci[gi[h]] = make_float4(acc.x, acc.y, acc.z, 0.f);
+        B.tea_eps[gi[h]] = acc.w;
     }
 }
 
@@ -157,112 +182,174 @@ __global__ void __launch_bounds__(256) k_tea_beta(KParams P, DevBuffers B, int c
     }
 }
 
+// One pair's contribution T_ij g to f, with d = r_j - r_i and r2 = |d|^2 > 0.
+// Far field (r > 2a, the common case): cii = 0.75 a/r (1 + 2a^2/(3r^2)),
+// crr/r^2 = 0.75 a/r^3 (1 - 2a^2/r^2), written in q = 1/r^2; the overlap
+// branch (r <= 2a) is rare and taken under a warp-divergent branch.
+__device__ __forceinline__ void tea_pair(float dx, float dy, float dz, float gx, float gy, float gz, float a,
+                                         float inv_a, float c075a, float c05a3, float c15a3, float four_a2,
+                                         float &fx, float &fy, float &fz) {
+    const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1e-6f);
+    const float rinv = rsqrtf(r2);
+    const float q = rinv * rinv;
+    float cii = rinv * fmaf(c05a3, q, c075a);
+    float crr_r2 = rinv * q * fmaf(-c15a3, q, c075a);
+    if (r2 <= four_a2) {
+        const float ra = r2 * rinv * inv_a;
+        cii = 1.0f - (9.0f / 32.0f) * ra;
+        crr_r2 = (3.0f / 32.0f) * ra * q;
+    }
+    const float s = crr_r2 * fmaf(dx, gx, fmaf(dy, gy, dz * gz));
+    fx = fmaf(cii, gx, fmaf(s, dx, fx));
+    fy = fmaf(cii, gy, fmaf(s, dy, fy));
+    fz = fmaf(cii, gz, fmaf(s, dz, fz));
+}
+
 // integrateTea_kernel_unlisted + integrateTea_force (src/bdhitea_kernel.cu:104-213):
 // f_i = F_i + C_i o R_i + sum_{j != i, non-extra} T_ij (F_j + beta C_i o R_j),
 // x_i += dt/gammaR f_i; angles by Euler-Maruyama from stream i + nb, which is
 // drawn for every bead.  Reads the current frame, writes the next one.
-__global__ void __launch_bounds__(512) k_tea_step(KParams P, DevBuffers B, const int2 *work) {
+// Each thread serves two beads i (il and il + kTeaI/2) against the tile's j,
+// so every shared-memory load feeds two pairs; extra beads enter the tile
+// with zero F and R and contribute nothing.
+template <int SLICES>
+__global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work) {
+    constexpr int kHalf = kTeaI / 2;
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
-    const int slices = blockDim.x / kTeaI;
-    const int il = threadIdx.x % kTeaI, sl = threadIdx.x / kTeaI;
-    const int g = w.y + il;
-    const bool valid = g < end;
+    const int il = threadIdx.x % kHalf, sl = threadIdx.x / kHalf;
     const int nb = P.nb;
     __shared__ float4 s_pos[kTeaTile], s_f[kTeaTile], s_r[kTeaTile];
-    __shared__ float4 s_red[512];
+    __shared__ float4 s_red[kTeaI * SLICES];
 
-    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
-    int flags = kFlagExtra;
-    float fx = 0.f, fy = 0.f, fz = 0.f, cbx = 0.f, cby = 0.f, cbz = 0.f;
-    if (valid) {
-        pi = B.frame_in[g];
-        flags = B.flags[g];
-        const float beta = B.tea_beta[traj], b2 = beta * beta;
-        const float4 ci = B.tea_ci[g];
-        const float cx = 1.0f / sqrtf(1.0f + b2 * ci.x);
-        const float cy = 1.0f / sqrtf(1.0f + b2 * ci.y);
-        const float cz = 1.0f / sqrtf(1.0f + b2 * ci.z);
-        if (sl == 0) {
-            const float4 Fi = B.force[g], Ri = B.tea_r[g];
-            fx = Fi.x + Ri.x * cx;
-            fy = Fi.y + Ri.y * cy;
-            fz = Fi.z + Ri.z * cz;
+    int gi[2];
+    bool act[2];
+    float4 pi[2];
+    float fx[2], fy[2], fz[2], cbx[2], cby[2], cbz[2];
+    const float beta = B.tea_beta[traj], b2 = beta * beta;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        gi[h] = w.y + il + h * kHalf;
+        pi[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+        fx[h] = fy[h] = fz[h] = 0.f;
+        cbx[h] = cby[h] = cbz[h] = 0.f;
+        act[h] = false;
+        if (gi[h] < end) {
+            pi[h] = B.frame_in[gi[h]];
+            act[h] = (B.flags[gi[h]] & kFlagExtra) == 0;
+            const float4 ci = B.tea_ci[gi[h]];
+            const float cx = 1.0f / sqrtf(1.0f + b2 * ci.x);
+            const float cy = 1.0f / sqrtf(1.0f + b2 * ci.y);
+            const float cz = 1.0f / sqrtf(1.0f + b2 * ci.z);
+            if (sl == 0) {
+                const float4 Fi = B.force[gi[h]], Ri = B.tea_r[gi[h]];
+                fx[h] = Fi.x + Ri.x * cx;
+                fy[h] = Fi.y + Ri.y * cy;
+                fz[h] = Fi.z + Ri.z * cz;
+            }
+            cbx[h] = cx * beta;
+            cby[h] = cy * beta;
+            cbz[h] = cz * beta;
         }
-        cbx = cx * beta;
-        cby = cy * beta;
-        cbz = cz * beta;
     }
-    const bool extra_i = (flags & kFlagExtra) != 0;
     const float a = P.tea_a, inv_a = 1.0f / P.tea_a;
+    const float c075a = 0.75f * a, c05a3 = 0.5f * a * a * a, c15a3 = 1.5f * a * a * a, four_a2 = 4.0f * a * a;
+    const bool any_act = act[0] || act[1];
     for (int j0 = base; j0 < end; j0 += kTeaTile) {
-        for (int k = threadIdx.x; k < kTeaTile; k += blockDim.x) {
+        for (int k = threadIdx.x; k < kTeaTile; k += kHalf * SLICES) {
             const int jg = j0 + k;
             if (jg < end) {
-                float4 q = B.frame_in[jg];
-                q.w = (B.flags[jg] & kFlagExtra) ? 0.0f : 1.0f;
-                s_pos[k] = q;
-                s_f[k] = B.force[jg];
-                s_r[k] = B.tea_r[jg];
+                s_pos[k] = B.frame_in[jg];
+                const bool ex = (B.flags[jg] & kFlagExtra) != 0;
+                s_f[k] = ex ? make_float4(0.f, 0.f, 0.f, 0.f) : B.force[jg];
+                s_r[k] = ex ? make_float4(0.f, 0.f, 0.f, 0.f) : B.tea_r[jg];
             }
         }
         __syncthreads();
-        if (valid && !extra_i) {
+        if (any_act) {
             const int n = min(kTeaTile, end - j0);
+            // the CTA's own beads (the self pairs) can only sit in this tile range
+            const bool self_tile = (w.y < j0 + n) && (w.y + kTeaI > j0);
+            if (!self_tile) {
 #pragma unroll 4
-            for (int t = sl; t < n; t += slices) {
-                const float4 q = s_pos[t];
-                const float m = (j0 + t == g) ? 0.0f : q.w;
-                const float4 Fj = s_f[t], Rj = s_r[t];
-                const float dx = q.x - pi.x, dy = q.y - pi.y, dz = q.z - pi.z;
-                float cii, crr_r2, rinv;
-                rpy_pair(dx * dx + dy * dy + dz * dz, a, inv_a, cii, crr_r2, rinv);
-                cii *= m;
-                const float gx = fmaf(Rj.x, cbx, Fj.x), gy = fmaf(Rj.y, cby, Fj.y), gz = fmaf(Rj.z, cbz, Fj.z);
-                const float s = m * crr_r2 * (dx * gx + dy * gy + dz * gz);
-                fx = fmaf(cii, gx, fmaf(s, dx, fx));
-                fy = fmaf(cii, gy, fmaf(s, dy, fy));
-                fz = fmaf(cii, gz, fmaf(s, dz, fz));
+                for (int t = sl; t < n; t += SLICES) {
+                    const float4 q = s_pos[t], Fj = s_f[t], Rj = s_r[t];
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        tea_pair(q.x - pi[h].x, q.y - pi[h].y, q.z - pi[h].z, fmaf(Rj.x, cbx[h], Fj.x),
+                                 fmaf(Rj.y, cby[h], Fj.y), fmaf(Rj.z, cbz[h], Fj.z), a, inv_a, c075a, c05a3, c15a3,
+                                 four_a2, fx[h], fy[h], fz[h]);
+                }
+            } else {
+                for (int t = sl; t < n; t += SLICES) {
+                    const float4 q = s_pos[t], Fj = s_f[t], Rj = s_r[t];
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        if (j0 + t != gi[h])
+                            tea_pair(q.x - pi[h].x, q.y - pi[h].y, q.z - pi[h].z, fmaf(Rj.x, cbx[h], Fj.x),
+                                     fmaf(Rj.y, cby[h], Fj.y), fmaf(Rj.z, cbz[h], Fj.z), a, inv_a, c075a, c05a3,
+                                     c15a3, four_a2, fx[h], fy[h], fz[h]);
+                }
             }
         }
         __syncthreads();
     }
-    s_red[threadIdx.x] = make_float4(fx, fy, fz, 0.f);
+#pragma unroll
+    for (int h = 0; h < 2; h++) s_red[(sl * 2 + h) * kHalf + il] = make_float4(fx[h], fy[h], fz[h], 0.f);
     __syncthreads();
-    if (sl != 0 || !valid) return;
-    for (int k = 1; k < slices; k++) {
-        const float4 v = s_red[k * kTeaI + il];
-        fx += v.x;
-        fy += v.y;
-        fz += v.z;
+    if (sl != 0) return;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int g = gi[h];
+        if (g >= end) continue;
+        float sx = fx[h], sy = fy[h], sz = fz[h];
+        for (int k = 1; k < SLICES; k++) {
+            const float4 v = s_red[(k * 2 + h) * kHalf + il];
+            sx += v.x;
+            sy += v.y;
+            sz += v.z;
+        }
+        const int flags = B.flags[g];
+        Frame Fr;
+        Fr.p0 = pi[h];
+        Fr.p1 = B.frame_in[nb + g];
+        Fr.p2 = B.frame_in[2 * nb + g];
+        Fr.p3 = B.frame_in[3 * nb + g];
+        uint4 s2 = B.seeds[nb + g];
+        const float4 ga = gauss4(s2);
+        B.seeds[nb + g] = s2;
+        if (!(flags & (kFlagExtra | kFlagFixed))) {
+            const float4 fa = B.force[nb + g];  // (ffi, ftheta, fpsi)
+            const float x = Fr.p0.x + P.kr * sx, y = Fr.p0.y + P.kr * sy, z = Fr.p0.z + P.kr * sz;
+            const float fi = Fr.p0.w + (P.kfi * fa.x + P.nfi * ga.x);
+            const float psi = Fr.p1.w + (P.kfi * fa.z + P.nfi * ga.y);
+            const float th = Fr.p2.w + (P.kth * fa.y + P.varTheta * ga.z);
+            Fr = make_frame(P, x, y, z, fi, th, psi);
+        }
+        store_frame(B.frame_out, nb, g, Fr);
     }
-    Frame Fr;
-    Fr.p0 = pi;
-    Fr.p1 = B.frame_in[nb + g];
-    Fr.p2 = B.frame_in[2 * nb + g];
-    Fr.p3 = B.frame_in[3 * nb + g];
-    uint4 s2 = B.seeds[nb + g];
-    const float4 ga = gauss4(s2);
-    B.seeds[nb + g] = s2;
-    if (!(flags & (kFlagExtra | kFlagFixed))) {
-        const float4 fa = B.force[nb + g];  // (ffi, ftheta, fpsi)
-        const float x = pi.x + P.kr * fx, y = pi.y + P.kr * fy, z = pi.z + P.kr * fz;
-        const float fi = pi.w + (P.kfi * fa.x + P.nfi * ga.x);
-        const float psi = Fr.p1.w + (P.kfi * fa.z + P.nfi * ga.y);
-        const float th = Fr.p2.w + (P.kth * fa.y + P.varTheta * ga.z);
-        Fr = make_frame(P, x, y, z, fi, th, psi);
-    }
-    store_frame(B.frame_out, nb, g, Fr);
 }
 
 void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
-    k_tea_eps<<<nwork, kTeaI * P.tea_slices, 0, s>>>(P, B, work);
+    const int t = kTeaI / 2 * P.tea_slices;
+    switch (P.tea_slices) {
+        case 1: k_tea_eps<1><<<nwork, t, 0, s>>>(P, B, work); break;
+        case 2: k_tea_eps<2><<<nwork, t, 0, s>>>(P, B, work); break;
+        case 4: k_tea_eps<4><<<nwork, t, 0, s>>>(P, B, work); break;
+        default: k_tea_eps<8><<<nwork, t, 0, s>>>(P, B, work); break;
+    }
 }
 void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s) {
     k_tea_beta<<<P.nt, 256, 0, s>>>(P, B, capricious, epsmax);
 }
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
-    k_tea_step<<<nwork, kTeaI * P.tea_slices, 0, s>>>(P, B, work);
+    const int t = kTeaI / 2 * P.tea_slices;
+    switch (P.tea_slices) {
+        case 1: k_tea_step<1><<<nwork, t, 0, s>>>(P, B, work); break;
+        case 2: k_tea_step<2><<<nwork, t, 0, s>>>(P, B, work); break;
+        case 4: k_tea_step<4><<<nwork, t, 0, s>>>(P, B, work); break;
+        default: k_tea_step<8><<<nwork, t, 0, s>>>(P, B, work); break;
+    }
 }
 
 }  // namespace mtg

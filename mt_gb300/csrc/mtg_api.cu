@@ -402,9 +402,10 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
     {
         int dev = p->device, sms = 148;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const double target = (double)sms * 2048.0 * 2.0;
+        // two beads per thread; aim for about two full waves at 64 registers
+        const double target = (double)sms * 2048.0;
         int sl = 1;
-        while (sl < 8 && (double)nb * sl < target) sl <<= 1;
+        while (sl < 8 && (double)nb / 2 * sl < target) sl <<= 1;
         e->kp.tea_slices = sl;
     }
 
