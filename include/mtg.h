@@ -255,6 +255,49 @@ int mtg_tea_update(mtg_engine *e, double *eps_out, float *beta_out, float *ci_ou
  * engine's stream; mtg_sync() waits for it and reports a non-finite total. */
 int mtg_energies_noalloc(mtg_engine *e, double *d_per_traj);
 
+/* ---- learned TEA ------------------------------------------------------- */
+/* A small network (32 -> 128 -> 128 -> 128 -> 4, SiLU; BF16 weights and
+ * activations, FP32 accumulation on the tensor cores; Adam on FP32 master
+ * weights) that predicts each bead's TEA coefficients C_i (3 components) and
+ * its trajectory's beta from a 32-feature neighbourhood descriptor, so the
+ * O(N^2) epsilon pass (src/bdhitea_kernel.cu:84-101, src/bdhitea.cu:57-118)
+ * is skipped.  No reference counterpart. */
+typedef struct mtg_surrogate mtg_surrogate;
+#define MTG_SURROGATE_FEATURES 32
+#define MTG_SURROGATE_OUTPUTS 4
+#define MTG_SURROGATE_PARAMS 37764   /* weights and biases, see mtg_surrogate_get_params */
+int mtg_surrogate_create(int device, int seed, mtg_surrogate **out);
+int mtg_surrogate_destroy(mtg_surrogate *s);
+/* params [MTG_SURROGATE_PARAMS] = w1[128][32], w2[128][128], w3[128][128],
+ * w4[4][128], b1[128], b2[128], b3[128], b4[4] (FP32 masters);
+ * norm [72] = feature means[32], feature inverse std[32], target means[4],
+ * target std[4].  Either pointer may be NULL. */
+int mtg_surrogate_get_params(mtg_surrogate *s, float *params, float *norm);
+int mtg_surrogate_set_params(mtg_surrogate *s, const float *params, const float *norm);
+/* Fits the normalisation to (X [n*32] raw features, T [n*4] targets), then
+ * trains with Adam (mini-batches of `batch`, a multiple of 128; samples
+ * shuffled per epoch with `seed`).  loss_per_epoch [epochs] (may be NULL):
+ * mean squared error in normalised target units. */
+int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n, int epochs, int batch, float lr,
+                        int seed, float *loss_per_epoch);
+/* Y [n*4] = predictions in target units for raw features X [n*32]. */
+int mtg_surrogate_predict(mtg_surrogate *s, const float *X, int n, float *Y);
+/* Loss (normalised units) and parameter gradient [MTG_SURROGATE_PARAMS] of
+ * one batch, without an update (for gradient checks). */
+int mtg_surrogate_loss_grad(mtg_surrogate *s, const float *X, const float *T, int n, double *loss, float *grad);
+/* Descriptors X [nbeads*32] of the current state and, with TEA on, the
+ * exact targets T [nbeads*4] = (C_i, beta) from a fresh epsilon pass. */
+int mtg_tea_training_data(mtg_engine *e, float *X, float *T);
+/* Puts the surrogate in charge of C_i and beta (s == NULL: exact TEA again).
+ * Every recheck_every steps (0: never) the exact pass runs beside it and the
+ * effective TEA forces of both, under identical forces and random forces,
+ * are compared; when their RMS difference relative to the exact ones
+ * exceeds max_err the engine falls back to exact TEA for good. */
+int mtg_set_surrogate(mtg_engine *e, mtg_surrogate *s, int recheck_every, float max_err);
+/* fell_back: 1 after a fall-back; rechecks: re-checks done; last_error: the
+ * last re-check's RMS relative difference. */
+int mtg_surrogate_status(mtg_engine *e, int *fell_back, int *rechecks, double *last_error);
+
 /* ---- measurement ------------------------------------------------------- */
 /* mtg_step bracketed by CUDA events recorded on the engine's stream;
  * *device_ms = the device time between them.  No reference counterpart (the
@@ -267,8 +310,9 @@ int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *devic
  * call replays a pair-list period graph more than once only its last replay
  * is counted; the call count below says how many launches were timed.)
  * Kinds: 0 pair-list rebuild, 1 fused plain step, 2 forces (+ TEA random
- * forces), 3 TEA epsilon pass, 4 TEA beta reduction, 5 TEA mobility step. */
-#define MTG_KERNEL_KINDS 6
+ * forces), 3 TEA epsilon pass, 4 TEA beta reduction, 5 TEA mobility step,
+ * 6 learned-TEA descriptors + network + C_i/beta, 7 learned-TEA re-check. */
+#define MTG_KERNEL_KINDS 8
 int mtg_set_kernel_timing(mtg_engine *e, int on);
 int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int reset);
 

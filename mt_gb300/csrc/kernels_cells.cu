@@ -22,16 +22,6 @@ namespace {
 constexpr float kPairReach = 6.6f;  // see kPairPrefilter in kernels_lists.cu
 constexpr int kLocalLJ = 64;        // LJ entries sorted in local memory; more -> sorted in place
 
-__device__ __forceinline__ int cell_coord(float x, float inv) {
-    float c = floorf(x * inv);
-    c = fminf(fmaxf(c, -1048576.0f), 1048576.0f);  // NaN -> -2^20 (fmaxf drops NaN)
-    return (int)c;
-}
-
-__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz) {
-    return ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ ((uint32_t)cz * 83492791u);
-}
-
 __global__ void k_cell_count(KParams P, const float4 *pos, const int *traj, const int *tbase, const int *tmask,
                              float inv_cell, int *key, int *cnt) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -241,16 +231,21 @@ inline int nblk(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
 
-void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffers &C, const int2 *work, int nwork,
-                          cudaStream_t s) {
+float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, float reach, cudaStream_t s) {
     // cells slightly larger than the reach, so that rounding of x / edge can
     // never put two beads closer than the reach two cells apart
-    const float reach = fmaxf(P.lj_on ? P.ljcut : 0.f, P.is_assembly ? kPairReach : 0.f);
     const float inv = 1.0f / (reach * 1.001f + 1e-3f);
     cudaMemsetAsync(C.cnt, 0, sizeof(int) * C.nbuckets, s);
     k_cell_count<<<nblk(P.nb, 256), 256, 0, s>>>(P, B.frame_in, B.traj, C.tbase, C.tmask, inv, C.key, C.cnt);
     k_cell_scan<<<P.nt, 1024, 0, s>>>(C.tbase, C.cnt, C.start, C.cursor);
     k_cell_fill<<<nblk(P.nb, 256), 256, 0, s>>>(P.nb, B.traj, B.off, C.key, C.cursor, C.cell_bead);
+    return inv;
+}
+
+void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffers &C, const int2 *work, int nwork,
+                          cudaStream_t s) {
+    const float reach = fmaxf(P.lj_on ? P.ljcut : 0.f, P.is_assembly ? kPairReach : 0.f);
+    const float inv = bin_beads(P, B, C, reach, s);
     k_cell_lists<<<nwork, kTile, 0, s>>>(P, B, work, C.tbase, C.tmask, C.start, C.cnt, C.cell_bead, inv);
 }
 

@@ -42,7 +42,9 @@ constexpr int kTeaTile = 256;
 // entries is 3 cii + crr (u_x + u_y + u_z)^2.  Two beads i per thread, like
 // k_tea_step; extra j enter the tile flagged and are skipped.
 template <int SLICES>
-__global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work) {
+__global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work,
+                                                                 const int *gate, int run_if) {
+    if (gate && *gate != run_if) return;
     constexpr int kHalf = kTeaI / 2;
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
@@ -133,7 +135,9 @@ __global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_eps(KParams P, DevBu
 // eps = sum / (3N'(3N'-3)), clamped to 1; a = (3N'-1) eps^2 - (3N'-2) eps;
 // beta = (1 - sqrt(1 - a)) / a, or 0.5 when |a| < 1e-7.  The reference's
 // exits become the kErrTeaEps bit.
-__global__ void __launch_bounds__(256) k_tea_beta(KParams P, DevBuffers B, int capricious, float epsmax) {
+__global__ void __launch_bounds__(256) k_tea_beta(KParams P, DevBuffers B, int capricious, float epsmax,
+                                                  const int *gate, int run_if) {
+    if (gate && *gate != run_if) return;
     const int t = blockIdx.x;
     const int base = B.off[t], end = B.off[t + 1];
     double s = 0.0;
@@ -212,8 +216,10 @@ __device__ __forceinline__ void tea_pair(float dx, float dy, float dz, float gx,
 // Each thread serves two beads i (il and il + kTeaI/2) against the tile's j,
 // so every shared-memory load feeds two pairs; extra beads enter the tile
 // with zero F and R and contribute nothing.
-template <int SLICES>
-__global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work) {
+template <int SLICES, bool FEFF>
+__global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work,
+                                                                  float4 *feff, const int *gate) {
+    if (FEFF && gate && *gate != 0) return;
     constexpr int kHalf = kTeaI / 2;
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
@@ -309,6 +315,10 @@ __global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevB
             sy += v.y;
             sz += v.z;
         }
+        if (FEFF) {
+            feff[g] = make_float4(sx, sy, sz, 0.f);
+            continue;
+        }
         const int flags = B.flags[g];
         Frame Fr;
         Fr.p0 = pi[h];
@@ -330,26 +340,43 @@ __global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevB
     }
 }
 
-void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
+void launch_tea_eps_gated(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
+                          int run_if, cudaStream_t s) {
     const int t = kTeaI / 2 * P.tea_slices;
     switch (P.tea_slices) {
-        case 1: k_tea_eps<1><<<nwork, t, 0, s>>>(P, B, work); break;
-        case 2: k_tea_eps<2><<<nwork, t, 0, s>>>(P, B, work); break;
-        case 4: k_tea_eps<4><<<nwork, t, 0, s>>>(P, B, work); break;
-        default: k_tea_eps<8><<<nwork, t, 0, s>>>(P, B, work); break;
+        case 1: k_tea_eps<1><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
+        case 2: k_tea_eps<2><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
+        case 4: k_tea_eps<4><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
+        default: k_tea_eps<8><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
     }
+}
+void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
+    launch_tea_eps_gated(P, B, work, nwork, nullptr, 0, s);
+}
+void launch_tea_beta_gated(const KParams &P, const DevBuffers &B, int capricious, float epsmax, const int *gate,
+                           int run_if, cudaStream_t s) {
+    k_tea_beta<<<P.nt, 256, 0, s>>>(P, B, capricious, epsmax, gate, run_if);
 }
 void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s) {
-    k_tea_beta<<<P.nt, 256, 0, s>>>(P, B, capricious, epsmax);
+    launch_tea_beta_gated(P, B, capricious, epsmax, nullptr, 0, s);
 }
-void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
+template <bool FEFF>
+static void tea_step_dispatch(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, float4 *feff,
+                              const int *gate, cudaStream_t s) {
     const int t = kTeaI / 2 * P.tea_slices;
     switch (P.tea_slices) {
-        case 1: k_tea_step<1><<<nwork, t, 0, s>>>(P, B, work); break;
-        case 2: k_tea_step<2><<<nwork, t, 0, s>>>(P, B, work); break;
-        case 4: k_tea_step<4><<<nwork, t, 0, s>>>(P, B, work); break;
-        default: k_tea_step<8><<<nwork, t, 0, s>>>(P, B, work); break;
+        case 1: k_tea_step<1, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
+        case 2: k_tea_step<2, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
+        case 4: k_tea_step<4, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
+        default: k_tea_step<8, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
     }
+}
+void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
+    tea_step_dispatch<false>(P, B, work, nwork, nullptr, nullptr, s);
+}
+void launch_tea_feff(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, float4 *feff,
+                     const int *gate, cudaStream_t s) {
+    tea_step_dispatch<true>(P, B, work, nwork, feff, gate, s);
 }
 
 }  // namespace mtg

@@ -100,6 +100,9 @@ int dalloc(T **p, size_t n) {
 
 int mtg_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
 
+void destroy_graphs(mtg_engine *e);
+void mtg_internal_reset_graphs(mtg_engine *e) { destroy_graphs(e); }
+
 namespace {
 
 KParams make_kparams(const mtg_params &p, int nb, int nt, int maxH, int maxLong, int maxLat, int maxLJ) {
@@ -190,6 +193,8 @@ int check_errors(mtg_engine *e) {
     return MTG_OK;
 }
 
+}  // namespace
+
 void destroy_graphs(mtg_engine *e) {
     for (auto &g : e->graph)
         if (g) {
@@ -199,6 +204,8 @@ void destroy_graphs(mtg_engine *e) {
     e->direct_base = 0;
     e->graph_slot_count[0] = e->graph_slot_count[1] = 0;
 }
+
+namespace {
 
 // The list rebuild with the engine's method.
 void launch_lists(mtg_engine *e) {
@@ -260,7 +267,13 @@ void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
     }
     if (p.hdi_on) {
         timed_launch(e, 2, [&] { launch_forces(e->kp, e->bufs(), true, e->stream); });
-        if (step % p.tea_epsilon_freq == 0) {
+        if (e->surr) {
+            // learned TEA: the network replaces the epsilon pass; the exact
+            // re-check decides whether it stays in charge
+            if (step % p.tea_epsilon_freq == 0) timed_launch(e, 6, [&] { enqueue_surrogate_eps(e); });
+            if (e->surr_recheck > 0 && step % e->surr_recheck == 0)
+                timed_launch(e, 7, [&] { enqueue_surrogate_recheck(e); });
+        } else if (step % p.tea_epsilon_freq == 0) {
             timed_launch(e, 3, [&] { launch_tea_eps(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
             timed_launch(e, 4, [&] { launch_tea_beta(e->kp, e->bufs(), p.tea_capricious, p.tea_epsmax, e->stream); });
         }
@@ -603,7 +616,9 @@ int mtg_destroy(mtg_engine *e) {
                     e->ljc, e->lj, e->lonc, e->lon, e->latc, e->lat, e->err, e->work, e->work_first,
                     e->en_partials, e->en_traj, e->en_bead, e->tea_r, e->tea_ci, e->tea_eps, e->tea_beta,
                     e->tea_eps_t, e->stage, e->stage_u8, e->stage_i, e->cell_tbase, e->cell_tmask,
-                    e->cell_key, e->cell_bead, e->cell_cnt, e->cell_start, e->cell_cursor, e->tea_work};
+                    e->cell_key, e->cell_bead, e->cell_cnt, e->cell_start, e->cell_cursor, e->tea_work,
+                    e->surr_desc, e->surr_pred, e->surr_stats, e->surr_gate, e->surr_err, e->surr_part,
+                    e->tea_ci2, e->feff_a, e->feff_b, e->tea_eps2, e->tea_beta2, e->tea_eps_t2};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (e->stage_host) cudaFreeHost(e->stage_host);
@@ -776,12 +791,13 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
     const mtg_params &p = e->p;
     long long period = p.ljpairsupdatefreq;
     if (p.hdi_on) period = lcm_ll(period, p.tea_epsilon_freq);
+    if (p.hdi_on && e->surr && e->surr_recheck > 0) period = lcm_ll(period, e->surr_recheck);
     const bool use_graphs = period <= 256;
     if (e->graph_period != period) {
         destroy_graphs(e);
         e->graph_period = (int)period;
     }
-    const int max_launch_per_step = 5;
+    const int max_launch_per_step = 6;
     e->direct_next = e->direct_base;
     e->used_slots.clear();
     long long s = first_step;

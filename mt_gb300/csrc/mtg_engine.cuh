@@ -63,6 +63,17 @@ struct mtg_engine {
     int *cell_tbase = nullptr, *cell_tmask = nullptr, *cell_key = nullptr, *cell_cnt = nullptr;
     int *cell_start = nullptr, *cell_cursor = nullptr, *cell_bead = nullptr;
     int cell_nbuckets = 0;
+    // learned TEA (surrogate.cu)
+    struct mtg_surrogate *surr = nullptr;
+    int surr_recheck = 0;
+    float surr_max_err = 0.01f;
+    float *surr_desc = nullptr, *surr_pred = nullptr;
+    float4 *surr_stats = nullptr;
+    int *surr_gate = nullptr;      // [0] fell back to exact, [1] re-checks done, [2] fallback not yet applied
+    double *surr_err = nullptr, *surr_part = nullptr;
+    float4 *tea_ci2 = nullptr, *feff_a = nullptr, *feff_b = nullptr;
+    float *tea_eps2 = nullptr, *tea_beta2 = nullptr;
+    double *tea_eps_t2 = nullptr;
 
     mtg::CellBuffers cells() const {
         mtg::CellBuffers c{};
@@ -108,3 +119,10 @@ struct mtg_engine {
 // Records msg as the calling thread's last error (mtg_last_error_string) and
 // returns code.
 int mtg_internal_fail(int code, const char *msg);
+
+// learned TEA helpers (surrogate.cu)
+int mtg_surrogate_buffers(mtg_engine *e);
+void enqueue_surrogate_eps(mtg_engine *e);
+void enqueue_surrogate_recheck(mtg_engine *e);
+// drops the captured step graphs (after a mode change)
+void mtg_internal_reset_graphs(mtg_engine *e);

@@ -201,6 +201,16 @@ struct CellBuffers {
 constexpr int kCellMaxLong = 16;   // largest list capacities the cell rebuild buffers locally
 constexpr int kCellMaxLat = 32;
 
+// Cell of a coordinate for cells of edge 1/inv (NaN and far-away values clamp).
+__device__ __forceinline__ int cell_coord(float x, float inv) {
+    float c = floorf(x * inv);
+    c = fminf(fmaxf(c, -1048576.0f), 1048576.0f);  // NaN -> -2^20 (fmaxf drops NaN)
+    return (int)c;
+}
+__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz) {
+    return ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ ((uint32_t)cz * 83492791u);
+}
+
 // ------------------------------------------------------ host entry points
 // (kernel launchers, defined in the .cu files)
 void launch_frames_from_coords(const KParams &P, const float *coords7, float4 *frame, cudaStream_t s);
@@ -209,6 +219,9 @@ void launch_forces_to_coords(const KParams &P, const float4 *force, float *coord
 void launch_rebuild(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
 void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffers &C, const int2 *work, int nwork,
                           cudaStream_t s);
+// Bins the current positions into the per-trajectory spatial hash with cells
+// just larger than `reach`; returns 1/edge for the consumers' cell lookups.
+float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, float reach, cudaStream_t s);
 void launch_step_plain(const KParams &P, const DevBuffers &B, bool keep_forces, cudaStream_t s);
 void launch_forces(const KParams &P, const DevBuffers &B, bool tea_prepare, cudaStream_t s);
 void launch_energy(const KParams &P, const DevBuffers &B, double *per_bead, double *partials,
@@ -220,6 +233,14 @@ constexpr int kTeaChunk = 64;
 void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
 void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s);
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
+// gated variants: run only while *gate == run_if
+void launch_tea_eps_gated(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
+                          int run_if, cudaStream_t s);
+void launch_tea_beta_gated(const KParams &P, const DevBuffers &B, int capricious, float epsmax, const int *gate,
+                           int run_if, cudaStream_t s);
+// effective TEA force (no update) into feff, while *gate == 0
+void launch_tea_feff(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, float4 *feff,
+                     const int *gate, cudaStream_t s);
 void launch_set_flags(int nb, const uint8_t *extra, const int *gtp, const int *on_tubule, int *flags,
                       cudaStream_t s);
 

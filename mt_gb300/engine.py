@@ -50,9 +50,25 @@ EXPORTS = {
     "mtg_measure_fp32_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "mtg_set_list_method": (C.c_int, [C.c_void_p, C.c_int]),
     "mtg_get_list_method": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "mtg_surrogate_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "mtg_surrogate_destroy": (C.c_int, [C.c_void_p]),
+    "mtg_surrogate_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "mtg_surrogate_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "mtg_surrogate_train": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
+                                      C.c_int, C.c_float, C.c_int, C.POINTER(C.c_float)]),
+    "mtg_surrogate_predict": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float)]),
+    "mtg_surrogate_loss_grad": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int,
+                                          C.POINTER(C.c_double), C.POINTER(C.c_float)]),
+    "mtg_tea_training_data": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "mtg_set_surrogate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_float]),
+    "mtg_surrogate_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
 }
 
-KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step")
+SURROGATE_FEATURES = 32
+SURROGATE_OUTPUTS = 4
+SURROGATE_PARAMS = 37764
+
+KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step", "surrogate", "recheck")
 
 _lib = None
 
@@ -275,6 +291,22 @@ class Engine:
         check(self.lib.mtg_kernel_times(self.h, t, n, int(reset)))
         return {k: (t[i], n[i]) for i, k in enumerate(KERNEL_KINDS)}
 
+    def tea_training_data(self, targets: bool = True):
+        """(descriptors [nb, 32], targets [nb, 4] = C_i, beta) of the current state."""
+        X = np.zeros((self.nb, SURROGATE_FEATURES), np.float32)
+        T = np.zeros((self.nb, SURROGATE_OUTPUTS), np.float32) if targets else None
+        check(self.lib.mtg_tea_training_data(self.h, ptr(X, C.c_float), ptr(T, C.c_float)))
+        return X, T
+
+    def set_surrogate(self, surrogate, recheck_every: int = 100, max_err: float = 0.01):
+        check(self.lib.mtg_set_surrogate(self.h, surrogate.h if surrogate else None, recheck_every, max_err))
+        self._surrogate = surrogate
+
+    def surrogate_status(self):
+        fb, nr, err = C.c_int(), C.c_int(), C.c_double()
+        check(self.lib.mtg_surrogate_status(self.h, C.byref(fb), C.byref(nr), C.byref(err)))
+        return {"fell_back": bool(fb.value), "rechecks": nr.value, "last_error": err.value}
+
     def energies(self, per_bead: bool = False):
         pt = np.zeros((self.nt, 7), np.float64)
         pb = np.zeros((self.nb, 7), np.float64) if per_bead else None
@@ -287,3 +319,58 @@ class Engine:
         ci = np.zeros((self.nb, 4), np.float32)
         rc = self.lib.mtg_tea_update(self.h, ptr(eps, C.c_double), ptr(beta, C.c_float), ptr(ci, C.c_float))
         return eps, beta, ci, rc
+
+
+class Surrogate:
+    """The learned-TEA network (mtg_surrogate_*)."""
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.mtg_surrogate_create(device, seed, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mtg_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        p = np.zeros(SURROGATE_PARAMS, np.float32)
+        n = np.zeros(72, np.float32)
+        check(self.lib.mtg_surrogate_get_params(self.h, ptr(p, C.c_float), ptr(n, C.c_float)))
+        return p, n
+
+    def set_params(self, params=None, norm=None):
+        pp = None if params is None else np.ascontiguousarray(params, np.float32)
+        nn = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        check(self.lib.mtg_surrogate_set_params(self.h, ptr(pp, C.c_float), ptr(nn, C.c_float)))
+
+    def train(self, X, T, epochs: int = 20, batch: int = 4096, lr: float = 1e-3, seed: int = 0):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        losses = np.zeros(epochs, np.float32)
+        check(self.lib.mtg_surrogate_train(self.h, ptr(X, C.c_float), ptr(T, C.c_float), len(X), epochs, batch,
+                                           lr, seed, ptr(losses, C.c_float)))
+        return losses
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((len(X), SURROGATE_OUTPUTS), np.float32)
+        check(self.lib.mtg_surrogate_predict(self.h, ptr(X, C.c_float), len(X), ptr(Y, C.c_float)))
+        return Y
+
+    def loss_grad(self, X, T):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        g = np.zeros(SURROGATE_PARAMS, np.float32)
+        loss = C.c_double()
+        check(self.lib.mtg_surrogate_loss_grad(self.h, ptr(X, C.c_float), ptr(T, C.c_float), len(X), C.byref(loss),
+                                               ptr(g, C.c_float)))
+        return loss.value, g
