@@ -58,6 +58,13 @@ WORKLOADS = {
     "tea_exact_16x3300": dict(kind="tea", ntraj=16, n_mon=100, n_free=2000, cube=100.0),
     # exact TEA at the size of the learned-TEA comparison: 64 x (13 PF x 200 + 3000)
     "tea_exact_64x5600": dict(kind="tea", ntraj=64, n_mon=200, n_free=3000, cube=150.0),
+    # learned vs exact TEA: the network is trained on 1e6 samples of the
+    # 16 x 3300 exact-TEA system (Adam, batch 4096, 20 epochs), then both run
+    # 64 x (13 PF x 200 + 3000) with an exact re-check every 100 steps
+    "tea_learned_vs_exact_64x5600": dict(kind="tea_compare", ntraj=64, n_mon=200, n_free=3000, cube=150.0,
+                                         train=dict(ntraj=16, n_mon=100, n_free=2000, cube=100.0),
+                                         samples=1_000_000, epochs=20, batch=4096, lr=1e-3, recheck=100,
+                                         max_err=0.01),
 }
 DEFAULT_WORKLOAD = "batched_plain_256x1520"
 
@@ -170,7 +177,7 @@ def measured_peaks():
 
 def workload_params(spec: dict, seed: int):
     from mt_gb300 import synth
-    if spec["kind"] == "tea":
+    if spec["kind"] in ("tea", "tea_compare"):
         return synth.default_params(seed=seed, hdi_on=1, tea_a=2.0, tea_epsilon_freq=10)
     return synth.default_params(seed=seed)
 
@@ -385,6 +392,154 @@ def run_gpu(args, spec, dist):
     return out
 
 
+def train_surrogate(spec: dict, device: int, seed: int):
+    """Exact-TEA runs of the training system -> (descriptor, C_i, beta) samples -> network."""
+    from mt_gb300 import engine
+    tr = dict(spec["train"], kind="tea")
+    b = make_batch(tr, seed + 1000)
+    b.params.device = device
+    e = engine.Engine(b)
+    e.upload_state(b.coords)
+    Xs, Ts, step, n = [], [], 0, 0
+    t0 = time.perf_counter()
+    while n < spec["samples"]:
+        e.step(step, 10)
+        step += 10
+        X, T = e.tea_training_data()
+        Xs.append(X)
+        Ts.append(T)
+        n += len(X)
+    e.close()
+    X = np.concatenate(Xs)[:spec["samples"]]
+    T = np.concatenate(Ts)[:spec["samples"]]
+    t_data = time.perf_counter() - t0
+    s = engine.Surrogate(device=device, seed=seed)
+    t0 = time.perf_counter()
+    losses = s.train(X, T, epochs=spec["epochs"], batch=spec["batch"], lr=spec["lr"], seed=seed)
+    t_train = time.perf_counter() - t0
+    # the gain over the method without the network: mean-target predictor on held-out samples
+    hold = slice(0, min(len(X), 50_000))
+    pred = s.predict(X[hold])
+    rms_net = np.sqrt(((pred - T[hold]) ** 2).mean(0)).tolist()
+    rms_mean = np.sqrt(((T.mean(0) - T[hold]) ** 2).mean(0)).tolist()
+    info = {"samples": int(len(X)), "md_steps_of_exact_tea": step, "data_s": t_data, "train_s": t_train,
+            "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1]),
+            "rms_err_net_(Cx,Cy,Cz,beta)": rms_net, "rms_err_mean_predictor": rms_mean}
+    return s, info
+
+
+def run_tea_compare(args, spec, dist):
+    import torch
+
+    from mt_gb300 import build as mbuild
+    from mt_gb300 import engine
+
+    mbuild.build()
+    torch.cuda.set_device(dist.local)
+    seed = 1 + dist.rank
+    surr, train_info = train_surrogate(spec, dist.local, seed)
+    b = make_batch(spec, seed)
+    b.params.device = dist.local
+    period = int(spec["recheck"])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dist.local}")
+    active = b.active_beads()
+    results = {}
+    for mode in ("exact", "learned"):
+        e = engine.Engine(b)
+        e.upload_state(b.coords)
+        if mode == "learned":
+            e.set_surrogate(surr, recheck_every=period, max_err=spec["max_err"])
+        step = 0
+        for _ in range(args.warmup):
+            e.step(step, period)
+            step += period
+        e.set_kernel_timing(True)
+        e.step(step, period)
+        step += period
+        e.kernel_times(reset=True)
+        clocks = ClockSampler(dist.local)
+        clocks.start()
+        dist.barrier()
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ms.append(e.step_timed(step, period))
+            step += period
+        dist.barrier()
+        clk = clocks.stop()
+        kt = e.kernel_times(reset=True)
+        e.set_kernel_timing(False)
+        t_max = dist.max(sum(ms))
+        value = dist.sum(active * period * args.steps) / (t_max / 1e3)
+        res = {"value": value, "ms_per_step": t_max / args.steps, "clocks": clk,
+               "kernel_ms": {k: (v[0] / v[1] if v[1] else None) for k, v in kt.items()},
+               "kernel_share": {k: v[0] / max(1e-12, sum(x[0] for x in kt.values())) for k, v in kt.items()},
+               "gpu_launches": int(sum(v[1] for v in kt.values())), "kt": kt}
+        if mode == "learned":
+            res["status"] = e.surrogate_status()
+        # e2e through the C ABI with pinned host buffers (one re-check period per step)
+        import ctypes as C
+        pin = engine.PinnedArray((e.nb, 7), np.float32)
+        pin.array[:] = e.download_state()
+        lib = engine.load()
+        fptr = pin.array.ctypes.data_as(C.POINTER(C.c_float))
+        tt = []
+        for _ in range(max(2, args.steps)):
+            t0 = time.perf_counter()
+            engine.check(lib.mtg_upload_state(e.h, fptr))
+            engine.check(lib.mtg_step(e.h, C.c_longlong(step), C.c_int(period)))
+            engine.check(lib.mtg_download_state(e.h, fptr, C.cast(None, C.POINTER(C.c_float))))
+            tt.append(time.perf_counter() - t0)
+            step += period
+        res["e2e"] = {"value": dist.sum(active * period * len(tt)) / dist.max(sum(tt)), "unit": UNIT,
+                      "h2d_bytes_per_step": 28 * e.nb, "d2h_bytes_per_step": 28 * e.nb}
+        pin.free()
+        e.close()
+        results[mode] = res
+    # roofline of the dominant kernel (the all-pairs mobility product)
+    import ctypes as C
+    tf = C.c_double()
+    engine.check(engine.load().mtg_measure_fp32_tflops(dist.local, C.byref(tf)))
+    kt = results["learned"]["kt"]
+    avg = kt["tea_step"][0] / max(1, kt["tea_step"][1])
+    work = 45.0 * tea_pairs(b)
+    achieved = work / (avg / 1e3) / 1e12
+    learned_ok = not results["learned"]["status"]["fell_back"]
+    out = None
+    if dist.rank == 0:
+        cpu = cpu_sample(dict(spec, kind="tea"), seed) if dist.ws == 1 and not args.no_cpu_baseline else None
+        L, X = results["learned"], results["exact"]
+        out = {
+            "metric": METRIC, "value": L["value"] if learned_ok else X["value"], "unit": UNIT, "n_gpus": dist.ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": L["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network: bf16/f32)",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "trajectories_per_gpu": b.ntraj, "beads_per_gpu": b.nbeads,
+                       "md_steps_per_bench_step": period, "recheck_every": period, "max_mobility_error": spec["max_err"],
+                       "l2": "flushed (256 MB write) before every timed step",
+                       "parallelism": f"replicas x{dist.ws} (independent trajectories)"},
+            "learned_tea": {"value": L["value"], "fell_back": not learned_ok,
+                            "mobility_error_last_recheck": L["status"]["last_error"],
+                            "rechecks": L["status"]["rechecks"], "kernel_ms": L["kernel_ms"],
+                            "kernel_share": L["kernel_share"]},
+            "exact_tea": {"value": X["value"], "ms_per_step": X["ms_per_step"], "kernel_ms": X["kernel_ms"],
+                          "kernel_share": X["kernel_share"], "e2e": X["e2e"]},
+            "learned_over_exact": L["value"] / X["value"],
+            "surrogate_training": train_info,
+            "roofline": {"bound": "fp32", "kernel": "k_tea_step", "achieved": achieved, "peak": tf.value,
+                         "peak_source": "measured FP32 FMA rate (mtg_measure_fp32_tflops)", "unit": "TFLOP/s",
+                         "frac": achieved / tf.value, "traffic": ncu_traffic("k_tea_step", args.workload),
+                         "algorithmic_flop_per_launch": work, "avg_launch_ms": avg},
+            "gpu_launches": L["gpu_launches"],
+            "e2e": L["e2e"] if learned_ok else X["e2e"],
+            "clocks": L["clocks"],
+            "cpu_baseline": cpu,
+        }
+    surr.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -398,7 +553,11 @@ def main():
     dist = Dist()
     try:
         if args.impl == "reference":
-            run_reference(args, spec, dist)
+            run_reference(args, dict(spec, kind="tea") if spec["kind"] == "tea_compare" else spec, dist)
+        elif spec["kind"] == "tea_compare":
+            out = run_tea_compare(args, spec, dist)
+            if out is not None:
+                print(json.dumps(out))
         else:
             out = run_gpu(args, spec, dist)
             if out is not None:
