@@ -316,9 +316,10 @@ int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *devic
 int mtg_set_kernel_timing(mtg_engine *e, int on);
 int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int reset);
 
-/* Measured FP32 FMA throughput of `device` in TFLOP/s (best of 5 runs of a
- * register-resident FMA chain over 8 CTAs per SM): the denominator of the
- * roofline of the FP32-pipe-bound TEA kernels. */
+/* Measured FP32 FMA throughput of `device` in TFLOP/s: the best of
+ * register-resident chains of scalar and of packed FP32x2 FMAs over 8 CTAs
+ * per SM (5 runs each), the denominator of the roofline of the
+ * FP32-pipe-bound TEA kernels. */
 int mtg_measure_fp32_tflops(int device, double *tflops);
 
 /* Page-locked host buffers for fast state transfers (cudaHostAlloc). */

@@ -209,6 +209,36 @@ __device__ __forceinline__ void tea_pair(float dx, float dy, float dz, float gx,
     fz = fmaf(cii, gz, fmaf(s, dz, fz));
 }
 
+// Two pairs at once (beads i0, i1 against one j) in packed FP32x2
+// arithmetic (each lane an IEEE single-precision fma/add/mul, as the scalar
+// path): the same formula as tea_pair.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ void tea_pair2(float2 dx, float2 dy, float2 dz, float2 gx, float2 gy, float2 gz, float a,
+                                          float inv_a, float2 c075a, float2 c05a3, float2 nc15a3, float four_a2,
+                                          float2 &fx, float2 &fy, float2 &fz) {
+    float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+    r2.x = fmaxf(r2.x, 1e-6f);
+    r2.y = fmaxf(r2.y, 1e-6f);
+    const float2 rinv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+    const float2 q = __fmul2_rn(rinv, rinv);
+    float2 cii = __fmul2_rn(rinv, __ffma2_rn(c05a3, q, c075a));
+    float2 crr_r2 = __fmul2_rn(__fmul2_rn(rinv, q), __ffma2_rn(nc15a3, q, c075a));
+    if (r2.x <= four_a2) {
+        const float ra = r2.x * rinv.x * inv_a;
+        cii.x = 1.0f - (9.0f / 32.0f) * ra;
+        crr_r2.x = (3.0f / 32.0f) * ra * q.x;
+    }
+    if (r2.y <= four_a2) {
+        const float ra = r2.y * rinv.y * inv_a;
+        cii.y = 1.0f - (9.0f / 32.0f) * ra;
+        crr_r2.y = (3.0f / 32.0f) * ra * q.y;
+    }
+    const float2 s = __fmul2_rn(crr_r2, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
+    fx = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, fx));
+    fy = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, fy));
+    fz = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, fz));
+}
+
 // integrateTea_kernel_unlisted + integrateTea_force (src/bdhitea_kernel.cu:104-213):
 // f_i = F_i + C_i o R_i + sum_{j != i, non-extra} T_ij (F_j + beta C_i o R_j),
 // x_i += dt/gammaR f_i; angles by Euler-Maruyama from stream i + nb, which is
@@ -277,15 +307,27 @@ __global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevB
             // the CTA's own beads (the self pairs) can only sit in this tile range
             const bool self_tile = (w.y < j0 + n) && (w.y + kTeaI > j0);
             if (!self_tile) {
+                // packed over the two beads: lane x = bead il, lane y = bead il + 32
+                const float2 nx = make_float2(-pi[0].x, -pi[1].x), ny = make_float2(-pi[0].y, -pi[1].y),
+                             nz = make_float2(-pi[0].z, -pi[1].z);
+                const float2 cb2x = make_float2(cbx[0], cbx[1]), cb2y = make_float2(cby[0], cby[1]),
+                             cb2z = make_float2(cbz[0], cbz[1]);
+                float2 ax = make_float2(fx[0], fx[1]), ay = make_float2(fy[0], fy[1]), az = make_float2(fz[0], fz[1]);
+                const float2 v075a = f2(c075a), v05a3 = f2(c05a3), vn15a3 = f2(-c15a3);
 #pragma unroll 4
                 for (int t = sl; t < n; t += SLICES) {
                     const float4 q = s_pos[t], Fj = s_f[t], Rj = s_r[t];
-#pragma unroll
-                    for (int h = 0; h < 2; h++)
-                        tea_pair(q.x - pi[h].x, q.y - pi[h].y, q.z - pi[h].z, fmaf(Rj.x, cbx[h], Fj.x),
-                                 fmaf(Rj.y, cby[h], Fj.y), fmaf(Rj.z, cbz[h], Fj.z), a, inv_a, c075a, c05a3, c15a3,
-                                 four_a2, fx[h], fy[h], fz[h]);
+                    tea_pair2(__fadd2_rn(f2(q.x), nx), __fadd2_rn(f2(q.y), ny), __fadd2_rn(f2(q.z), nz),
+                              __ffma2_rn(f2(Rj.x), cb2x, f2(Fj.x)), __ffma2_rn(f2(Rj.y), cb2y, f2(Fj.y)),
+                              __ffma2_rn(f2(Rj.z), cb2z, f2(Fj.z)), a, inv_a, v075a, v05a3, vn15a3, four_a2, ax, ay,
+                              az);
                 }
+                fx[0] = ax.x;
+                fx[1] = ax.y;
+                fy[0] = ay.x;
+                fy[1] = ay.y;
+                fz[0] = az.x;
+                fz[1] = az.y;
             } else {
                 for (int t = sl; t < n; t += SLICES) {
                     const float4 q = s_pos[t], Fj = s_f[t], Rj = s_r[t];

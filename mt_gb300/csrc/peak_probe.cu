@@ -21,6 +21,22 @@ __global__ void __launch_bounds__(256) k_fma_chain(float *out, int iters, float 
     if (s == 12345.678f) out[0] = s;  // keeps the chains live
 }
 
+// The same with packed FP32x2 FMAs (2 FLOP x 2 lanes per instruction).
+__global__ void __launch_bounds__(256) k_fma2_chain(float *out, int iters, float a, float b) {
+    float2 x0 = make_float2(threadIdx.x * 1e-3f, 1), x1 = make_float2(2, 3), x2 = make_float2(4, 5),
+           x3 = make_float2(6, 7);
+    const float2 va = make_float2(a, a), vb = make_float2(b, b);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            x0 = __ffma2_rn(x0, va, vb); x1 = __ffma2_rn(x1, va, vb);
+            x2 = __ffma2_rn(x2, va, vb); x3 = __ffma2_rn(x3, va, vb);
+        }
+    }
+    const float s = ((x0.x + x0.y) + (x1.x + x1.y)) + ((x2.x + x2.y) + (x3.x + x3.y));
+    if (s == 12345.678f) out[0] = s;
+}
+
 }  // namespace
 
 extern "C" int mtg_measure_fp32_tflops(int device, double *tflops) {
@@ -35,15 +51,19 @@ extern "C" int mtg_measure_fp32_tflops(int device, double *tflops) {
     cudaEventCreate(&b);
     const int blocks = sms * 8, threads = 256, iters = 4096;
     k_fma_chain<<<blocks, threads>>>(out, 64, 0.999f, 1e-3f);  // warm-up
+    k_fma2_chain<<<blocks, threads>>>(out, 64, 0.999f, 1e-3f);
     double best = 0.0;
-    for (int rep = 0; rep < 5; rep++) {
+    for (int rep = 0; rep < 10; rep++) {
         cudaEventRecord(a);
-        k_fma_chain<<<blocks, threads>>>(out, iters, 0.999f, 1e-3f);
+        if (rep & 1)
+            k_fma2_chain<<<blocks, threads>>>(out, iters, 0.999f, 1e-3f);
+        else
+            k_fma_chain<<<blocks, threads>>>(out, iters, 0.999f, 1e-3f);
         cudaEventRecord(b);
         cudaEventSynchronize(b);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, a, b);
-        const double flop = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+        const double flop = 2.0 * 8 * 16 * (double)iters * blocks * threads;  // same FLOP count in both chains
         if (ms > 0) best = flop / (ms * 1e-3) / 1e12 > best ? flop / (ms * 1e-3) / 1e12 : best;
     }
     cudaEventDestroy(a);
