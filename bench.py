@@ -52,6 +52,11 @@ WORKLOADS = {
     "batched_plain_256x1520": dict(kind="plain", ntraj=256, n_mon=40, n_free=1000, cube=100.0),
     # small case for quick checks
     "plain_16x1520": dict(kind="plain", ntraj=16, n_mon=40, n_free=1000, cube=100.0),
+    # uneven batch: 1024 trajectories, protofilament length U{8..120}, free
+    # tubulin U{0..2000} in a 150 nm cube, 30% with a bent plus end
+    # (0.1-0.3 rad per monomer); launch shapes from the autotuner
+    "ragged_1024": dict(kind="plain", ragged=True, ntraj=1024, pf_range=(8, 120), free_range=(0, 2000), cube=150.0,
+                        n_mon=64, n_free=1000),
     # exact TEA hydrodynamics: 16 trajectories of a 13 PF x 100 monomer lattice
     # (1300 beads) + 2000 free monomers; RPY radius 2 nm, epsilon/beta every
     # 10 steps (FP64 reduction on the device)
@@ -185,8 +190,19 @@ def workload_params(spec: dict, seed: int):
 def make_batch(spec: dict, seed: int, ntraj: int | None = None):
     from mt_gb300 import synth
     p = workload_params(spec, seed)
+    if spec.get("ragged"):
+        return synth.ragged_batch(p, ntraj or spec["ntraj"], seed=seed, pf_range=spec["pf_range"],
+                                  free_range=spec["free_range"], cube=spec["cube"])
     return synth.uniform_batch(p, ntraj or spec["ntraj"], spec["n_mon"], spec["n_free"], seed=seed,
                                cube=spec["cube"])
+
+
+TUNE_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "mt_gb300", "autotune.json")
+
+
+def tune_key(b, workload: str) -> str:
+    import torch
+    return f"{torch.cuda.get_device_name()}|{workload}|nb={b.nbeads}|nt={b.ntraj}|tea={b.params.hdi_on}"
 
 
 def tea_pairs(b) -> int:
@@ -293,6 +309,7 @@ def run_gpu(args, spec, dist):
     period = int(b.params.ljpairsupdatefreq)
     active = b.active_beads()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dist.local}")
+    tune = e.autotune(0, period, cache=TUNE_CACHE, key=tune_key(b, args.workload))
 
     step = 0
     for _ in range(args.warmup):
@@ -378,7 +395,8 @@ def run_gpu(args, spec, dist):
             "config": {"workload": args.workload, "trajectories_per_gpu": b.ntraj, "beads_per_gpu": b.nbeads,
                        "active_beads_per_gpu": active, "md_steps_per_bench_step": period,
                        "l2": "flushed (256 MB write) before every timed step",
-                       "parallelism": f"replicas x{dist.ws} (independent trajectories)"},
+                       "parallelism": f"replicas x{dist.ws} (independent trajectories)",
+                       "tuning": tune},
             "roofline": roof,
             "kernel_ms": {k: (kt_ms[k] / launches[k] if launches[k] else None) for k in kt_ms},
             "kernel_share": {k: kt_ms[k] / max(1e-12, sum(kt_ms.values())) for k in kt_ms},

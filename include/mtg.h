@@ -298,6 +298,25 @@ int mtg_set_surrogate(mtg_engine *e, mtg_surrogate *s, int recheck_every, float 
  * last re-check's RMS relative difference. */
 int mtg_surrogate_status(mtg_engine *e, int *fell_back, int *rechecks, double *last_error);
 
+/* ---- tuning ------------------------------------------------------------ */
+/* Launch shapes of the engine's kernels.  list_method as
+ * mtg_set_list_method (1 tiles, 2 cells); step_block: threads per CTA of the
+ * fused plain step (64, 128, 256); tea_slices: threads per bead in the
+ * all-pairs TEA kernels (1, 2, 4, 8).  No reference counterpart (the
+ * reference launches everything with 32-thread blocks, src/mt.h:34). */
+typedef struct {
+    int list_method;
+    int step_block;
+    int tea_slices;
+} mtg_tuning;
+int mtg_get_tuning(mtg_engine *e, mtg_tuning *t);
+int mtg_set_tuning(mtg_engine *e, const mtg_tuning *t);
+/* Times every candidate tuning over trial_steps steps from first_step
+ * (CUDA events; each trial restarts from a snapshot of the state and noise
+ * streams, which are restored afterwards, so the simulation is unchanged)
+ * and keeps the fastest.  best / best_ms may be NULL. */
+int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tuning *best, float *best_ms);
+
 /* ---- measurement ------------------------------------------------------- */
 /* mtg_step bracketed by CUDA events recorded on the engine's stream;
  * *device_ms = the device time between them.  No reference counterpart (the

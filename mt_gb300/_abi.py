@@ -99,3 +99,9 @@ def ptr(a, ctype):
         return C.cast(None, C.POINTER(ctype))
     assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
     return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class MtgTuning(C.Structure):
+    """mtg_tuning: launch shapes chosen by the autotuner."""
+
+    _fields_ = [("list_method", _i), ("step_block", _i), ("tea_slices", _i)]

@@ -412,10 +412,11 @@ void launch_forces_to_coords(const KParams &P, const float4 *force, float *c7, c
     k_forces_to_coords<<<blocks(P.nb, 256), 256, 0, s>>>(P.nb, force, c7);
 }
 void launch_step_plain(const KParams &P, const DevBuffers &B, bool keep_forces, cudaStream_t s) {
+    const int t = P.step_block > 0 ? P.step_block : 128;
     if (keep_forces)
-        k_step_plain<true><<<blocks(P.nb, 128), 128, 0, s>>>(P, B);
+        k_step_plain<true><<<blocks(P.nb, t), t, 0, s>>>(P, B);
     else
-        k_step_plain<false><<<blocks(P.nb, 128), 128, 0, s>>>(P, B);
+        k_step_plain<false><<<blocks(P.nb, t), t, 0, s>>>(P, B);
 }
 void launch_forces(const KParams &P, const DevBuffers &B, bool tea_prepare, cudaStream_t s) {
     if (tea_prepare)

@@ -156,6 +156,7 @@ KParams make_kparams(const mtg_params &p, int nb, int nt, int maxH, int maxLong,
     k.maxLong = maxLong;
     k.maxLat = maxLat;
     k.maxLJ = maxLJ;
+    k.step_block = 128;
     k.tea_a = p.tea_a;
     k.tea_var = sqrtf(2.0f * 0.0019872041f * p.Temp * p.gammaR / p.dt);
     return k;
@@ -900,6 +901,87 @@ int mtg_get_list_method(mtg_engine *e, int *method) {
     if (!e || !method) return fail(MTG_E_CONFIG, "engine or method is NULL");
     *method = e->use_cells ? 2 : 1;
     return MTG_OK;
+}
+
+int mtg_get_tuning(mtg_engine *e, mtg_tuning *t) {
+    if (!e || !t) return fail(MTG_E_CONFIG, "engine or tuning is NULL");
+    t->list_method = e->use_cells ? 2 : 1;
+    t->step_block = e->kp.step_block;
+    t->tea_slices = e->kp.tea_slices;
+    return MTG_OK;
+}
+
+int mtg_set_tuning(mtg_engine *e, const mtg_tuning *t) {
+    if (!e || !t) return fail(MTG_E_CONFIG, "engine or tuning is NULL");
+    if (t->step_block != 64 && t->step_block != 128 && t->step_block != 256)
+        return fail(MTG_E_CONFIG, "step_block must be 64, 128 or 256");
+    if (t->tea_slices != 1 && t->tea_slices != 2 && t->tea_slices != 4 && t->tea_slices != 8)
+        return fail(MTG_E_CONFIG, "tea_slices must be 1, 2, 4 or 8");
+    int rc = mtg_set_list_method(e, t->list_method);
+    if (rc) return rc;
+    e->kp.step_block = t->step_block;
+    e->kp.tea_slices = t->tea_slices;
+    destroy_graphs(e);
+    return MTG_OK;
+}
+
+int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tuning *best, float *best_ms) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (!e->have_state) return fail(MTG_E_STATE, "no state uploaded");
+    if (trial_steps <= 0) return fail(MTG_E_CONFIG, "trial_steps must be positive");
+    cudaSetDevice(e->device);
+    // snapshot of everything a trial advances: the state and the noise streams
+    const size_t fbytes = sizeof(float4) * 4 * (size_t)e->nb, sbytes = sizeof(uint4) * 2 * (size_t)e->nb;
+    void *snap = nullptr;
+    CK(cudaMalloc(&snap, fbytes + sbytes));
+    CK(cudaMemcpyAsync(snap, e->frame[e->cur], fbytes, cudaMemcpyDeviceToDevice, e->stream));
+    CK(cudaMemcpyAsync((char *)snap + fbytes, e->seeds, sbytes, cudaMemcpyDeviceToDevice, e->stream));
+    const int cur0 = e->cur;
+    mtg_tuning orig;
+    mtg_get_tuning(e, &orig);
+    std::vector<mtg_tuning> cands;
+    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat;
+    const bool lists = e->p.lj_on || e->p.is_assembly;
+    for (int lm : {1, 2}) {
+        if (lm == 2 && (!cells_ok || !lists)) continue;
+        if (lm == 1 && !lists && !cands.empty()) continue;
+        if (e->p.hdi_on) {
+            for (int sl : {1, 2, 4, 8}) cands.push_back({lm, orig.step_block, sl});
+        } else {
+            for (int bs : {64, 128, 256}) cands.push_back({lm, bs, orig.tea_slices});
+        }
+    }
+    float best_t = 3.4e38f;
+    mtg_tuning bt = orig;
+    int rc = MTG_OK;
+    for (const auto &c : cands) {
+        if ((rc = mtg_set_tuning(e, &c)) != 0) break;
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && rc == MTG_OK; rep++) {  // first run captures the graph
+            e->cur = cur0;
+            cudaMemcpyAsync(e->frame[e->cur], snap, fbytes, cudaMemcpyDeviceToDevice, e->stream);
+            cudaMemcpyAsync(e->seeds, (char *)snap + fbytes, sbytes, cudaMemcpyDeviceToDevice, e->stream);
+            rc = mtg_step_timed(e, first_step, trial_steps, &ms);
+        }
+        if (rc) break;
+        if (ms < best_t) {
+            best_t = ms;
+            bt = c;
+        }
+    }
+    e->cur = cur0;
+    cudaMemcpyAsync(e->frame[e->cur], snap, fbytes, cudaMemcpyDeviceToDevice, e->stream);
+    cudaMemcpyAsync(e->seeds, (char *)snap + fbytes, sbytes, cudaMemcpyDeviceToDevice, e->stream);
+    cudaStreamSynchronize(e->stream);
+    cudaFree(snap);
+    if (rc) {
+        mtg_set_tuning(e, &orig);
+        return rc;
+    }
+    rc = mtg_set_tuning(e, &bt);
+    if (best) *best = bt;
+    if (best_ms) *best_ms = best_t;
+    return rc;
 }
 
 int mtg_set_kernel_timing(mtg_engine *e, int on) {

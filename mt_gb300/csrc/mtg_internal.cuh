@@ -60,6 +60,7 @@ struct KParams {
     // TEA
     float tea_a, tea_var;
     int tea_slices;        // threads per bead i in the all-pairs TEA kernels (1, 2, 4 or 8)
+    int step_block;        // threads per CTA of the fused plain step (64, 128 or 256)
 };
 
 // Device buffers of one engine.

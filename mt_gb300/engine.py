@@ -12,7 +12,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import MtgBatchTopology, MtgParams, MtgTopology, ptr
+from ._abi import MtgBatchTopology, MtgParams, MtgTopology, MtgTuning, ptr
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmtg.so")
 
@@ -50,6 +50,9 @@ EXPORTS = {
     "mtg_measure_fp32_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "mtg_set_list_method": (C.c_int, [C.c_void_p, C.c_int]),
     "mtg_get_list_method": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "mtg_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(MtgTuning)]),
+    "mtg_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(MtgTuning)]),
+    "mtg_autotune": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(MtgTuning), C.POINTER(C.c_float)]),
     "mtg_surrogate_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "mtg_surrogate_destroy": (C.c_int, [C.c_void_p]),
     "mtg_surrogate_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
@@ -290,6 +293,42 @@ class Engine:
         n = (C.c_longlong * len(KERNEL_KINDS))()
         check(self.lib.mtg_kernel_times(self.h, t, n, int(reset)))
         return {k: (t[i], n[i]) for i, k in enumerate(KERNEL_KINDS)}
+
+    def tuning(self) -> dict:
+        t = MtgTuning()
+        check(self.lib.mtg_get_tuning(self.h, C.byref(t)))
+        return {"list_method": t.list_method, "step_block": t.step_block, "tea_slices": t.tea_slices}
+
+    def set_tuning(self, list_method: int, step_block: int, tea_slices: int):
+        t = MtgTuning(list_method, step_block, tea_slices)
+        check(self.lib.mtg_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, first_step: int, trial_steps: int, cache: str | None = None, key: str | None = None):
+        """Runs mtg_autotune, or applies a cached result for `key` (the GPU name
+        and the workload signature) from the JSON file `cache`."""
+        import json
+        if cache and key and os.path.exists(cache):
+            try:
+                entry = json.load(open(cache)).get(key)
+            except (OSError, ValueError):
+                entry = None
+            if entry:
+                self.set_tuning(**entry["tuning"])
+                return dict(entry, cached=True)
+        t = MtgTuning()
+        ms = C.c_float()
+        check(self.lib.mtg_autotune(self.h, C.c_longlong(first_step), trial_steps, C.byref(t), C.byref(ms)))
+        entry = {"tuning": {"list_method": t.list_method, "step_block": t.step_block, "tea_slices": t.tea_slices},
+                 "trial_ms": ms.value, "cached": False}
+        if cache and key:
+            try:
+                data = json.load(open(cache)) if os.path.exists(cache) else {}
+            except (OSError, ValueError):
+                data = {}
+            data[key] = {k: v for k, v in entry.items() if k != "cached"}
+            os.makedirs(os.path.dirname(os.path.abspath(cache)), exist_ok=True)
+            json.dump(data, open(cache, "w"), indent=1)
+        return entry
 
     def tea_training_data(self, targets: bool = True):
         """(descriptors [nb, 32], targets [nb, 4] = C_i, beta) of the current state."""

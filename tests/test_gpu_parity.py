@@ -238,3 +238,17 @@ def test_cell_lists_equal_tile_lists_on_a_large_batch(engine_mod):
         cnt, arr, cap = cells[k]
         for i in range(e.nb):
             assert np.array_equal(arr[cap * i:cap * i + cnt[i]], tiles[k][1][cap * i:cap * i + cnt[i]]), (k, i)
+
+
+def test_autotune_leaves_the_simulation_unchanged(engine_mod):
+    """The autotuner restores the state and noise streams after its trials,
+    and the plain-path kernels give identical results for every launch shape."""
+    b = small_system(seed=19, ntr=3)
+    e1 = make_engine(engine_mod, b)
+    res = e1.autotune(0, 10)
+    assert res["tuning"]["step_block"] in (64, 128, 256)
+    e1.step(0, 20)
+    e2 = make_engine(engine_mod, b)
+    e2.step(0, 20)
+    assert np.array_equal(e1.download_state(), e2.download_state())
+    assert np.array_equal(e1.download_rng(), e2.download_rng())
