@@ -217,7 +217,8 @@ void launch_lists(mtg_engine *e) {
 }
 
 void choose_list_method(mtg_engine *e) {
-    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat && e->cell_tbase;
+    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat && e->kp.maxLJ <= 256 &&
+                          e->cell_tbase;
     if (e->list_method == 1 || !cells_ok)
         e->use_cells = false;
     else if (e->list_method == 2)
@@ -892,7 +893,8 @@ int mtg_set_list_method(mtg_engine *e, int method) {
     e->list_method = method;
     choose_list_method(e);
     if (method == 2 && !e->use_cells)
-        return fail(MTG_E_CONFIG, "the cell-list rebuild supports list capacities up to %d/%d", kCellMaxLong, kCellMaxLat);
+        return fail(MTG_E_CONFIG, "the cell-list rebuild supports list capacities up to %d/%d/256", kCellMaxLong,
+                    kCellMaxLat);
     destroy_graphs(e);
     return MTG_OK;
 }
@@ -940,7 +942,7 @@ int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tunin
     mtg_tuning orig;
     mtg_get_tuning(e, &orig);
     std::vector<mtg_tuning> cands;
-    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat;
+    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat && e->kp.maxLJ <= 256;
     const bool lists = e->p.lj_on || e->p.is_assembly;
     for (int lm : {1, 2}) {
         if (lm == 2 && (!cells_ok || !lists)) continue;
