@@ -197,8 +197,7 @@ int mtg_list_capacity(const mtg_engine *e, int *max_long, int *max_lat, int *max
 /* How the lists are rebuilt; both produce identical lists.  0 = automatic
  * (cell list when a trajectory has >= 512 beads), 1 = brute-force shared-memory
  * tiles over each trajectory (the reference's O(N^2) loops), 2 = per-trajectory
- * spatial-hash cell list (list capacities up to 16 longitudinal / 32 lateral /
- * 256 LJ). */
+ * spatial-hash cell list (list capacities up to 16 longitudinal / 32 lateral). */
 int mtg_set_list_method(mtg_engine *e, int method);
 int mtg_get_list_method(mtg_engine *e, int *method);
 

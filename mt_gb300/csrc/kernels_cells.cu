@@ -8,10 +8,11 @@
 //   1. k_cell_count : bucket of every bead, bucket populations
 //   2. k_cell_scan  : one CTA per trajectory, exclusive scan of its table
 //   3. k_cell_fill  : beads scattered into bucket order
-//   4. k_cell_lists : a warp per bead: candidates from the 27 cells' buckets
-//      (each bucket visited once), the reference's list tests, hits ordered
-//      by rank so each list is in ascending j (orientation 0 before 1 for the
-//      lateral list), exactly the order of the reference's j loops
+//   4. k_cell_lists : per bead, candidates from the 27 cells' buckets (each
+//      bucket visited once) read from a bucket-ordered copy of the
+//      positions, the reference's list tests, then an insertion sort so each
+//      list is in ascending j (orientation 0 before 1 for the lateral list),
+//      exactly the order of the reference's j loops
 //      (src/compute_cuda.cu:564-661, :927-936).
 #include "mtg_internal.cuh"
 
@@ -72,159 +73,167 @@ __global__ void __launch_bounds__(1024) k_cell_scan(const int *tbase, const int 
 
 // Bucket-ordered bead lists; positions are relative to the trajectory's
 // first bead, so slots of trajectory t start at off[t].
-__global__ void k_cell_fill(int nb, const int *traj, const int *off, const int *key, int *cursor, int *cell_bead) {
+__global__ void k_cell_fill(int nb, const int *traj, const int *off, const int *key, int *cursor, int *cell_bead,
+                            const float4 *pos, float4 *cell_pos) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nb) return;
-    const int slot = atomicAdd(&cursor[key[g]], 1);
-    cell_bead[off[traj[g]] + slot] = g;
+    const int slot = off[traj[g]] + atomicAdd(&cursor[key[g]], 1);
+    cell_bead[slot] = g;
+    float4 p = pos[g];
+    p.w = __int_as_float(g);   // bucket-ordered copy of the positions, bead index in w
+    cell_pos[slot] = p;
 }
 
-// Warp per bead: the 27 neighbour cells' buckets are deduplicated across
-// lanes, their candidates tested 32 at a time, the hits compacted in order
-// of discovery into per-warp shared buffers, then written out at their rank
-// (the number of smaller keys), i.e. in ascending j.
-constexpr int kListWarps = 8;
-constexpr int kWarpLJ = 256;   // per-warp LJ hit buffer; larger capacities use the tiled rebuild
-
-__device__ __forceinline__ void warp_append(int *buf, int &n, int cap, bool hit, int key, bool &overflow) {
-    const unsigned m = __ballot_sync(0xffffffffu, hit);
-    if (m) {
-        const int lane = threadIdx.x & 31;
-        const int pos = n + __popc(m & ((1u << lane) - 1u));
-        if (hit) {
-            if (pos < cap)
-                buf[pos] = key;
-            else
-                overflow = true;
+__device__ __forceinline__ void isort(int *a, int n) {
+    for (int i = 1; i < n; i++) {
+        const int v = a[i];
+        int j = i - 1;
+        while (j >= 0 && a[j] > v) {
+            a[j + 1] = a[j];
+            j--;
         }
-        n += __popc(m);
+        a[j + 1] = v;
     }
 }
 
-// writes buf[0..n) (distinct keys) to out[rank * stride] in ascending order
-__device__ __forceinline__ void warp_rank_store(const int *buf, int n, int *out, int stride, int mode, int h0) {
-    const int lane = threadIdx.x & 31;
-    for (int k = lane; k < n; k += 32) {
-        const int v = buf[k];
-        int rank = 0;
-        for (int m = 0; m < n; m++) rank += buf[m] < v;
-        int val = v;
-        if (mode == 1) {                      // longitudinal: sign from the harmonic partner side
-            val = h0 < 0 ? v : -v;
-        } else if (mode == 2) {               // lateral: key 2j + orientation
-            const int j = v >> 1;
-            const int code = j != 0 ? j : kZeroCode;
-            val = (v & 1) ? code : -code;
+// In-place insertion sort of a k-major list (rare path: > kLocalLJ entries).
+__device__ void isort_strided(int *a, int n, int stride) {
+    for (int i = 1; i < n; i++) {
+        const int v = a[(size_t)i * stride];
+        int j = i - 1;
+        while (j >= 0 && a[(size_t)j * stride] > v) {
+            a[(size_t)(j + 1) * stride] = a[(size_t)j * stride];
+            j--;
         }
-        out[(size_t)rank * stride] = val;
+        a[(size_t)(j + 1) * stride] = v;
     }
 }
 
-__global__ void __launch_bounds__(kListWarps * 32) k_cell_lists(KParams P, DevBuffers B, const int2 *work,
-                                                                const int *tbase, const int *tmask, const int *start,
-                                                                const int *cnt, const int *cell_bead, float inv_cell) {
-    __shared__ int s_lj[kListWarps][kWarpLJ];
-    __shared__ int s_lo[kListWarps][kCellMaxLong];
-    __shared__ int s_la[kListWarps][kCellMaxLat];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+constexpr int kLocalLJ = 64;   // LJ hits sorted in local memory; more are sorted in place
+
+// Thread per bead: candidates are read from the bucket-ordered position copy
+// (one contiguous 16 B load each); the rare assembly candidates (< 6.6 nm)
+// also read the neighbour's site planes.
+__global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B, const int2 *work, const int *tbase,
+                                                         const int *tmask, const int *start, const int *cnt,
+                                                         const float4 *cell_pos, float inv_cell) {
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
+    const int g = w.y + threadIdx.x;
+    if (g >= end) return;
     const int nb = P.nb;
     const float4 *fr = B.frame_in;
+    const int flags = B.flags[g];
+    const bool extra_i = (flags & kFlagExtra) != 0;
+    const bool do_lj = P.lj_on && !extra_i;
+    const bool do_pairs = P.is_assembly && !extra_i;
+    if (!do_lj && !do_pairs) {
+        if (P.lj_on) B.ljc[g] = 0;
+        if (P.is_assembly) {
+            B.lonc[g] = 0;
+            B.latc[g] = 0;
+        }
+        return;
+    }
+    const float4 pi = fr[g];
+    const int il = g - base;
+    const int h0 = B.harm[g * P.maxH];
+    const int hpart = h0 < 0 ? -h0 : h0;
+    const int cx = cell_coord(pi.x, inv_cell), cy = cell_coord(pi.y, inv_cell), cz = cell_coord(pi.z, inv_cell);
     const int tb = tbase[traj];
     const uint32_t mask = (uint32_t)tmask[traj];
-    const int capLJ = min(P.maxLJ, kWarpLJ);
-    // the CTA's kTile beads, kTile / kListWarps per warp
-    for (int g = w.y + wid; g < min(w.y + kTile, end); g += kListWarps) {
-        const int flags = B.flags[g];
-        const bool extra_i = (flags & kFlagExtra) != 0;
-        const bool do_lj = P.lj_on && !extra_i;
-        const bool do_pairs = P.is_assembly && !extra_i;
-        if (!do_lj && !do_pairs) {
-            if (lane == 0) {
-                if (P.lj_on) B.ljc[g] = 0;
-                if (P.is_assembly) {
-                    B.lonc[g] = 0;
-                    B.latc[g] = 0;
+
+    int lj_buf[kLocalLJ];
+    int lo_buf[kCellMaxLong], la_buf[kCellMaxLat];
+    int nlj = 0, nlo = 0, nla = 0;
+    bool overflow = false;
+    int visited[27];
+    int nvis = 0;
+    for (int c = 0; c < 27; c++) {
+        const int bkt = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
+        bool seen = false;
+        for (int v = 0; v < nvis; v++) seen |= (visited[v] == bkt);
+        if (seen) continue;
+        visited[nvis++] = bkt;
+        const int s0 = base + start[bkt], s1 = s0 + cnt[bkt];
+        for (int s = s0; s < s1; s++) {
+            const float4 q = cell_pos[s];
+            const int jg = __float_as_int(q.w);
+            const int jl = jg - base;
+            const float cd = centre_dist(pi, q);
+            if (do_lj && jl != il && cd < P.ljcut) {
+                if (nlj >= P.maxLJ) {
+                    overflow = true;
+                } else if (nlj < kLocalLJ) {
+                    lj_buf[nlj] = jl;
+                } else {
+                    if (nlj == kLocalLJ)  // spill the local part first
+                        for (int k = 0; k < kLocalLJ; k++) B.lj[k * nb + g] = lj_buf[k];
+                    B.lj[nlj * nb + g] = jl;
                 }
+                nlj++;
             }
-            continue;
-        }
-        const float4 pi = fr[g], ui = fr[nb + g], li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
-        const int il = g - base;
-        const int h0 = B.harm[g * P.maxH];
-        const float rmon = h0 < 0 ? -2.0f : 2.0f;
-        const int hpart = h0 < 0 ? -h0 : h0;
-        const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
-        const int cx = cell_coord(pi.x, inv_cell), cy = cell_coord(pi.y, inv_cell), cz = cell_coord(pi.z, inv_cell);
-        // lanes 0..26 own one neighbour cell each; duplicate buckets are dropped
-        int bkt = -1;
-        if (lane < 27) bkt = tb + (int)(cell_hash(cx + lane % 3 - 1, cy + (lane / 3) % 3 - 1, cz + lane / 9 - 1) & mask);
-        bool dup = false;
-        for (int k = 0; k < 27; k++) {
-            const int other = __shfl_sync(0xffffffffu, bkt, k);
-            dup |= (k < lane) && (other == bkt);
-        }
-        unsigned todo = __ballot_sync(0xffffffffu, lane < 27 && !dup);
-        int nlj = 0, nlo = 0, nla = 0;
-        bool overflow = false;
-        while (todo) {
-            const int src = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const int b = __shfl_sync(0xffffffffu, bkt, src);
-            const int s0 = base + start[b], s1 = s0 + cnt[b];
-            for (int s = s0; s < s1; s += 32) {
-                const int sidx = s + lane;
-                const bool have = sidx < s1;
-                int jl = -1;
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                float cd = 3.0e38f;
-                int jg = 0;
-                if (have) {
-                    jg = cell_bead[sidx];
-                    jl = jg - base;
-                    q = fr[jg];
-                    cd = centre_dist(pi, q);
-                }
-                warp_append(s_lj[wid], nlj, capLJ, do_lj && have && jl != il && cd < P.ljcut, jl, overflow);
-                bool lo_hit = false, la0 = false, la1 = false;
-                if (do_pairs && have && cd < kPairReach && jl != hpart) {
-                    const int fj = B.flags[jg];
-                    if (((flags ^ fj) & kFlagBeta) != 0) {
-                        const float4 uj = fr[nb + jg];
-                        lo_hit = norm3_rn(site_delta(pi, q, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) <
-                                 2.5f;
-                    }
-                    if (jl != il) {
-                        const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
-                        la0 = norm3_rn(site_delta(pi, q, f3(li1), f3(l2))) < 2.5f;
-                        la1 = norm3_rn(site_delta(pi, q, f3(li2), f3(l1))) < 2.5f;
+            if (do_pairs && cd < kPairReach && jl != hpart) {
+                const float4 pj = fr[jg];   // the exact state (q carries the index in w)
+                const float rmon = h0 < 0 ? -2.0f : 2.0f;
+                const int fj = B.flags[jg];
+                if (((flags ^ fj) & kFlagBeta) != 0) {
+                    const float4 ui = fr[nb + g], uj = fr[nb + jg];
+                    const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
+                    if (norm3_rn(site_delta(pi, pj, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) <
+                        2.5f) {
+                        if (nlo < P.maxLong)
+                            lo_buf[nlo] = jl;
+                        else
+                            overflow = true;
+                        nlo++;
                     }
                 }
-                warp_append(s_lo[wid], nlo, P.maxLong, lo_hit, jl, overflow);
-                warp_append(s_la[wid], nla, P.maxLat, la0, 2 * jl, overflow);
-                warp_append(s_la[wid], nla, P.maxLat, la1, 2 * jl + 1, overflow);
+                if (jl != il) {
+                    const float4 li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
+                    const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
+                    if (norm3_rn(site_delta(pi, pj, f3(li1), f3(l2))) < 2.5f) {
+                        if (nla < P.maxLat)
+                            la_buf[nla] = 2 * jl;       // orientation 0 -> -j
+                        else
+                            overflow = true;
+                        nla++;
+                    }
+                    if (norm3_rn(site_delta(pi, pj, f3(li2), f3(l1))) < 2.5f) {
+                        if (nla < P.maxLat)
+                            la_buf[nla] = 2 * jl + 1;   // orientation 1 -> +j
+                        else
+                            overflow = true;
+                        nla++;
+                    }
+                }
             }
         }
-        __syncwarp();
-        if (P.lj_on) {
-            const int n = min(nlj, capLJ);
-            warp_rank_store(s_lj[wid], n, B.lj + g, nb, 0, h0);
-            if (lane == 0) B.ljc[g] = n;
-            if (nlj > capLJ) overflow = true;
-        }
-        if (P.is_assembly) {
-            const int n1 = min(nlo, P.maxLong), n2 = min(nla, P.maxLat);
-            warp_rank_store(s_lo[wid], n1, B.lon + g, nb, 1, h0);
-            warp_rank_store(s_la[wid], n2, B.lat + g, nb, 2, h0);
-            if (lane == 0) {
-                B.lonc[g] = n1;
-                B.latc[g] = n2;
-            }
-        }
-        if (__any_sync(0xffffffffu, overflow) && lane == 0) atomicOr(B.err, kErrOverflow);
-        __syncwarp();
     }
+    if (P.lj_on) {
+        const int n = min(nlj, P.maxLJ);
+        if (n <= kLocalLJ) {
+            isort(lj_buf, n);
+            for (int k = 0; k < n; k++) B.lj[k * nb + g] = lj_buf[k];
+        } else {
+            isort_strided(B.lj + g, n, nb);
+        }
+        B.ljc[g] = n;
+    }
+    if (P.is_assembly) {
+        const int n1 = min(nlo, P.maxLong), n2 = min(nla, P.maxLat);
+        isort(lo_buf, n1);
+        isort(la_buf, n2);
+        for (int k = 0; k < n1; k++) B.lon[k * nb + g] = h0 < 0 ? lo_buf[k] : -lo_buf[k];
+        for (int k = 0; k < n2; k++) {
+            const int j = la_buf[k] >> 1;
+            const int code = j != 0 ? j : kZeroCode;
+            B.lat[k * nb + g] = (la_buf[k] & 1) ? code : -code;
+        }
+        B.lonc[g] = n1;
+        B.latc[g] = n2;
+    }
+    if (overflow) atomicOr(B.err, kErrOverflow);
 }
 
 inline int nblk(int n, int t) { return (n + t - 1) / t; }
@@ -238,7 +247,8 @@ float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, flo
     cudaMemsetAsync(C.cnt, 0, sizeof(int) * C.nbuckets, s);
     k_cell_count<<<nblk(P.nb, 256), 256, 0, s>>>(P, B.frame_in, B.traj, C.tbase, C.tmask, inv, C.key, C.cnt);
     k_cell_scan<<<P.nt, 1024, 0, s>>>(C.tbase, C.cnt, C.start, C.cursor);
-    k_cell_fill<<<nblk(P.nb, 256), 256, 0, s>>>(P.nb, B.traj, B.off, C.key, C.cursor, C.cell_bead);
+    k_cell_fill<<<nblk(P.nb, 256), 256, 0, s>>>(P.nb, B.traj, B.off, C.key, C.cursor, C.cell_bead, B.frame_in,
+                                                 C.cell_pos);
     return inv;
 }
 
@@ -246,7 +256,7 @@ void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffe
                           cudaStream_t s) {
     const float reach = fmaxf(P.lj_on ? P.ljcut : 0.f, P.is_assembly ? kPairReach : 0.f);
     const float inv = bin_beads(P, B, C, reach, s);
-    k_cell_lists<<<nwork, kListWarps * 32, 0, s>>>(P, B, work, C.tbase, C.tmask, C.start, C.cnt, C.cell_bead, inv);
+    k_cell_lists<<<nwork, kTile, 0, s>>>(P, B, work, C.tbase, C.tmask, C.start, C.cnt, C.cell_pos, inv);
 }
 
 }  // namespace mtg

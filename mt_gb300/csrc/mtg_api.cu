@@ -217,8 +217,7 @@ void launch_lists(mtg_engine *e) {
 }
 
 void choose_list_method(mtg_engine *e) {
-    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat && e->kp.maxLJ <= 256 &&
-                          e->cell_tbase;
+    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat && e->cell_tbase;
     if (e->list_method == 1 || !cells_ok)
         e->use_cells = false;
     else if (e->list_method == 2)
@@ -481,6 +480,7 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
     ALLOC(e->cell_tmask, nt);
     ALLOC(e->cell_key, nb);
     ALLOC(e->cell_bead, nb);
+    ALLOC(e->cell_pos, nb);
     ALLOC(e->cell_cnt, e->cell_nbuckets);
     ALLOC(e->cell_start, e->cell_nbuckets);
     ALLOC(e->cell_cursor, e->cell_nbuckets);
@@ -618,7 +618,7 @@ int mtg_destroy(mtg_engine *e) {
                     e->ljc, e->lj, e->lonc, e->lon, e->latc, e->lat, e->err, e->work, e->work_first,
                     e->en_partials, e->en_traj, e->en_bead, e->tea_r, e->tea_ci, e->tea_eps, e->tea_beta,
                     e->tea_eps_t, e->stage, e->stage_u8, e->stage_i, e->cell_tbase, e->cell_tmask,
-                    e->cell_key, e->cell_bead, e->cell_cnt, e->cell_start, e->cell_cursor, e->tea_work,
+                    e->cell_key, e->cell_bead, e->cell_pos, e->cell_cnt, e->cell_start, e->cell_cursor, e->tea_work,
                     e->surr_desc, e->surr_pred, e->surr_stats, e->surr_gate, e->surr_err, e->surr_part,
                     e->tea_ci2, e->feff_a, e->feff_b, e->tea_eps2, e->tea_beta2, e->tea_eps_t2};
     for (void *q : ptrs)
@@ -893,7 +893,7 @@ int mtg_set_list_method(mtg_engine *e, int method) {
     e->list_method = method;
     choose_list_method(e);
     if (method == 2 && !e->use_cells)
-        return fail(MTG_E_CONFIG, "the cell-list rebuild supports list capacities up to %d/%d/256", kCellMaxLong,
+        return fail(MTG_E_CONFIG, "the cell-list rebuild supports list capacities up to %d/%d", kCellMaxLong,
                     kCellMaxLat);
     destroy_graphs(e);
     return MTG_OK;
@@ -942,7 +942,7 @@ int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tunin
     mtg_tuning orig;
     mtg_get_tuning(e, &orig);
     std::vector<mtg_tuning> cands;
-    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat && e->kp.maxLJ <= 256;
+    const bool cells_ok = e->kp.maxLong <= kCellMaxLong && e->kp.maxLat <= kCellMaxLat;
     const bool lists = e->p.lj_on || e->p.is_assembly;
     for (int lm : {1, 2}) {
         if (lm == 2 && (!cells_ok || !lists)) continue;

@@ -62,6 +62,7 @@ struct mtg_engine {
     int max_traj_beads = 0;
     int *cell_tbase = nullptr, *cell_tmask = nullptr, *cell_key = nullptr, *cell_cnt = nullptr;
     int *cell_start = nullptr, *cell_cursor = nullptr, *cell_bead = nullptr;
+    float4 *cell_pos = nullptr;
     int cell_nbuckets = 0;
     // learned TEA (surrogate.cu)
     struct mtg_surrogate *surr = nullptr;
@@ -85,6 +86,7 @@ struct mtg_engine {
         c.start = cell_start;
         c.cursor = cell_cursor;
         c.cell_bead = cell_bead;
+        c.cell_pos = cell_pos;
         return c;
     }
 

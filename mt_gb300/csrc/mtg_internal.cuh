@@ -198,6 +198,7 @@ struct CellBuffers {
     int *key;              // [nb] bucket of each bead
     int *cnt, *start, *cursor;  // [nbuckets]
     int *cell_bead;        // [nb] beads in bucket order
+    float4 *cell_pos;      // [nb] their positions, bead index in w
 };
 constexpr int kCellMaxLong = 16;   // largest list capacities the cell rebuild buffers locally
 constexpr int kCellMaxLat = 32;

@@ -99,12 +99,12 @@ __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, 
                     visited[nvis++] = bkt;
                     const int s0 = base + C.start[bkt], s1 = s0 + C.cnt[bkt];
                     for (int s = s0; s < s1; s++) {
-                        const int jg = C.cell_bead[s];
-                        if (jg == g || (B.flags[jg] & kFlagExtra)) continue;
-                        const float4 q = B.frame_in[jg];
+                        const float4 q = C.cell_pos[s];
+                        const int jg = __float_as_int(q.w);
                         const float ex = q.x - pi.x, ey = q.y - pi.y, ez = q.z - pi.z;
                         const float r2 = ex * ex + ey * ey + ez * ez;
-                        if (!(r2 < kDescCut * kDescCut) || r2 <= 0.f) continue;
+                        if (!(r2 < kDescCut * kDescCut) || r2 <= 0.f || jg == g) continue;
+                        if (B.flags[jg] & kFlagExtra) continue;
                         const float rinv = rsqrtf(r2), r = r2 * rinv;
                         const int sh = r < 5.0f ? 0 : (r < 10.0f ? 10 : 20);
                         const float ux = ex * rinv, uy = ey * rinv, uz = ez * rinv;
