@@ -147,15 +147,22 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
     int lo_buf[kCellMaxLong], la_buf[kCellMaxLat];
     int nlj = 0, nlo = 0, nla = 0;
     bool overflow = false;
-    int visited[27];
-    int nvis = 0;
+    // the 27 buckets and their ranges, all lookups issued before any is used
+    int bk[27], st[27], ct[27];
+#pragma unroll
+    for (int c = 0; c < 27; c++) bk[c] = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
+#pragma unroll
     for (int c = 0; c < 27; c++) {
-        const int bkt = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
-        bool seen = false;
-        for (int v = 0; v < nvis; v++) seen |= (visited[v] == bkt);
+        st[c] = start[bk[c]];
+        ct[c] = cnt[bk[c]];
+    }
+    for (int c = 0; c < 27; c++) {
+        if (ct[c] == 0) continue;
+        const int bkt = bk[c];
+        bool seen = false;   // two cells hashed to one bucket: visit it once
+        for (int v = 0; v < c; v++) seen |= (bk[v] == bkt);
         if (seen) continue;
-        visited[nvis++] = bkt;
-        const int s0 = base + start[bkt], s1 = s0 + cnt[bkt];
+        const int s0 = base + st[c], s1 = s0 + ct[c];
         for (int s = s0; s < s1; s++) {
             const float4 q = cell_pos[s];
             const int jg = __float_as_int(q.w);

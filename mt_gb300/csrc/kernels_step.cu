@@ -119,17 +119,28 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
     }
     // LJ r^-6 repulsion with the hard 6 nm force cutoff (:470-495)
     if (P.lj_on) {
+        // four neighbours per round: their indices, then their positions, are
+        // all in flight before the first is used
         const int n = B.ljc[g];
-        for (int k = 0; k < n; k++) {
-            const float4 rj = fr[base + B.lj[k * nb + g]];
-            const float dx = Fi.p0.x - rj.x, dy = Fi.p0.y - rj.y, dz = Fi.p0.z - rj.z;
-            const float dr = sqrtf(dx * dx + dy * dy + dz * dz);
-            if (dr < 6.0f) {
-                const float dr2 = dr * dr, dr4 = dr2 * dr2;
-                const float s = P.lj_pref * (6.0f / (dr4 * dr4));
-                A.fx += s * dx;
-                A.fy += s * dy;
-                A.fz += s * dz;
+        for (int k0 = 0; k0 < n; k0 += 4) {
+            int jj[4];
+            float4 rj[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) jj[u] = k0 + u < n ? B.lj[(k0 + u) * nb + g] : -1;
+#pragma unroll
+            for (int u = 0; u < 4; u++) rj[u] = jj[u] >= 0 ? fr[base + jj[u]] : Fi.p0;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (jj[u] < 0) continue;
+                const float dx = Fi.p0.x - rj[u].x, dy = Fi.p0.y - rj[u].y, dz = Fi.p0.z - rj[u].z;
+                const float dr = sqrtf(dx * dx + dy * dy + dz * dz);
+                if (dr < 6.0f) {
+                    const float dr2 = dr * dr, dr4 = dr2 * dr2;
+                    const float s = P.lj_pref * (6.0f / (dr4 * dr4));
+                    A.fx += s * dx;
+                    A.fy += s * dy;
+                    A.fz += s * dz;
+                }
             }
         }
     }

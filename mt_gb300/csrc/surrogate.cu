@@ -87,17 +87,22 @@ __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, 
         const int cx = cell_coord(pi.x, inv_cell), cy = cell_coord(pi.y, inv_cell), cz = cell_coord(pi.z, inv_cell);
         const int tb = C.tbase[traj];
         const uint32_t mask = (uint32_t)C.tmask[traj];
-        int visited[27];
-        int nvis = 0;
-        for (int dz = -1; dz <= 1; dz++)
-            for (int dy = -1; dy <= 1; dy++)
-                for (int dx = -1; dx <= 1; dx++) {
-                    const int bkt = tb + (int)(cell_hash(cx + dx, cy + dy, cz + dz) & mask);
-                    bool seen = false;
-                    for (int v = 0; v < nvis; v++) seen |= (visited[v] == bkt);
-                    if (seen) continue;
-                    visited[nvis++] = bkt;
-                    const int s0 = base + C.start[bkt], s1 = s0 + C.cnt[bkt];
+        int bk[27], st[27], ct[27];
+#pragma unroll
+        for (int c = 0; c < 27; c++)
+            bk[c] = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
+#pragma unroll
+        for (int c = 0; c < 27; c++) {
+            st[c] = C.start[bk[c]];
+            ct[c] = C.cnt[bk[c]];
+        }
+        for (int c = 0; c < 27; c++) {
+            if (ct[c] == 0) continue;
+            bool seen = false;
+            for (int v = 0; v < c; v++) seen |= (bk[v] == bk[c]);
+            if (seen) continue;
+            {
+                    const int s0 = base + st[c], s1 = s0 + ct[c];
                     for (int s = s0; s < s1; s++) {
                         const float4 q = C.cell_pos[s];
                         const int jg = __float_as_int(q.w);
@@ -119,10 +124,11 @@ __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, 
                         f[sh + 8] += ux * uz * rinv;
                         f[sh + 9] += uy * uz * rinv;
                     }
-                }
-        const float4 st = stats[traj];
-        f[30] = logf(fmaxf(st.w, 1.0f));
-        const float dx = pi.x - st.x, dy = pi.y - st.y, dz = pi.z - st.z;
+            }
+        }
+        const float4 ts = stats[traj];
+        f[30] = logf(fmaxf(ts.w, 1.0f));
+        const float dx = pi.x - ts.x, dy = pi.y - ts.y, dz = pi.z - ts.z;
         f[31] = sqrtf(dx * dx + dy * dy + dz * dz) * 0.01f;
     }
 #pragma unroll
