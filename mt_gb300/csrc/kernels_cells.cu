@@ -156,15 +156,26 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
         st[c] = start[bk[c]];
         ct[c] = cnt[bk[c]];
     }
+    // one flat candidate stream over the 27 buckets (a bucket two cells hash
+    // to is taken once), so a warp pays for its longest stream, not for the
+    // longest bucket of every cell in turn
+    int total = 0;
     for (int c = 0; c < 27; c++) {
-        if (ct[c] == 0) continue;
-        const int bkt = bk[c];
-        bool seen = false;   // two cells hashed to one bucket: visit it once
-        for (int v = 0; v < c; v++) seen |= (bk[v] == bkt);
-        if (seen) continue;
-        const int s0 = base + st[c], s1 = s0 + ct[c];
-        for (int s = s0; s < s1; s++) {
-            const float4 q = cell_pos[s];
+        bool seen = false;
+        for (int v = 0; v < c; v++) seen |= (bk[v] == bk[c]);
+        if (seen) ct[c] = 0;
+        total += ct[c];
+    }
+    int c = -1, s = 0, rem = 0;
+    for (int t = 0; t < total; t++) {
+        while (rem == 0) {
+            c++;
+            s = base + st[c];
+            rem = ct[c];
+        }
+        rem--;
+        {
+            const float4 q = cell_pos[s++];
             const int jg = __float_as_int(q.w);
             const int jl = jg - base;
             const float cd = centre_dist(pi, q);
