@@ -156,26 +156,15 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
         st[c] = start[bk[c]];
         ct[c] = cnt[bk[c]];
     }
-    // one flat candidate stream over the 27 buckets (a bucket two cells hash
-    // to is taken once), so a warp pays for its longest stream, not for the
-    // longest bucket of every cell in turn
-    int total = 0;
     for (int c = 0; c < 27; c++) {
-        bool seen = false;
-        for (int v = 0; v < c; v++) seen |= (bk[v] == bk[c]);
-        if (seen) ct[c] = 0;
-        total += ct[c];
-    }
-    int c = -1, s = 0, rem = 0;
-    for (int t = 0; t < total; t++) {
-        while (rem == 0) {
-            c++;
-            s = base + st[c];
-            rem = ct[c];
-        }
-        rem--;
-        {
-            const float4 q = cell_pos[s++];
+        if (ct[c] == 0) continue;
+        const int bkt = bk[c];
+        bool seen = false;   // two cells hashed to one bucket: visit it once
+        for (int v = 0; v < c; v++) seen |= (bk[v] == bkt);
+        if (seen) continue;
+        const int s0 = base + st[c], s1 = s0 + ct[c];
+        for (int s = s0; s < s1; s++) {
+            const float4 q = cell_pos[s];
             const int jg = __float_as_int(q.w);
             const int jl = jg - base;
             const float cd = centre_dist(pi, q);
@@ -196,7 +185,7 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
                 const float rmon = h0 < 0 ? -2.0f : 2.0f;
                 const int fj = B.flags[jg];
                 if (((flags ^ fj) & kFlagBeta) != 0) {
-                    const float4 ui = fr[nb + g], uj = fr[nb + jg];
+                    const float4 ui = B.sites[g], uj = B.sites[jg];
                     const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
                     if (norm3_rn(site_delta(pi, pj, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) <
                         2.5f) {
@@ -208,8 +197,8 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
                     }
                 }
                 if (jl != il) {
-                    const float4 li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
-                    const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
+                    const float4 li1 = B.sites[nb + g], li2 = B.sites[2 * nb + g];
+                    const float4 l1 = B.sites[nb + jg], l2 = B.sites[2 * nb + jg];
                     if (norm3_rn(site_delta(pi, pj, f3(li1), f3(l2))) < 2.5f) {
                         if (nla < P.maxLat)
                             la_buf[nla] = 2 * jl;       // orientation 0 -> -j
