@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
                 const float rmon = h0 < 0 ? -2.0f : 2.0f;
                 const int fj = B.flags[jg];
                 if (((flags ^ fj) & kFlagBeta) != 0) {
-                    const float4 ui = B.sites[g], uj = B.sites[jg];
+                    const float4 ui = fr[nb + g], uj = fr[nb + jg];
                     const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
                     if (norm3_rn(site_delta(pi, pj, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) <
                         2.5f) {
@@ -197,8 +197,8 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
                     }
                 }
                 if (jl != il) {
-                    const float4 li1 = B.sites[nb + g], li2 = B.sites[2 * nb + g];
-                    const float4 l1 = B.sites[nb + jg], l2 = B.sites[2 * nb + jg];
+                    const float4 li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
+                    const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
                     if (norm3_rn(site_delta(pi, pj, f3(li1), f3(l2))) < 2.5f) {
                         if (nla < P.maxLat)
                             la_buf[nla] = 2 * jl;       // orientation 0 -> -j

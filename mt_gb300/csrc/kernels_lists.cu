@@ -61,11 +61,9 @@ __global__ void __launch_bounds__(kTile) k_rebuild(KParams P, DevBuffers B, cons
     int flags = kFlagExtra, h0 = -1;
     if (valid) {
         pi = fr[g];
-        if (P.is_assembly) {
-            ui = B.sites[g];
-            li1 = B.sites[nb + g];
-            li2 = B.sites[2 * nb + g];
-        }
+        ui = fr[nb + g];
+        li1 = fr[2 * nb + g];
+        li2 = fr[3 * nb + g];
         flags = B.flags[g];
         h0 = B.harm[g * P.maxH];
     }
@@ -92,9 +90,9 @@ __global__ void __launch_bounds__(kTile) k_rebuild(KParams P, DevBuffers B, cons
             pj = fr[jg];
             s_pos[threadIdx.x] = pj;
             if (P.is_assembly) {
-                s_uz[threadIdx.x] = B.sites[jg];
-                s_l1[threadIdx.x] = B.sites[nb + jg];
-                s_l2[threadIdx.x] = B.sites[2 * nb + jg];
+                s_uz[threadIdx.x] = fr[nb + jg];
+                s_l1[threadIdx.x] = fr[2 * nb + jg];
+                s_l2[threadIdx.x] = fr[3 * nb + jg];
                 s_flags[threadIdx.x] = B.flags[jg];
             }
         }

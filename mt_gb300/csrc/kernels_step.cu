@@ -1,10 +1,10 @@
 // kernels_step.cu - per-bead forces, the fused force + Euler-Maruyama step,
 // energies, and the state <-> Coord conversions.
 //
-// One thread per bead.  A bead's neighbours are read from the current state
-// buffer (a 16 B position gather for an LJ partner; 24 B and its orientation
-// for a harmonic, longitudinal or lateral partner); the moving bead writes
-// its new state to the other buffer, so forces and integration fuse into one
+// One thread per bead.  A bead's neighbours are read from the current frame
+// buffer (16 B gathers of precomputed lab-frame site vectors, L2-resident for
+// the batch sizes of interest); the moving bead writes its new state and new
+// site vectors to the other buffer, so forces and integration fuse into one
 // launch per step without a race.
 #include "mtg_internal.cuh"
 
@@ -58,15 +58,14 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         const int e = B.harm[g * P.maxH + k];
         const float rmon = e < 0 ? 2.0f : -2.0f;
         const int pj = base + (e < 0 ? -e : e);
-        const Frame Fj = frame_of(P, fr, B.ang_in, pj);
-        const float4 rj = Fj.p0, uj = Fj.p1;
+        const float4 rj = fr[pj], uj = fr[nb + pj];
         const float3 wi = make_float3(uzi.x * rmon, uzi.y * rmon, uzi.z * rmon);
         const float3 wj = make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon);
         const float3 d = site_delta(Fi.p0, rj, wi, wj);
         const float dr = norm3_rn(d);
         acc_pair(A, P.C, d, wi);
         if (dr < 1.0f) {
-            const float thj = Fj.p2.w;
+            const float thj = fr[2 * nb + pj].w;
             acc_bend(P, A, rmon, uj.w - Fi.p1.w, rj.w - Fi.p0.w, thj - Fi.p2.w,
                      (flags & kFlagGtp) ? P.th0_gtp : P.th0_gdp);
         }
@@ -77,8 +76,7 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         const int e = B.lon[k * nb + g];
         const float rmon = e < 0 ? 2.0f : -2.0f;
         const int pj = base + (e < 0 ? -e : e);
-        const Frame Fj = frame_of(P, fr, B.ang_in, pj);
-        const float4 rj = Fj.p0, uj = Fj.p1;
+        const float4 rj = fr[pj], uj = fr[nb + pj];
         const float3 wi = make_float3(uzi.x * rmon, uzi.y * rmon, uzi.z * rmon);
         const float3 wj = make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon);
         const float3 d = site_delta(Fi.p0, rj, wi, wj);
@@ -94,7 +92,7 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
             // theta0 of the bead nearer the plus end (:282-283)
             int glast = flags;
             if (!(Fi.p0.z > rj.z)) glast = fj >= 0 ? fj : B.flags[pj];
-            const float thj = Fj.p2.w;
+            const float thj = fr[2 * nb + pj].w;
             acc_bend(P, A, rmon, uj.w - Fi.p1.w, rj.w - Fi.p0.w, thj - Fi.p2.w,
                      (glast & kFlagGtp) ? P.th0_gtp : P.th0_gdp);
         }
@@ -107,9 +105,8 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         int j = e < 0 ? -e : e;
         if (j == kZeroCode) j = 0;
         const int pj = base + j;
-        const Frame Fj = frame_of(P, fr, B.ang_in, pj);
-        const float4 rj = Fj.p0;
-        const float4 sj = neg ? Fj.p3 : Fj.p2;
+        const float4 rj = fr[pj];
+        const float4 sj = neg ? fr[3 * nb + pj] : fr[2 * nb + pj];
         const float3 wi = neg ? f3(Fi.p2) : f3(Fi.p3);
         const float3 d = site_delta(Fi.p0, rj, wi, f3(sj));
         const float dr = norm3_rn(d);
@@ -175,44 +172,51 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
     out[5] = A.fpsi + A.tz;
 }
 
+__device__ __forceinline__ Frame load_frame(const float4 *planes, int nb, int g) {
+    Frame F;
+    F.p0 = planes[g];
+    F.p1 = planes[nb + g];
+    F.p2 = planes[2 * nb + g];
+    F.p3 = planes[3 * nb + g];
+    return F;
+}
+
 // Euler-Maruyama update of one moving bead (integrate_kernel,
-// src/compute_cuda.cu:955-963): xyz from normals gx, angles from ga; the new
-// state goes to the other buffer.
-__device__ __forceinline__ void em_update(const KParams &P, const DevBuffers &B, int g, const Frame &Fi,
-                                          const float f[6], float4 gx, float4 ga) {
+// src/compute_cuda.cu:955-963): xyz from normals gx, angles from ga.
+__device__ __forceinline__ Frame em_update(const KParams &P, const Frame &Fi, const float f[6], float4 gx,
+                                           float4 ga) {
     const float x = Fi.p0.x + (P.kr * f[0] + P.varR * gx.x);
     const float y = Fi.p0.y + (P.kr * f[1] + P.varR * gx.y);
     const float z = Fi.p0.z + (P.kr * f[2] + P.varR * gx.z);
     const float fi = Fi.p0.w + (P.kfi * f[3] + P.nfi * ga.x);
     const float psi = Fi.p1.w + (P.kfi * f[5] + P.nfi * ga.y);
     const float th = Fi.p2.w + (P.kth * f[4] + P.varTheta * ga.z);
-    store_state(B.frame_out, B.ang_out, g, x, y, z, fi, th, psi);
+    return make_frame(P, x, y, z, fi, th, psi);
 }
 
 template <bool KEEP_FORCES>
-__global__ void __launch_bounds__(256, 4) k_step_plain(KParams P, DevBuffers B) {
+__global__ void __launch_bounds__(256) k_step_plain(KParams P, DevBuffers B) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= P.nb) return;
     const int nb = P.nb;
     const int flags = B.flags[g];
+    Frame Fi = load_frame(B.frame_in, nb, g);
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const bool moving = !(flags & (kFlagExtra | kFlagFixed));
-    if (moving || (KEEP_FORCES && !(flags & kFlagExtra))) {
-        const Frame Fi = frame_of(P, B.frame_in, B.ang_in, g);
-        const int traj = B.traj[g];
-        bead_forces(P, B, g, traj, B.off[traj], flags, Fi, f);
+    if (!(flags & kFlagExtra)) {
+        const bool moving = !(flags & kFlagFixed);
+        if (moving || KEEP_FORCES) {
+            const int traj = B.traj[g];
+            bead_forces(P, B, g, traj, B.off[traj], flags, Fi, f);
+        }
         if (moving) {
             uint4 s1 = B.seeds[g], s2 = B.seeds[nb + g];
             const float4 gx = gauss4(s1), ga = gauss4(s2);
             B.seeds[g] = s1;
             B.seeds[nb + g] = s2;
-            em_update(P, B, g, Fi, f, gx, ga);
+            Fi = em_update(P, Fi, f, gx, ga);
         }
     }
-    if (!moving) {  // fixed and extra beads keep their state
-        B.frame_out[g] = B.frame_in[g];
-        B.ang_out[g] = B.ang_in[g];
-    }
+    store_frame(B.frame_out, nb, g, Fi);
     if (KEEP_FORCES) {
         B.force[g] = make_float4(f[0], f[1], f[2], 0.f);
         B.force[nb + g] = make_float4(f[3], f[4], f[5], 0.f);
@@ -230,7 +234,7 @@ __global__ void __launch_bounds__(256) k_forces(KParams P, DevBuffers B) {
     const int flags = B.flags[g];
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (!(flags & kFlagExtra)) {
-        const Frame Fi = frame_of(P, B.frame_in, B.ang_in, g);
+        const Frame Fi = load_frame(B.frame_in, nb, g);
         const int traj = B.traj[g];
         bead_forces(P, B, g, traj, B.off[traj], flags, Fi, f);
     }
@@ -261,7 +265,7 @@ __global__ void __launch_bounds__(kTile) k_energy(KParams P, DevBuffers B, const
     if (g < end) {
         const int flags = B.flags[g];
         if (!(flags & kFlagExtra)) {
-            const Frame Fi = frame_of(P, fr, B.ang_in, g);
+            const Frame Fi = load_frame(fr, nb, g);
             const float3 uzi = f3(Fi.p1);
             const bool off_tub = (flags & kFlagOnTubule) == 0;
             const int hc = (flags >> kHarmShift) & 7;
@@ -269,8 +273,7 @@ __global__ void __launch_bounds__(kTile) k_energy(KParams P, DevBuffers B, const
                 const int e = B.harm[g * P.maxH + k];
                 const float rmon = e < 0 ? 2.0f : -2.0f;
                 const int pj = base + (e < 0 ? -e : e);
-                const Frame Fj = frame_of(P, fr, B.ang_in, pj);
-                const float4 rj = Fj.p0, uj = Fj.p1;
+                const float4 rj = fr[pj], uj = fr[nb + pj];
                 const float3 d = site_delta(Fi.p0, rj, make_float3(uzi.x * rmon, uzi.y * rmon, uzi.z * rmon),
                                             make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon));
                 const float dr = norm3_rn(d);
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(kTile) k_energy(KParams P, DevBuffers B, const
                     const float th0 = (flags & kFlagGtp) ? P.th0_gtp : P.th0_gdp;
                     U[3] += P.B_psi * (1.0f - cosf((Fi.p1.w - uj.w) - P.psi_0));
                     U[4] += P.B_fi * (1.0f - cosf((Fi.p0.w - rj.w) - P.fi_0));
-                    U[5] += P.B_theta * (1.0f - cosf((Fj.p2.w - Fi.p2.w) - th0));
+                    U[5] += P.B_theta * (1.0f - cosf((fr[2 * nb + pj].w - Fi.p2.w) - th0));
                 }
             }
             const int nl = B.lonc[g];
@@ -288,8 +291,7 @@ __global__ void __launch_bounds__(kTile) k_energy(KParams P, DevBuffers B, const
                 const int e = B.lon[k * nb + g];
                 const float rmon = e < 0 ? 2.0f : -2.0f;
                 const int pj = base + (e < 0 ? -e : e);
-                const Frame Fj = frame_of(P, fr, B.ang_in, pj);
-                const float4 rj = Fj.p0, uj = Fj.p1;
+                const float4 rj = fr[pj], uj = fr[nb + pj];
                 const float3 d = site_delta(Fi.p0, rj, make_float3(uzi.x * rmon, uzi.y * rmon, uzi.z * rmon),
                                             make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon));
                 const float dr = norm3_rn(d);
@@ -301,7 +303,7 @@ __global__ void __launch_bounds__(kTile) k_energy(KParams P, DevBuffers B, const
                     const float th0 = (glast & kFlagGtp) ? P.th0_gtp : P.th0_gdp;
                     U[3] += P.B_psi * (1.0f - cosf((Fi.p1.w - uj.w) - P.psi_0));
                     U[4] += P.B_fi * (1.0f - cosf((Fi.p0.w - rj.w) - P.fi_0));
-                    U[5] += P.B_theta * (1.0f - cosf((Fi.p2.w - Fj.p2.w) - th0));
+                    U[5] += P.B_theta * (1.0f - cosf((Fi.p2.w - fr[2 * nb + pj].w) - th0));
                 }
             }
             const int nt = B.latc[g];
@@ -311,9 +313,8 @@ __global__ void __launch_bounds__(kTile) k_energy(KParams P, DevBuffers B, const
                 int j = e < 0 ? -e : e;
                 if (j == kZeroCode) j = 0;
                 const int pj = base + j;
-                const Frame Fj = frame_of(P, fr, B.ang_in, pj);
-                const float4 rj = Fj.p0;
-                const float4 sj = neg ? Fj.p3 : Fj.p2;
+                const float4 rj = fr[pj];
+                const float4 sj = neg ? fr[3 * nb + pj] : fr[2 * nb + pj];
                 const float3 d = site_delta(Fi.p0, rj, neg ? f3(Fi.p2) : f3(Fi.p3), f3(sj));
                 const float dr = norm3_rn(d);
                 const int fj = B.flags[pj];
@@ -364,36 +365,25 @@ __global__ void k_energy_totals(int nt, const double *partials, const int *work_
 }
 
 // ----------------------------------------------------------- conversions
-__global__ void k_frames_from_coords(KParams P, const float *c7, float4 *pos, float2 *ang) {
+__global__ void k_frames_from_coords(KParams P, const float *c7, float4 *planes) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= P.nb) return;
     const float *c = c7 + 7 * (size_t)g;
-    store_state(pos, ang, g, c[0], c[1], c[2], c[3], c[4], c[5]);
+    store_frame(planes, P.nb, g, make_frame(P, c[0], c[1], c[2], c[3], c[4], c[5]));
 }
 
-__global__ void k_coords_from_frames(int nb, const float4 *pos, const float2 *ang, float *c7) {
+__global__ void k_coords_from_frames(int nb, const float4 *planes, float *c7) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nb) return;
-    const float4 a = pos[g];
-    const float2 b = ang[g];
+    const float4 a = planes[g];
     float *c = c7 + 7 * (size_t)g;
     c[0] = a.x;
     c[1] = a.y;
     c[2] = a.z;
     c[3] = a.w;
-    c[4] = b.x;
-    c[5] = b.y;
+    c[4] = planes[2 * nb + g].w;
+    c[5] = planes[nb + g].w;
     c[6] = 0.f;
-}
-
-// Site planes of every bead: (R e_z, psi), (R p1, theta), (R p2, 0).
-__global__ void k_make_sites(KParams P, DevBuffers B, float4 *sites) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= P.nb) return;
-    const Frame F = frame_of(P, B.frame_in, B.ang_in, g);
-    sites[g] = F.p1;
-    sites[P.nb + g] = F.p2;
-    sites[2 * P.nb + g] = F.p3;
 }
 
 __global__ void k_forces_to_coords(int nb, const float4 *force, float *c7) {
@@ -423,14 +413,11 @@ __global__ void k_set_flags(int nb, const uint8_t *extra, const int *gtp, const 
 // --------------------------------------------------------------- launchers
 static inline int blocks(int n, int t) { return (n + t - 1) / t; }
 
-void launch_frames_from_coords(const KParams &P, const float *c7, float4 *pos, float2 *ang, cudaStream_t s) {
-    k_frames_from_coords<<<blocks(P.nb, 256), 256, 0, s>>>(P, c7, pos, ang);
+void launch_frames_from_coords(const KParams &P, const float *c7, float4 *frame, cudaStream_t s) {
+    k_frames_from_coords<<<blocks(P.nb, 256), 256, 0, s>>>(P, c7, frame);
 }
-void launch_coords_from_frames(const KParams &P, const float4 *pos, const float2 *ang, float *c7, cudaStream_t s) {
-    k_coords_from_frames<<<blocks(P.nb, 256), 256, 0, s>>>(P.nb, pos, ang, c7);
-}
-void launch_make_sites(const KParams &P, const DevBuffers &B, float4 *sites, cudaStream_t s) {
-    k_make_sites<<<blocks(P.nb, 256), 256, 0, s>>>(P, B, sites);
+void launch_coords_from_frames(const KParams &P, const float4 *frame, float *c7, cudaStream_t s) {
+    k_coords_from_frames<<<blocks(P.nb, 256), 256, 0, s>>>(P.nb, frame, c7);
 }
 void launch_forces_to_coords(const KParams &P, const float4 *force, float *c7, cudaStream_t s) {
     k_forces_to_coords<<<blocks(P.nb, 256), 256, 0, s>>>(P.nb, force, c7);

@@ -362,22 +362,23 @@ __global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevB
             continue;
         }
         const int flags = B.flags[g];
-        const float4 p0 = pi[h];
-        const float2 an = B.ang_in[g];  // (theta, psi)
+        Frame Fr;
+        Fr.p0 = pi[h];
+        Fr.p1 = B.frame_in[nb + g];
+        Fr.p2 = B.frame_in[2 * nb + g];
+        Fr.p3 = B.frame_in[3 * nb + g];
         uint4 s2 = B.seeds[nb + g];
         const float4 ga = gauss4(s2);
         B.seeds[nb + g] = s2;
         if (!(flags & (kFlagExtra | kFlagFixed))) {
             const float4 fa = B.force[nb + g];  // (ffi, ftheta, fpsi)
-            const float x = p0.x + P.kr * sx, y = p0.y + P.kr * sy, z = p0.z + P.kr * sz;
-            const float fi = p0.w + (P.kfi * fa.x + P.nfi * ga.x);
-            const float psi = an.y + (P.kfi * fa.z + P.nfi * ga.y);
-            const float th = an.x + (P.kth * fa.y + P.varTheta * ga.z);
-            store_state(B.frame_out, B.ang_out, g, x, y, z, fi, th, psi);
-        } else {
-            B.frame_out[g] = p0;
-            B.ang_out[g] = an;
+            const float x = Fr.p0.x + P.kr * sx, y = Fr.p0.y + P.kr * sy, z = Fr.p0.z + P.kr * sz;
+            const float fi = Fr.p0.w + (P.kfi * fa.x + P.nfi * ga.x);
+            const float psi = Fr.p1.w + (P.kfi * fa.z + P.nfi * ga.y);
+            const float th = Fr.p2.w + (P.kth * fa.y + P.varTheta * ga.z);
+            Fr = make_frame(P, x, y, z, fi, th, psi);
         }
+        store_frame(B.frame_out, nb, g, Fr);
     }
 }
 

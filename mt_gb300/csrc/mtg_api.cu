@@ -210,7 +210,6 @@ namespace {
 
 // The list rebuild with the engine's method.
 void launch_lists(mtg_engine *e) {
-    if (e->p.is_assembly) launch_make_sites(e->kp, e->bufs(), e->sites, e->stream);
     if (e->use_cells)
         launch_rebuild_cells(e->kp, e->bufs(), e->cells(), e->work, e->nwork, e->stream);
     else
@@ -440,11 +439,8 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
     ALLOC(e->flags, nb);
     ALLOC(e->harm, (size_t)maxH * nb);
     ALLOC(e->zs, nt);
-    ALLOC(e->frame[0], nb);
-    ALLOC(e->frame[1], nb);
-    ALLOC(e->ang[0], nb);
-    ALLOC(e->ang[1], nb);
-    if (p->is_assembly) ALLOC(e->sites, 3 * (size_t)nb);
+    ALLOC(e->frame[0], 4 * (size_t)nb);
+    ALLOC(e->frame[1], 4 * (size_t)nb);
     ALLOC(e->force, 2 * (size_t)nb);
     ALLOC(e->seeds, 2 * (size_t)nb);
     ALLOC(e->ljc, nb);
@@ -618,8 +614,7 @@ int mtg_destroy(mtg_engine *e) {
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     destroy_graphs(e);
-    void *ptrs[] = {e->off, e->traj, e->flags, e->harm, e->zs, e->frame[0], e->frame[1], e->ang[0], e->ang[1],
-                    e->sites, e->force, e->seeds,
+    void *ptrs[] = {e->off, e->traj, e->flags, e->harm, e->zs, e->frame[0], e->frame[1], e->force, e->seeds,
                     e->ljc, e->lj, e->lonc, e->lon, e->latc, e->lat, e->err, e->work, e->work_first,
                     e->en_partials, e->en_traj, e->en_bead, e->tea_r, e->tea_ci, e->tea_eps, e->tea_beta,
                     e->tea_eps_t, e->stage, e->stage_u8, e->stage_i, e->cell_tbase, e->cell_tmask,
@@ -683,7 +678,7 @@ int mtg_upload_state(mtg_engine *e, const float *r) {
     if (!e || !r) return fail(MTG_E_CONFIG, "engine or r is NULL");
     cudaSetDevice(e->device);
     CK(cudaMemcpyAsync(e->stage, r, sizeof(float) * 7 * (size_t)e->nb, cudaMemcpyHostToDevice, e->stream));
-    launch_frames_from_coords(e->kp, e->stage, e->frame[e->cur], e->ang[e->cur], e->stream);
+    launch_frames_from_coords(e->kp, e->stage, e->frame[e->cur], e->stream);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e->stream));
     e->have_state = true;
@@ -695,7 +690,7 @@ int mtg_download_state(mtg_engine *e, float *r, float *f) {
     cudaSetDevice(e->device);
     const size_t bytes = sizeof(float) * 7 * (size_t)e->nb;
     if (r) {
-        launch_coords_from_frames(e->kp, e->frame[e->cur], e->ang[e->cur], e->stage, e->stream);
+        launch_coords_from_frames(e->kp, e->frame[e->cur], e->stage, e->stream);
         CK(cudaMemcpyAsync(r, e->stage, bytes, cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
     }
@@ -938,19 +933,11 @@ int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tunin
     if (trial_steps <= 0) return fail(MTG_E_CONFIG, "trial_steps must be positive");
     cudaSetDevice(e->device);
     // snapshot of everything a trial advances: the state and the noise streams
-    const size_t fbytes = sizeof(float4) * (size_t)e->nb, abytes = sizeof(float2) * (size_t)e->nb,
-                 sbytes = sizeof(uint4) * 2 * (size_t)e->nb;
+    const size_t fbytes = sizeof(float4) * 4 * (size_t)e->nb, sbytes = sizeof(uint4) * 2 * (size_t)e->nb;
     void *snap = nullptr;
-    CK(cudaMalloc(&snap, fbytes + abytes + sbytes));
-    char *snap_a = (char *)snap + fbytes, *snap_s = snap_a + abytes;
-    auto restore = [&] {
-        cudaMemcpyAsync(e->frame[e->cur], snap, fbytes, cudaMemcpyDeviceToDevice, e->stream);
-        cudaMemcpyAsync(e->ang[e->cur], snap_a, abytes, cudaMemcpyDeviceToDevice, e->stream);
-        cudaMemcpyAsync(e->seeds, snap_s, sbytes, cudaMemcpyDeviceToDevice, e->stream);
-    };
+    CK(cudaMalloc(&snap, fbytes + sbytes));
     CK(cudaMemcpyAsync(snap, e->frame[e->cur], fbytes, cudaMemcpyDeviceToDevice, e->stream));
-    CK(cudaMemcpyAsync(snap_a, e->ang[e->cur], abytes, cudaMemcpyDeviceToDevice, e->stream));
-    CK(cudaMemcpyAsync(snap_s, e->seeds, sbytes, cudaMemcpyDeviceToDevice, e->stream));
+    CK(cudaMemcpyAsync((char *)snap + fbytes, e->seeds, sbytes, cudaMemcpyDeviceToDevice, e->stream));
     const int cur0 = e->cur;
     mtg_tuning orig;
     mtg_get_tuning(e, &orig);
@@ -974,7 +961,8 @@ int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tunin
         float ms = 0.f;
         for (int rep = 0; rep < 2 && rc == MTG_OK; rep++) {  // first run captures the graph
             e->cur = cur0;
-            restore();
+            cudaMemcpyAsync(e->frame[e->cur], snap, fbytes, cudaMemcpyDeviceToDevice, e->stream);
+            cudaMemcpyAsync(e->seeds, (char *)snap + fbytes, sbytes, cudaMemcpyDeviceToDevice, e->stream);
             rc = mtg_step_timed(e, first_step, trial_steps, &ms);
         }
         if (rc) break;
@@ -984,7 +972,8 @@ int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tunin
         }
     }
     e->cur = cur0;
-    restore();
+    cudaMemcpyAsync(e->frame[e->cur], snap, fbytes, cudaMemcpyDeviceToDevice, e->stream);
+    cudaMemcpyAsync(e->seeds, (char *)snap + fbytes, sbytes, cudaMemcpyDeviceToDevice, e->stream);
     cudaStreamSynchronize(e->stream);
     cudaFree(snap);
     if (rc) {

@@ -23,9 +23,7 @@ struct mtg_engine {
     // device
     int *off = nullptr, *traj = nullptr, *flags = nullptr, *harm = nullptr;
     float *zs = nullptr;
-    float4 *frame[2] = {nullptr, nullptr};  // positions (x, y, z, fi), double-buffered
-    float2 *ang[2] = {nullptr, nullptr};    // (theta, psi), double-buffered
-    float4 *sites = nullptr;                // [3nb] site planes for assembly-list rebuilds
+    float4 *frame[2] = {nullptr, nullptr};
     float4 *force = nullptr;
     uint4 *seeds = nullptr;
     int *ljc = nullptr, *lj = nullptr, *lonc = nullptr, *lon = nullptr, *latc = nullptr, *lat = nullptr;
@@ -101,9 +99,6 @@ struct mtg_engine {
         b.zs = zs;
         b.frame_in = frame[cur];
         b.frame_out = frame[cur ^ 1];
-        b.ang_in = ang[cur];
-        b.ang_out = ang[cur ^ 1];
-        b.sites = sites;
         b.force = force;
         b.seeds = seeds;
         b.ljc = ljc;

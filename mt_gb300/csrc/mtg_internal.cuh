@@ -2,13 +2,14 @@
 // object of the GB300 engine.  Not part of the public ABI (include/mtg.h).
 //
 // HBM layout (nb beads over nt trajectories, CSR offsets):
-//   state[2]   : double-buffered, 24 B per bead: pos float4 (x, y, z, fi)
-//                and ang float2 (theta, psi).  A bead's binding sites come
-//                from its orientation R = Rz(psi) Ry(theta) Rx(fi) (make_frame)
-//                where they are needed: three sincos per orientation-
-//                dependent neighbour instead of 40 more bytes per bead-step.
-//   sites[3nb] : site planes (R e_z, psi), (R p1, theta), (R p2, 0) of every
-//                bead, written at a list rebuild for the assembly-list tests.
+//   frame[2]   : two buffers of 4 planes x nb float4 (double-buffered state)
+//                plane 0 = (x, y, z, fi)
+//                plane 1 = (R e_z, psi)       axial site direction
+//                plane 2 = (R p1, theta)      lateral site p1 in the lab frame
+//                plane 3 = (R p2, 0)          lateral site p2 in the lab frame
+//                R = Rz(psi) Ry(theta) Rx(fi) is the bead's orientation; the
+//                planes are written by the kernel that moves the bead, so a
+//                neighbour's sites cost one 16 B gather instead of six sin/cos.
 //   flags[nb]  : bit 0 extra, 1 fixed, 2 mon_type, 3 gtp==1, 4 on_tubule!=0,
 //                bits 8..10 harmonic count
 //   harm[nb*maxH] : harmonic partners, local index, reference sign encoding
@@ -69,11 +70,8 @@ struct DevBuffers {
     const int *flags;      // [nb]
     const int *harm;       // [nb*maxH]
     const float *zs;       // [nt]
-    float4 *frame_in;      // positions of the current state (x, y, z, fi)
-    float4 *frame_out;     // positions of the next state
-    float2 *ang_in;        // (theta, psi) of the current state
-    float2 *ang_out;       // (theta, psi) of the next state
-    const float4 *sites;   // [3nb] site planes of the last rebuild (assembly mode)
+    float4 *frame_in;      // 4 planes
+    float4 *frame_out;     // 4 planes
     float4 *force;         // 2 planes (may be null where unused)
     uint4 *seeds;          // [2nb]
     int *ljc, *lj, *lonc, *lon, *latc, *lat;
@@ -151,16 +149,11 @@ __device__ __forceinline__ Frame make_frame(const KParams &P, float x, float y, 
     return F;
 }
 
-// Full frame (positions and site planes) of bead g from its 24 B state.
-__device__ __forceinline__ Frame frame_of(const KParams &P, const float4 *pos, const float2 *ang, int g) {
-    const float4 a = pos[g];
-    const float2 b = ang[g];
-    return make_frame(P, a.x, a.y, a.z, a.w, b.x, b.y);
-}
-__device__ __forceinline__ void store_state(float4 *pos, float2 *ang, int g, float x, float y, float z, float fi,
-                                            float theta, float psi) {
-    pos[g] = make_float4(x, y, z, fi);
-    ang[g] = make_float2(theta, psi);
+__device__ __forceinline__ void store_frame(float4 *planes, int nb, int g, const Frame &F) {
+    planes[g] = F.p0;
+    planes[nb + g] = F.p1;
+    planes[2 * nb + g] = F.p2;
+    planes[3 * nb + g] = F.p3;
 }
 
 // ------------------------------------------------------------ potentials
@@ -222,11 +215,8 @@ __device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz) {
 
 // ------------------------------------------------------ host entry points
 // (kernel launchers, defined in the .cu files)
-void launch_frames_from_coords(const KParams &P, const float *coords7, float4 *pos, float2 *ang, cudaStream_t s);
-void launch_coords_from_frames(const KParams &P, const float4 *pos, const float2 *ang, float *coords7,
-                               cudaStream_t s);
-// site planes of every bead into sites [3nb] (before an assembly-list rebuild)
-void launch_make_sites(const KParams &P, const DevBuffers &B, float4 *sites, cudaStream_t s);
+void launch_frames_from_coords(const KParams &P, const float *coords7, float4 *frame, cudaStream_t s);
+void launch_coords_from_frames(const KParams &P, const float4 *frame, float *coords7, cudaStream_t s);
 void launch_forces_to_coords(const KParams &P, const float4 *force, float *coords7, cudaStream_t s);
 void launch_rebuild(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
 void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffers &C, const int2 *work, int nwork,
