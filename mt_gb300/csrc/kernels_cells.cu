@@ -38,7 +38,6 @@ __global__ void k_cell_count(KParams P, const float4 *pos, const int *traj, cons
 __global__ void __launch_bounds__(1024) k_cell_scan(const int *tbase, const int *cnt, int *start, int *cursor) {
     const int t = blockIdx.x;
     const int b0 = tbase[t], n = tbase[t + 1] - tbase[t];
-    __shared__ int s_part[1024];
     __shared__ int s_warp[32];
     const int per = (n + blockDim.x - 1) / blockDim.x;
     const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
@@ -63,7 +62,6 @@ __global__ void __launch_bounds__(1024) k_cell_scan(const int *tbase, const int 
     }
     __syncthreads();
     int run = (v - local) + (wid > 0 ? s_warp[wid - 1] : 0);
-    s_part[threadIdx.x] = run;
     for (int i = lo; i < hi; i++) {
         start[b0 + i] = run;
         cursor[b0 + i] = run;
@@ -73,15 +71,42 @@ __global__ void __launch_bounds__(1024) k_cell_scan(const int *tbase, const int 
 
 // Bucket-ordered bead lists; positions are relative to the trajectory's
 // first bead, so slots of trajectory t start at off[t].
-__global__ void k_cell_fill(int nb, const int *traj, const int *off, const int *key, int *cursor, int *cell_bead,
-                            const float4 *pos, float4 *cell_pos) {
+__global__ void k_cell_fill(int nb, const int *traj, const int *off, const int *key, const int *flags, int *cursor,
+                            int *cell_bead, const float4 *pos, float4 *cell_pos) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nb) return;
     const int slot = off[traj[g]] + atomicAdd(&cursor[key[g]], 1);
     cell_bead[slot] = g;
     float4 p = pos[g];
-    p.w = __int_as_float(g);   // bucket-ordered copy of the positions, bead index in w
+    // bucket-ordered copy of the positions, bead index (and the extra flag) in w
+    p.w = __int_as_float(g | ((flags[g] & kFlagExtra) ? kCellExtraBit : 0));
     cell_pos[slot] = p;
+}
+
+// Ascending bead index within every bucket (the atomic fill leaves them in
+// arrival order), so that sums over a bucket are reproducible.  One CTA per
+// trajectory, one thread per bucket; buckets hold a few beads.
+__global__ void k_cell_sort(const int *off, const int *tbase, const int *tmask, const int *start, const int *cnt,
+                            int *cell_bead, float4 *cell_pos) {
+    const int t = blockIdx.x, base = off[t], tb = tbase[t], nbk = tmask[t] + 1;
+    for (int b = threadIdx.x; b < nbk; b += blockDim.x) {
+        const int n = cnt[tb + b];
+        if (n < 2) continue;
+        int *cb = cell_bead + base + start[tb + b];
+        float4 *cp = cell_pos + base + start[tb + b];
+        for (int i = 1; i < n; i++) {
+            const int v = cb[i];
+            const float4 pv = cp[i];
+            int j = i - 1;
+            while (j >= 0 && cb[j] > v) {
+                cb[j + 1] = cb[j];
+                cp[j + 1] = cp[j];
+                j--;
+            }
+            cb[j + 1] = v;
+            cp[j + 1] = pv;
+        }
+    }
 }
 
 __device__ __forceinline__ void isort(int *a, int n) {
@@ -165,7 +190,7 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
         const int s0 = base + st[c], s1 = s0 + ct[c];
         for (int s = s0; s < s1; s++) {
             const float4 q = cell_pos[s];
-            const int jg = __float_as_int(q.w);
+            const int jg = __float_as_int(q.w) & kCellIndexMask;
             const int jl = jg - base;
             const float cd = centre_dist(pi, q);
             if (do_lj && jl != il && cd < P.ljcut) {
@@ -254,8 +279,9 @@ float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, flo
     cudaMemsetAsync(C.cnt, 0, sizeof(int) * C.nbuckets, s);
     k_cell_count<<<nblk(P.nb, 256), 256, 0, s>>>(P, B.frame_in, B.traj, C.tbase, C.tmask, inv, C.key, C.cnt);
     k_cell_scan<<<P.nt, 1024, 0, s>>>(C.tbase, C.cnt, C.start, C.cursor);
-    k_cell_fill<<<nblk(P.nb, 256), 256, 0, s>>>(P.nb, B.traj, B.off, C.key, C.cursor, C.cell_bead, B.frame_in,
-                                                 C.cell_pos);
+    k_cell_fill<<<nblk(P.nb, 256), 256, 0, s>>>(P.nb, B.traj, B.off, C.key, B.flags, C.cursor, C.cell_bead,
+                                                 B.frame_in, C.cell_pos);
+    k_cell_sort<<<P.nt, 256, 0, s>>>(B.off, C.tbase, C.tmask, C.start, C.cnt, C.cell_bead, C.cell_pos);
     return inv;
 }
 

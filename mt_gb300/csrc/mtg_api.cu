@@ -190,6 +190,7 @@ int check_errors(mtg_engine *e) {
         if (h & kErrTeaEps)
             return fail(MTG_E_TEA_EPS, "TEA epsilon out of range (> 1 in capricious mode, > epsmax, or a too diagonal tensor)");
         if (h & kErrNonFinite) return fail(MTG_E_NONFINITE, "non-finite energy total");
+        if (h & kErrTimeout) return fail(MTG_E_TIMEOUT, "a bounded wait for the tensor cores ran out");
     }
     return MTG_OK;
 }

@@ -34,6 +34,7 @@ constexpr int kZeroCode = 999999;   // lateral encoding of bead 0 (src/mt.h:35)
 constexpr int kErrOverflow = 1;     // bit in the device error word
 constexpr int kErrTeaEps = 2;
 constexpr int kErrNonFinite = 4;
+constexpr int kErrTimeout = 8;     // a bounded wait on the tensor cores ran out
 
 // Scalars every kernel reads (passed by value: constant bank).
 struct KParams {
@@ -197,9 +198,11 @@ struct CellBuffers {
     const int *tmask;      // [nt] table size - 1 (power of two)
     int *key;              // [nb] bucket of each bead
     int *cnt, *start, *cursor;  // [nbuckets]
-    int *cell_bead;        // [nb] beads in bucket order
-    float4 *cell_pos;      // [nb] their positions, bead index in w
+    int *cell_bead;        // [nb] beads in bucket order (ascending index within a bucket)
+    float4 *cell_pos;      // [nb] their positions; w = bead index | kCellExtraBit for extra beads
 };
+constexpr int kCellIndexMask = 0x7fffffff;
+constexpr int kCellExtraBit = (int)0x80000000u;
 constexpr int kCellMaxLong = 16;   // largest list capacities the cell rebuild buffers locally
 constexpr int kCellMaxLat = 32;
 

@@ -61,5 +61,11 @@ cudaError_t launch_adam(const Weights &W, const float *G, int nparts, float lr, 
 cudaError_t launch_refresh(const Weights &W, cudaStream_t s);
 cudaError_t launch_loss_sum(const float *part, int nparts, float *out, cudaStream_t s);
 
+// Inference on the tcgen05 tensor cores (kernels_mlp_tc.cu): Y = network of
+// the normalised X, n rows; a wait that runs out sets kErrTimeout in *err.
+cudaError_t prepare_tc();
+cudaError_t launch_infer_tc(const Weights &W, const float *X, int n, const float *norm, float *Y, int *err,
+                            cudaStream_t s);
+
 }  // namespace mlp
 }  // namespace mtg

@@ -70,20 +70,41 @@ __global__ void k_traj_stats(KParams P, DevBuffers B, float4 *stats) {
     }
 }
 
+// Shell accumulation of one neighbour: the ten features of its shell.
+__device__ __forceinline__ void desc_add(float (&s)[10], float rinv, float ux, float uy, float uz) {
+    const float r2i = rinv * rinv;
+    s[0] += 1.0f;
+    s[1] += rinv;
+    s[2] += r2i;
+    s[3] += r2i * rinv;
+    s[4] += ux * ux * rinv;
+    s[5] += uy * uy * rinv;
+    s[6] += uz * uz * rinv;
+    s[7] += ux * uy * rinv;
+    s[8] += ux * uz * rinv;
+    s[9] += uy * uz * rinv;
+}
+
+// One thread per bead, taken in bucket order: the threads of a warp sit in
+// one or two cells and walk the same 27-cell neighbourhood, so candidate
+// loads are broadcasts and the loops mostly uniform.  Cells are 20 nm; the
+// candidates of a bucket are visited in ascending bead index.
 __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, CellBuffers C, const int2 *work,
                                                        float inv_cell, const float4 *stats, float *desc,
                                                        const int *gate) {
     if (gate && *gate) return;
     const int2 w = work[blockIdx.x];
-    const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
-    const int g = w.y + threadIdx.x;
-    if (g >= end) return;
-    float f[kF];
+    const int traj = w.x, end = B.off[traj + 1];
+    const int base = B.off[traj];
+    const int slot = w.y + threadIdx.x;
+    if (slot >= end) return;
+    const float4 pi = C.cell_pos[slot];
+    const int word = __float_as_int(pi.w), g = word & kCellIndexMask;
+    float s0[10], s1[10], s2[10];
 #pragma unroll
-    for (int k = 0; k < kF; k++) f[k] = 0.f;
-    const int flags = B.flags[g];
-    if (!(flags & kFlagExtra)) {
-        const float4 pi = B.frame_in[g];
+    for (int k = 0; k < 10; k++) s0[k] = s1[k] = s2[k] = 0.f;
+    float f30 = 0.f, f31 = 0.f;
+    if (!(word & kCellExtraBit)) {
         const int cx = cell_coord(pi.x, inv_cell), cy = cell_coord(pi.y, inv_cell), cz = cell_coord(pi.z, inv_cell);
         const int tb = C.tbase[traj];
         const uint32_t mask = (uint32_t)C.tmask[traj];
@@ -96,43 +117,43 @@ __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, 
             st[c] = C.start[bk[c]];
             ct[c] = C.cnt[bk[c]];
         }
+#pragma unroll
         for (int c = 0; c < 27; c++) {
-            if (ct[c] == 0) continue;
-            bool seen = false;
+            bool seen = false;   // two cells hashed to one bucket: visit it once
+#pragma unroll
             for (int v = 0; v < c; v++) seen |= (bk[v] == bk[c]);
-            if (seen) continue;
-            {
-                    const int s0 = base + st[c], s1 = s0 + ct[c];
-                    for (int s = s0; s < s1; s++) {
-                        const float4 q = C.cell_pos[s];
-                        const int jg = __float_as_int(q.w);
-                        const float ex = q.x - pi.x, ey = q.y - pi.y, ez = q.z - pi.z;
-                        const float r2 = ex * ex + ey * ey + ez * ez;
-                        if (!(r2 < kDescCut * kDescCut) || r2 <= 0.f || jg == g) continue;
-                        if (B.flags[jg] & kFlagExtra) continue;
-                        const float rinv = rsqrtf(r2), r = r2 * rinv;
-                        const int sh = r < 5.0f ? 0 : (r < 10.0f ? 10 : 20);
-                        const float ux = ex * rinv, uy = ey * rinv, uz = ez * rinv;
-                        f[sh + 0] += 1.0f;
-                        f[sh + 1] += rinv;
-                        f[sh + 2] += rinv * rinv;
-                        f[sh + 3] += rinv * rinv * rinv;
-                        f[sh + 4] += ux * ux * rinv;
-                        f[sh + 5] += uy * uy * rinv;
-                        f[sh + 6] += uz * uz * rinv;
-                        f[sh + 7] += ux * uy * rinv;
-                        f[sh + 8] += ux * uz * rinv;
-                        f[sh + 9] += uy * uz * rinv;
-                    }
+            if (seen || ct[c] == 0) continue;
+            const int s1e = base + st[c] + ct[c];
+            for (int s = base + st[c]; s < s1e; s++) {
+                const float4 q = C.cell_pos[s];
+                const int wj = __float_as_int(q.w);
+                const float ex = q.x - pi.x, ey = q.y - pi.y, ez = q.z - pi.z;
+                const float r2 = ex * ex + ey * ey + ez * ez;
+                if (!(r2 < kDescCut * kDescCut) || !(r2 > 0.f) || (wj & kCellExtraBit) || wj == g) continue;
+                const float rinv = rsqrtf(r2), r = r2 * rinv;
+                const float ux = ex * rinv, uy = ey * rinv, uz = ez * rinv;
+                if (r < 5.0f)
+                    desc_add(s0, rinv, ux, uy, uz);
+                else if (r < 10.0f)
+                    desc_add(s1, rinv, ux, uy, uz);
+                else
+                    desc_add(s2, rinv, ux, uy, uz);
             }
         }
         const float4 ts = stats[traj];
-        f[30] = logf(fmaxf(ts.w, 1.0f));
+        f30 = logf(fmaxf(ts.w, 1.0f));
         const float dx = pi.x - ts.x, dy = pi.y - ts.y, dz = pi.z - ts.z;
-        f[31] = sqrtf(dx * dx + dy * dy + dz * dz) * 0.01f;
+        f31 = sqrtf(dx * dx + dy * dy + dz * dz) * 0.01f;
     }
-#pragma unroll
-    for (int k = 0; k < kF; k++) desc[(size_t)g * kF + k] = f[k];
+    float4 *o = reinterpret_cast<float4 *>(desc + (size_t)g * kF);
+    o[0] = make_float4(s0[0], s0[1], s0[2], s0[3]);
+    o[1] = make_float4(s0[4], s0[5], s0[6], s0[7]);
+    o[2] = make_float4(s0[8], s0[9], s1[0], s1[1]);
+    o[3] = make_float4(s1[2], s1[3], s1[4], s1[5]);
+    o[4] = make_float4(s1[6], s1[7], s1[8], s1[9]);
+    o[5] = make_float4(s2[0], s2[1], s2[2], s2[3]);
+    o[6] = make_float4(s2[4], s2[5], s2[6], s2[7]);
+    o[7] = make_float4(s2[8], s2[9], f30, f31);
 }
 
 // Exact targets from the current epsilon pass: C_i and beta.
@@ -279,6 +300,7 @@ struct mtg_surrogate {
     float h_norm[2 * mlp::kIn] = {0};
     float h_ynorm[2 * mlp::kOut] = {0};
     __nv_bfloat16 *bf = nullptr;  // all BF16 copies
+    int *err = nullptr;            // device error word of the tensor-core inference
     int adam_step = 0;
 };
 
@@ -312,6 +334,7 @@ int mtg_surrogate_create(int device, int seed, mtg_surrogate **out) {
     *out = nullptr;
     SCK(cudaSetDevice(device));
     SCK(mlp::prepare());
+    SCK(mlp::prepare_tc());
     auto *s = new mtg_surrogate();
     s->device = device;
     SCK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -331,6 +354,8 @@ int mtg_surrogate_create(int device, int seed, mtg_surrogate **out) {
     s->W.w4t = s->W.w3t + mlp::kHid * mlp::kHid;
     SCK(cudaMalloc(&s->norm, sizeof(s->h_norm)));
     SCK(cudaMalloc(&s->ynorm, sizeof(s->h_ynorm)));
+    SCK(cudaMalloc(&s->err, sizeof(int)));
+    SCK(cudaMemsetAsync(s->err, 0, sizeof(int), s->stream));
     // Glorot-uniform weights, zero biases, identity normalisation
     std::vector<float> h(P, 0.f);
     std::mt19937 rng((uint32_t)seed);
@@ -363,6 +388,7 @@ int mtg_surrogate_destroy(mtg_surrogate *s) {
     cudaFree(s->bf);
     cudaFree(s->norm);
     cudaFree(s->ynorm);
+    cudaFree(s->err);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return MTG_OK;
@@ -405,11 +431,17 @@ int mtg_surrogate_predict(mtg_surrogate *s, const float *X, int n, float *Y) {
     SCK(cudaMalloc(&dX, sizeof(float) * (size_t)n * mlp::kIn + 16));
     SCK(cudaMalloc(&dY, sizeof(float) * (size_t)n * mlp::kOut + 16));
     SCK(cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * mlp::kIn, cudaMemcpyHostToDevice, s->stream));
-    SCK(mlp::launch_forward(s->W, dX, nullptr, n, s->norm, dY, nullptr, s->stream));
+    SCK(mlp::launch_infer_tc(s->W, dX, n, s->norm, dY, s->err, s->stream));
+    int herr = 0;
     SCK(cudaMemcpyAsync(Y, dY, sizeof(float) * (size_t)n * mlp::kOut, cudaMemcpyDeviceToHost, s->stream));
+    SCK(cudaMemcpyAsync(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaStreamSynchronize(s->stream));
     cudaFree(dX);
     cudaFree(dY);
+    if (herr) {
+        cudaMemsetAsync(s->err, 0, sizeof(int), s->stream);
+        return sfail(MTG_E_TIMEOUT, "a bounded wait for the tensor cores ran out");
+    }
     // back to target units
     for (int i = 0; i < n; i++)
         for (int k = 0; k < mlp::kOut; k++)
@@ -597,7 +629,7 @@ void enqueue_surrogate_eps(mtg_engine *e) {
     const float inv = bin_beads(e->kp, B, e->cells(), kDescCut, e->stream);
     k_descriptors<<<e->nwork, kTile, 0, e->stream>>>(e->kp, B, e->cells(), e->work, inv, e->surr_stats, e->surr_desc,
                                                      gate);
-    mlp::launch_forward(e->surr->W, e->surr_desc, nullptr, e->nb, e->surr->norm, e->surr_pred, nullptr, e->stream);
+    mlp::launch_infer_tc(e->surr->W, e->surr_desc, e->nb, e->surr->norm, e->surr_pred, e->err, e->stream);
     k_surr_beta<<<e->nt, 256, 0, e->stream>>>(e->kp, B, e->surr_pred, e->surr->ynorm, gate);
     k_surr_ci<<<(e->nb + 255) / 256, 256, 0, e->stream>>>(e->kp, B, e->surr_pred, e->surr->ynorm, gate);
     // after a fallback the exact pass runs instead (gated on the flag)

@@ -92,3 +92,44 @@ def normalise(X, T, norm):
     """Applies the 72-float normalisation of mtg_surrogate_get_params."""
     xm, xis, tm, ts = norm[:IN], norm[IN:2 * IN], norm[2 * IN:2 * IN + OUT], norm[2 * IN + OUT:]
     return (np.asarray(X, np.float64) - xm) * xis, (np.asarray(T, np.float64) - tm) / ts
+
+
+DESC_CUT = 20.0
+SHELLS = (0.0, 5.0, 10.0, 20.0)
+
+
+def descriptors(coords, offsets, extra):
+    """The 32-feature per-bead descriptor in FP64 (no reference counterpart:
+    the learned TEA's input).  For each bead i of trajectory t, over the
+    non-extra beads j != i of t with 0 < r_ij < 20 nm, in the shells
+    [0,5), [5,10), [10,20) nm: count, sum 1/r, 1/r^2, 1/r^3, and
+    sum u_a u_b / r for (a,b) = xx, yy, zz, xy, xz, yz with u = (r_j - r_i)/r;
+    then log N' (non-extra beads of t) and |r_i - centroid of t| / 100 nm.
+    Extra beads get all zeros."""
+    pos = np.asarray(coords, np.float64)[:, :3]
+    extra = np.asarray(extra).astype(bool)
+    out = np.zeros((len(pos), IN))
+    for t in range(len(offsets) - 1):
+        a, b = int(offsets[t]), int(offsets[t + 1])
+        p = pos[a:b]
+        act = ~extra[a:b]
+        n_act = int(act.sum())
+        cen = p[act].mean(0) if n_act else np.zeros(3)
+        d = p[None, :, :] - p[:, None, :]            # d[i, j] = r_j - r_i
+        r = np.sqrt((d * d).sum(-1))
+        ok = act[None, :] & (r > 0) & (r < DESC_CUT)
+        np.fill_diagonal(ok, False)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ri = np.where(ok, 1.0 / r, 0.0)
+            u = np.where(ok[..., None], d * ri[..., None], 0.0)
+        terms = [np.ones_like(ri), ri, ri ** 2, ri ** 3,
+                 u[..., 0] ** 2 * ri, u[..., 1] ** 2 * ri, u[..., 2] ** 2 * ri,
+                 u[..., 0] * u[..., 1] * ri, u[..., 0] * u[..., 2] * ri, u[..., 1] * u[..., 2] * ri]
+        for s in range(3):
+            m = ok & (r >= SHELLS[s]) & (r < SHELLS[s + 1])
+            for k, v in enumerate(terms):
+                out[a:b, 10 * s + k] = np.where(m, v, 0.0).sum(1)
+        out[a:b, 30] = np.log(max(n_act, 1))
+        out[a:b, 31] = np.sqrt(((p - cen) ** 2).sum(1)) * 0.01
+        out[a:b][~act] = 0.0
+    return out

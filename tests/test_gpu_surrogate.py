@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 from helpers import small_system
+from mt_gb300 import synth
 from oracle import mlp_oracle as M
 
 pytestmark = pytest.mark.gpu
@@ -45,6 +46,30 @@ def test_predict_matches_cpu_oracle(engine_mod):
     y = s.predict(X)
     y_ref = y_ref * nrm[2 * M.IN + M.OUT:] + nrm[2 * M.IN:2 * M.IN + M.OUT]
     assert np.abs(y - y_ref).max() < 2e-2 * (np.abs(y_ref).max() + 1e-3)
+
+
+def check_descriptors(engine_mod, b):
+    e = engine_mod.Engine(b)
+    e.upload_state(b.coords)
+    X, _ = e.tea_training_data(targets=False)
+    state = e.download_state()
+    e.close()
+    ref = M.descriptors(state, b.offsets, b.extra)
+    assert np.all(X[b.extra != 0] == 0)
+    # per feature column, relative to its norm (FP32 sums of up to a few hundred terms)
+    for k in range(M.IN):
+        den = np.linalg.norm(ref[:, k]) + 1e-12
+        assert np.linalg.norm(X[:, k] - ref[:, k]) / den < 2e-5, (k, np.linalg.norm(X[:, k] - ref[:, k]) / den)
+
+
+def test_descriptors_match_cpu_oracle(engine_mod):
+    check_descriptors(engine_mod, small_system(seed=35, ntr=3, n_mon=20, n_free=200, tea=True, extra=2))
+
+
+def test_descriptors_match_cpu_oracle_ragged(engine_mod):
+    p = synth.default_params(seed=36, hdi_on=1)
+    check_descriptors(engine_mod, synth.ragged_batch(p, 5, seed=36, pf_range=(8, 20), free_range=(0, 300),
+                                                     cube=60.0))
 
 
 def tea_dataset(engine_mod, seed, snapshots=12, every=5):
