@@ -84,28 +84,28 @@ __global__ void k_cell_fill(int nb, const int *traj, const int *off, const int *
 }
 
 // Ascending bead index within every bucket (the atomic fill leaves them in
-// arrival order), so that sums over a bucket are reproducible.  One CTA per
-// trajectory, one thread per bucket; buckets hold a few beads.
+// arrival order), so that sums over a bucket are reproducible.  Grid
+// (trajectory, bucket chunk), one thread per bucket; buckets hold a few beads.
 __global__ void k_cell_sort(const int *off, const int *tbase, const int *tmask, const int *start, const int *cnt,
                             int *cell_bead, float4 *cell_pos) {
     const int t = blockIdx.x, base = off[t], tb = tbase[t], nbk = tmask[t] + 1;
-    for (int b = threadIdx.x; b < nbk; b += blockDim.x) {
-        const int n = cnt[tb + b];
-        if (n < 2) continue;
-        int *cb = cell_bead + base + start[tb + b];
-        float4 *cp = cell_pos + base + start[tb + b];
-        for (int i = 1; i < n; i++) {
-            const int v = cb[i];
-            const float4 pv = cp[i];
-            int j = i - 1;
-            while (j >= 0 && cb[j] > v) {
-                cb[j + 1] = cb[j];
-                cp[j + 1] = cp[j];
-                j--;
-            }
-            cb[j + 1] = v;
-            cp[j + 1] = pv;
+    const int b = blockIdx.y * blockDim.x + threadIdx.x;
+    if (b >= nbk) return;
+    const int n = cnt[tb + b];
+    if (n < 2) return;
+    int *cb = cell_bead + base + start[tb + b];
+    float4 *cp = cell_pos + base + start[tb + b];
+    for (int i = 1; i < n; i++) {
+        const int v = cb[i];
+        const float4 pv = cp[i];
+        int j = i - 1;
+        while (j >= 0 && cb[j] > v) {
+            cb[j + 1] = cb[j];
+            cp[j + 1] = cp[j];
+            j--;
         }
+        cb[j + 1] = v;
+        cp[j + 1] = pv;
     }
 }
 
@@ -281,7 +281,8 @@ float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, flo
     k_cell_scan<<<P.nt, 1024, 0, s>>>(C.tbase, C.cnt, C.start, C.cursor);
     k_cell_fill<<<nblk(P.nb, 256), 256, 0, s>>>(P.nb, B.traj, B.off, C.key, B.flags, C.cursor, C.cell_bead,
                                                  B.frame_in, C.cell_pos);
-    k_cell_sort<<<P.nt, 256, 0, s>>>(B.off, C.tbase, C.tmask, C.start, C.cnt, C.cell_bead, C.cell_pos);
+    k_cell_sort<<<dim3(P.nt, (C.max_buckets + 127) / 128), 128, 0, s>>>(B.off, C.tbase, C.tmask, C.start, C.cnt,
+                                                                        C.cell_bead, C.cell_pos);
     return inv;
 }
 

@@ -475,6 +475,7 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
         while (size < n) size <<= 1;
         tbase[tr + 1] = tbase[tr] + size;
         tmask[tr] = size - 1;
+        e->cell_max_buckets = size > e->cell_max_buckets ? size : e->cell_max_buckets;
     }
     e->cell_nbuckets = tbase[nt];
     ALLOC(e->cell_tbase, nt + 1);

@@ -63,7 +63,7 @@ struct mtg_engine {
     int *cell_tbase = nullptr, *cell_tmask = nullptr, *cell_key = nullptr, *cell_cnt = nullptr;
     int *cell_start = nullptr, *cell_cursor = nullptr, *cell_bead = nullptr;
     float4 *cell_pos = nullptr;
-    int cell_nbuckets = 0;
+    int cell_nbuckets = 0, cell_max_buckets = 0;
     // learned TEA (surrogate.cu)
     struct mtg_surrogate *surr = nullptr;
     int surr_recheck = 0;
@@ -79,6 +79,7 @@ struct mtg_engine {
     mtg::CellBuffers cells() const {
         mtg::CellBuffers c{};
         c.nbuckets = cell_nbuckets;
+        c.max_buckets = cell_max_buckets;
         c.tbase = cell_tbase;
         c.tmask = cell_tmask;
         c.key = cell_key;

@@ -194,6 +194,7 @@ __device__ __forceinline__ float norm3_rn(float3 d) {
 // Spatial-hash buffers of the cell-list rebuild (kernels_cells.cu).
 struct CellBuffers {
     int nbuckets;          // sum over trajectories of their table sizes
+    int max_buckets;       // largest table of one trajectory
     const int *tbase;      // [nt+1] first bucket of each trajectory's table
     const int *tmask;      // [nt] table size - 1 (power of two)
     int *key;              // [nb] bucket of each bead

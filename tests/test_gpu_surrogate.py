@@ -48,9 +48,13 @@ def test_predict_matches_cpu_oracle(engine_mod):
     assert np.abs(y - y_ref).max() < 2e-2 * (np.abs(y_ref).max() + 1e-3)
 
 
-def check_descriptors(engine_mod, b):
+def check_descriptors(engine_mod, b, seed):
+    # thermal jitter: exact lattice distances (4 nm multiples) would sit on the
+    # 20 nm cutoff, where FP32 and FP64 may decide differently
+    coords = b.coords.copy()
+    coords[:, :3] += np.random.default_rng(seed).normal(0.0, 0.01, size=(len(coords), 3)).astype(np.float32)
     e = engine_mod.Engine(b)
-    e.upload_state(b.coords)
+    e.upload_state(coords)
     X, _ = e.tea_training_data(targets=False)
     state = e.download_state()
     e.close()
@@ -63,13 +67,13 @@ def check_descriptors(engine_mod, b):
 
 
 def test_descriptors_match_cpu_oracle(engine_mod):
-    check_descriptors(engine_mod, small_system(seed=35, ntr=3, n_mon=20, n_free=200, tea=True, extra=2))
+    check_descriptors(engine_mod, small_system(seed=35, ntr=3, n_mon=20, n_free=200, tea=True, extra=2), 35)
 
 
 def test_descriptors_match_cpu_oracle_ragged(engine_mod):
     p = synth.default_params(seed=36, hdi_on=1)
     check_descriptors(engine_mod, synth.ragged_batch(p, 5, seed=36, pf_range=(8, 20), free_range=(0, 300),
-                                                     cube=60.0))
+                                                     cube=60.0), 36)
 
 
 def tea_dataset(engine_mod, seed, snapshots=12, every=5):
