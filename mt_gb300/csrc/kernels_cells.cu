@@ -272,7 +272,8 @@ inline int nblk(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
 
-float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, float reach, cudaStream_t s) {
+float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, float reach, bool ordered,
+                cudaStream_t s) {
     // cells slightly larger than the reach, so that rounding of x / edge can
     // never put two beads closer than the reach two cells apart
     const float inv = 1.0f / (reach * 1.001f + 1e-3f);
@@ -281,15 +282,16 @@ float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, flo
     k_cell_scan<<<P.nt, 1024, 0, s>>>(C.tbase, C.cnt, C.start, C.cursor);
     k_cell_fill<<<nblk(P.nb, 256), 256, 0, s>>>(P.nb, B.traj, B.off, C.key, B.flags, C.cursor, C.cell_bead,
                                                  B.frame_in, C.cell_pos);
-    k_cell_sort<<<dim3(P.nt, (C.max_buckets + 127) / 128), 128, 0, s>>>(B.off, C.tbase, C.tmask, C.start, C.cnt,
-                                                                        C.cell_bead, C.cell_pos);
+    if (ordered)
+        k_cell_sort<<<dim3(P.nt, (C.max_buckets + 127) / 128), 128, 0, s>>>(B.off, C.tbase, C.tmask, C.start, C.cnt,
+                                                                            C.cell_bead, C.cell_pos);
     return inv;
 }
 
 void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffers &C, const int2 *work, int nwork,
                           cudaStream_t s) {
     const float reach = fmaxf(P.lj_on ? P.ljcut : 0.f, P.is_assembly ? kPairReach : 0.f);
-    const float inv = bin_beads(P, B, C, reach, s);
+    const float inv = bin_beads(P, B, C, reach, false, s);   // the lists are sorted afterwards
     k_cell_lists<<<nwork, kTile, 0, s>>>(P, B, work, C.tbase, C.tmask, C.start, C.cnt, C.cell_pos, inv);
 }
 

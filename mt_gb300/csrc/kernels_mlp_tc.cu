@@ -184,14 +184,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(const Weights W,
     const uint32_t bw[4] = {smem_u32(S.w1), smem_u32(S.w2), smem_u32(S.w3), smem_u32(S.w4)};
     uint32_t phase = 0;
     const int ntiles = (n + kTcRows - 1) / kTcRows;
+    // inputs: 128 rows x 32 features = 8 float4 per thread, coalesced; the
+    // next tile's are loaded while the current one runs
+    constexpr int kXv = kTcRows * (kIn / 4) / kTcThreads;
+    float4 xv[kXv];
+    auto load_x = [&](int tile) {
+#pragma unroll
+        for (int u = 0; u < kXv; u++) {
+            const int i = tid + u * kTcThreads, r = i / (kIn / 4), c = (i % (kIn / 4)) * 4;
+            const int gr = tile * kTcRows + r;
+            xv[u] = (tile < ntiles && gr < n) ? *reinterpret_cast<const float4 *>(X + (size_t)gr * kIn + c)
+                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    load_x(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int row0 = tile * kTcRows;
-        // inputs: 128 rows x 32 features, coalesced float4 loads, normalised, BF16
-        for (int i = tid; i < kTcRows * (kIn / 4); i += blockDim.x) {
-            const int r = i / (kIn / 4), c = (i % (kIn / 4)) * 4;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < kXv; u++) {
+            const int i = tid + u * kTcThreads, r = i / (kIn / 4), c = (i % (kIn / 4)) * 4;
+            float4 v = xv[u];
             if (row0 + r < n) {
-                v = *reinterpret_cast<const float4 *>(X + (size_t)(row0 + r) * kIn + c);
                 v.x = (v.x - S.nrm[c]) * S.nrm[kIn + c];
                 v.y = (v.y - S.nrm[c + 1]) * S.nrm[kIn + c + 1];
                 v.z = (v.z - S.nrm[c + 2]) * S.nrm[kIn + c + 2];
@@ -200,6 +213,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(const Weights W,
             *reinterpret_cast<uint2 *>(reinterpret_cast<char *>(S.x) + core_off(r, c, kIn)) =
                 make_uint2(pack_bf16(v.x, v.y), pack_bf16(v.z, v.w));
         }
+        load_x(tile + gridDim.x);
         bool ok = true;
         for (int layer = 0; layer < 4 && ok; layer++) {
             fence_async_smem();

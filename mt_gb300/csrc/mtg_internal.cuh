@@ -227,7 +227,10 @@ void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffe
                           cudaStream_t s);
 // Bins the current positions into the per-trajectory spatial hash with cells
 // just larger than `reach`; returns 1/edge for the consumers' cell lookups.
-float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, float reach, cudaStream_t s);
+// `ordered` sorts every bucket by bead index (for sums that must not depend
+// on the arrival order of the atomic fill).
+float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, float reach, bool ordered,
+                cudaStream_t s);
 void launch_step_plain(const KParams &P, const DevBuffers &B, bool keep_forces, cudaStream_t s);
 void launch_forces(const KParams &P, const DevBuffers &B, bool tea_prepare, cudaStream_t s);
 void launch_energy(const KParams &P, const DevBuffers &B, double *per_bead, double *partials,

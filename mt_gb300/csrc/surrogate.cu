@@ -108,36 +108,43 @@ __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, 
         const int cx = cell_coord(pi.x, inv_cell), cy = cell_coord(pi.y, inv_cell), cz = cell_coord(pi.z, inv_cell);
         const int tb = C.tbase[traj];
         const uint32_t mask = (uint32_t)C.tmask[traj];
-        int bk[27], st[27], ct[27];
+        int bk[27];
 #pragma unroll
         for (int c = 0; c < 27; c++)
             bk[c] = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
+        int st_next = C.start[bk[0]], ct_next = C.cnt[bk[0]];
 #pragma unroll
         for (int c = 0; c < 27; c++) {
-            st[c] = C.start[bk[c]];
-            ct[c] = C.cnt[bk[c]];
-        }
-#pragma unroll
-        for (int c = 0; c < 27; c++) {
+            const int st_c = st_next, ct_c = ct_next;
+            if (c + 1 < 27) {   // the next cell's range is fetched while this one runs
+                st_next = C.start[bk[c + 1]];
+                ct_next = C.cnt[bk[c + 1]];
+            }
             bool seen = false;   // two cells hashed to one bucket: visit it once
 #pragma unroll
             for (int v = 0; v < c; v++) seen |= (bk[v] == bk[c]);
-            if (seen || ct[c] == 0) continue;
-            const int s1e = base + st[c] + ct[c];
-            for (int s = base + st[c]; s < s1e; s++) {
-                const float4 q = C.cell_pos[s];
-                const int wj = __float_as_int(q.w);
-                const float ex = q.x - pi.x, ey = q.y - pi.y, ez = q.z - pi.z;
-                const float r2 = ex * ex + ey * ey + ez * ez;
-                if (!(r2 < kDescCut * kDescCut) || !(r2 > 0.f) || (wj & kCellExtraBit) || wj == g) continue;
-                const float rinv = rsqrtf(r2), r = r2 * rinv;
-                const float ux = ex * rinv, uy = ey * rinv, uz = ez * rinv;
-                if (r < 5.0f)
-                    desc_add(s0, rinv, ux, uy, uz);
-                else if (r < 10.0f)
-                    desc_add(s1, rinv, ux, uy, uz);
-                else
-                    desc_add(s2, rinv, ux, uy, uz);
+            if (seen || ct_c == 0) continue;
+            const int s1e = base + st_c + ct_c;
+            for (int s = base + st_c; s < s1e; s += 4) {
+                float4 q[4];   // four candidates in flight
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    q[u] = s + u < s1e ? C.cell_pos[s + u] : make_float4(0.f, 0.f, 0.f, __int_as_float(kCellExtraBit));
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int wj = __float_as_int(q[u].w);
+                    const float ex = q[u].x - pi.x, ey = q[u].y - pi.y, ez = q[u].z - pi.z;
+                    const float r2 = ex * ex + ey * ey + ez * ez;
+                    if (!(r2 < kDescCut * kDescCut) || !(r2 > 0.f) || (wj & kCellExtraBit) || wj == g) continue;
+                    const float rinv = rsqrtf(r2), r = r2 * rinv;
+                    const float ux = ex * rinv, uy = ey * rinv, uz = ez * rinv;
+                    if (r < 5.0f)
+                        desc_add(s0, rinv, ux, uy, uz);
+                    else if (r < 10.0f)
+                        desc_add(s1, rinv, ux, uy, uz);
+                    else
+                        desc_add(s2, rinv, ux, uy, uz);
+                }
             }
         }
         const float4 ts = stats[traj];
@@ -579,7 +586,7 @@ int mtg_tea_training_data(mtg_engine *e, float *X, float *T) {
     if (rc) return rc;
     const DevBuffers B = e->bufs();
     k_traj_stats<<<e->nt, 256, 0, e->stream>>>(e->kp, B, e->surr_stats);
-    const float inv = bin_beads(e->kp, B, e->cells(), kDescCut, e->stream);
+    const float inv = bin_beads(e->kp, B, e->cells(), kDescCut, true, e->stream);
     k_descriptors<<<e->nwork, kTile, 0, e->stream>>>(e->kp, B, e->cells(), e->work, inv, e->surr_stats, e->surr_desc,
                                                      nullptr);
     if (T) {
@@ -626,7 +633,7 @@ void enqueue_surrogate_eps(mtg_engine *e) {
     const DevBuffers B = e->bufs();
     const int *gate = e->surr_gate;
     k_traj_stats<<<e->nt, 256, 0, e->stream>>>(e->kp, B, e->surr_stats);
-    const float inv = bin_beads(e->kp, B, e->cells(), kDescCut, e->stream);
+    const float inv = bin_beads(e->kp, B, e->cells(), kDescCut, true, e->stream);
     k_descriptors<<<e->nwork, kTile, 0, e->stream>>>(e->kp, B, e->cells(), e->work, inv, e->surr_stats, e->surr_desc,
                                                      gate);
     mlp::launch_infer_tc(e->surr->W, e->surr_desc, e->nb, e->surr->norm, e->surr_pred, e->err, e->stream);
