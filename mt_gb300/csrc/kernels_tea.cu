@@ -3,59 +3,40 @@
 // RPY mobility product fused with the position update.
 //
 // Both O(N^2) kernels run one CTA per (trajectory, chunk of kTeaChunk beads)
-// and stream the trajectory through shared memory in tiles; each bead i is
-// served by `tea_slices` threads that take interleaved j of every tile, so
-// small batches still fill the GPU, and the partial sums meet in shared
-// memory.  Every thread reads the tile by broadcast, two beads j per load,
-// and works on them in packed FP32x2 arithmetic.  They are bound by the FP32
-// pipe (about 45 FLOP per ordered pair).
+// and stream the trajectory through shared memory in tiles of kTeaTile
+// beads j.  A thread serves kTeaNI beads i (lanes il, il + 32, ...) as packed
+// FP32x2 pairs; `tea_slices` threads share each bead i and take interleaved
+// j of every tile, so small batches still fill the GPU, and the partial sums
+// meet in shared memory.  The tile holds every value of bead j twice (both
+// lanes of a packed operand), so one broadcast 8-byte load feeds a packed
+// pair of beads i.  Away from the CTA's own beads the far-field formula runs
+// for every pair; the few overlapping pairs (r <= 2a) are found through the
+// running minimum of r^2 and corrected afterwards.  The tile that holds the
+// CTA's own beads (the self pairs) runs the scalar formula with both branches.
+// Sums are kept in units of 0.75 a (T' = T / (0.75 a)).  The kernels are
+// bound by the FP32 pipe (about 45 FLOP per ordered pair).
 #include "mtg_internal.cuh"
 
 namespace mtg {
 
-// 1/sqrt(x) as the single hardware approximation instruction (a few ulp);
-// pair distances are never subnormal, so the flush-to-zero form gives the
-// same value for them without a subnormal fix-up.
-__device__ __forceinline__ float rsqrt_hw(float x) {
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
+constexpr int kTeaNI = 4;                   // beads i per thread
+constexpr int kTeaPairsI = kTeaNI / 2;      // packed pairs of them
+constexpr int kTeaLanes = 32;               // threads per slice
+constexpr int kTeaI = kTeaChunk;            // beads i per CTA
+static_assert(kTeaI == kTeaLanes * kTeaNI, "chunk = lanes x beads per thread");
+constexpr int kTeaTile = 256;               // beads j per tile
+constexpr float kFarAway = 1.0e18f;         // position of padding and extra beads j
 
-// Normalised RPY block D_ij/D_ii (integrateTea_RPY, src/bdhitea_kernel.cu:38-58):
-// T = cii I + crr u u^T with ra = r/a; ra > 2: crr = 0.75/ra (1 - 2/ra^2),
-// cii = 0.75/ra (1 + 2/(3 ra^2)); otherwise crr = 3 ra/32, cii = 1 - 9 ra/32.
-// RPY coefficients from the squared distance (branch-free): cii, and
-// crr / r^2 so that T g = cii g + (crr / r^2) d (d . g) with d = r_j - r_i.
-__device__ __forceinline__ void rpy_pair(float r2, float a, float inv_a, float &cii, float &crr_r2, float &rinv) {
-    r2 = fmaxf(r2, 1e-6f);                  // coincident beads stay finite (masked by the caller)
-    rinv = rsqrt_hw(r2);
-    const float ra = r2 * rinv * inv_a;
-    const float ira = a * rinv, ira2 = ira * ira;
-    const float far_rr = 0.75f * ira * (1.0f - 2.0f * ira2);
-    const float far_ii = 0.75f * ira * (1.0f + (2.0f / 3.0f) * ira2);
-    const bool far = ra > 2.0f;
-    crr_r2 = (far ? far_rr : (3.0f / 32.0f) * ra) * rinv * rinv;
-    cii = far ? far_ii : 1.0f - (9.0f / 32.0f) * ra;
-}
-
-// Work split of the all-pairs TEA kernels: a CTA holds kTeaI beads i, each
-// served by `slices` threads that cover interleaved j of every tile; the
-// partial sums meet in shared memory.  slices = blockDim.x / kTeaI.
-constexpr int kTeaI = kTeaChunk;
-constexpr int kTeaTile = 256;
-
-// Shared-memory tile of the all-pairs kernels as a structure of arrays: one
-// 8-byte load gives the values of two consecutive beads j, which are the two
-// lanes of the packed FP32x2 arithmetic.  Beads past the trajectory's end and
-// extra beads get a far-away position (and zero F and R): every term they
-// give is zero or below the rounding of the sums, and every tile is full.
+// Tile of the all-pairs kernels, every value duplicated into both lanes.
+// Beads past the trajectory's end and extra beads sit far away with zero F
+// and R: every term they give is zero or below the rounding of the sums.
 struct TeaTile {
-    float x[kTeaTile], y[kTeaTile], z[kTeaTile];
-    float fx[kTeaTile], fy[kTeaTile], fz[kTeaTile];
-    float rx[kTeaTile], ry[kTeaTile], rz[kTeaTile];
+    float2 x[kTeaTile], y[kTeaTile], z[kTeaTile];
+    float2 fx[kTeaTile], fy[kTeaTile], fz[kTeaTile];
+    float2 rx[kTeaTile], ry[kTeaTile], rz[kTeaTile];
 };
-constexpr float kFarAway = 1.0e18f;
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 
 template <bool WITH_FR>
 __device__ __forceinline__ void tea_tile_load(TeaTile &T, const DevBuffers &B, int j0, int end) {
@@ -69,153 +50,184 @@ __device__ __forceinline__ void tea_tile_load(TeaTile &T, const DevBuffers &B, i
                 R = B.tea_r[jg];
             }
         }
-        T.x[k] = p.x;
-        T.y[k] = p.y;
-        T.z[k] = p.z;
+        T.x[k] = f2(p.x);
+        T.y[k] = f2(p.y);
+        T.z[k] = f2(p.z);
         if (WITH_FR) {
-            T.fx[k] = F.x;
-            T.fy[k] = F.y;
-            T.fz[k] = F.z;
-            T.rx[k] = R.x;
-            T.ry[k] = R.y;
-            T.rz[k] = R.z;
+            T.fx[k] = f2(F.x);
+            T.fy[k] = f2(F.y);
+            T.fz[k] = f2(F.z);
+            T.rx[k] = f2(R.x);
+            T.ry[k] = f2(R.y);
+            T.rz[k] = f2(R.z);
         }
     }
 }
 
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 ld2(const float *a, int m) { return reinterpret_cast<const float2 *>(a)[m]; }
+// Scaled RPY coefficients (integrateTea_RPY, src/bdhitea_kernel.cu:38-58:
+// T = cii I + crr u u^T, ra = r/a; ra > 2: cii = 0.75/ra (1 + 2/(3 ra^2)),
+// crr = 0.75/ra (1 - 2/ra^2); otherwise cii = 1 - 9 ra/32, crr = 3 ra/32),
+// divided by 0.75 a.  With rinv = 1/r, q = rinv^2, t = q rinv the far field
+// is cii' = rinv + (2/3) a^2 t and crr' = rinv - 2 a^2 t.
+struct TeaConst {
+    float kap, two_a2, four_a2, inv_a, inv_c075a, c075a;
+};
+__device__ __forceinline__ TeaConst tea_const(float a) {
+    return {(2.0f / 3.0f) * a * a, 2.0f * a * a, 4.0f * a * a, 1.0f / a, 1.0f / (0.75f * a), 0.75f * a};
+}
+// near branch (r <= 2a): scaled cii', crr'
+__device__ __forceinline__ void rpy_near(const TeaConst &K, float r2, float rinv, float &cii, float &crr) {
+    const float ra = r2 * rinv * K.inv_a;
+    cii = (1.0f - (9.0f / 32.0f) * ra) * K.inv_c075a;
+    crr = (3.0f / 32.0f) * ra * K.inv_c075a;
+}
 
-// The epsilon-pass terms of one pair from its coefficients: the row sums of
-// squares minus cii^2 (Bc d_c^2 with Bc = (2 cii + crr) crr / r^2), cii^2,
-// and the sum of all nine entries 3 cii + crr/r^2 (d_x + d_y + d_z)^2.
+// ------------------------------------------------------------ epsilon pass
+// Scaled epsilon terms of one pair from cii', crr', q: the row sums of
+// squares minus cii'^2 (Bc d_c^2 with Bc = (2 cii' + crr') crr' q), cii'^2, and
+// the sum of all nine entries 3 cii' + crr' q (d_x + d_y + d_z)^2.
 struct EpsTerms {
     float bx, by, bz, a2, w;
 };
 __device__ __forceinline__ EpsTerms eps_terms(float dx, float dy, float dz, float cii, float crr, float q) {
-    const float bc = fmaf(2.0f, cii, crr) * crr * q;
+    const float crq = crr * q;
+    const float bc = fmaf(2.0f, cii, crr) * crq;
     const float us = dx + dy + dz;
-    return {bc * dx * dx, bc * dy * dy, bc * dz * dz, cii * cii, fmaf(crr * q, us * us, 3.0f * cii)};
+    return {bc * dx * dx, bc * dy * dy, bc * dz * dz, cii * cii, fmaf(crq * us, us, 3.0f * cii)};
 }
 
 // integrateTea_epsilon_unlisted (src/bdhitea_kernel.cu:84-101): per bead i,
 // sum over non-extra j != i of the row sums of squared entries (-> tea_ci)
 // and of all nine entries (-> tea_eps).  With T = cii I + crr u u^T the row
 // sums of squares are cii^2 + (2 cii + crr) crr u_c^2 and the sum of all
-// entries is 3 cii + crr (u_x + u_y + u_z)^2.  Two beads i per thread and,
-// away from the CTA's own beads, packed over pairs of j with the far-field
-// coefficients (cii = 0.75 a/r + 0.5 a^3/r^3, crr = 0.75 a/r - 1.5 a^3/r^3);
-// overlapping pairs (r <= 2a) are corrected afterwards, as in k_tea_step.
+// entries is 3 cii + crr (u_x + u_y + u_z)^2.
 template <int SLICES>
-__global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work,
-                                                                 const int *gate, int run_if) {
+__global__ void __launch_bounds__(kTeaLanes *SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work,
+                                                                const int *gate, int run_if) {
     if (gate && *gate != run_if) return;
-    constexpr int kHalf = kTeaI / 2;
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
-    const int il = threadIdx.x % kHalf, sl = threadIdx.x / kHalf;
+    const int il = threadIdx.x % kTeaLanes, sl = threadIdx.x / kTeaLanes;
     __shared__ TeaTile T;
     __shared__ float4 s_red[kTeaI * SLICES];
-    int gi[2];
-    bool act[2];
-    float4 pi[2];
-    float2 nx[2], ny[2], nz[2], sx[2], sy[2], sz[2], sa[2], sw[2];
+    int gi[kTeaNI];
+    bool act[kTeaNI];
+    float4 pi[kTeaNI];
+    float2 nx[kTeaPairsI], ny[kTeaPairsI], nz[kTeaPairsI];
+    float2 sx[kTeaPairsI], sy[kTeaPairsI], sz[kTeaPairsI], sa[kTeaPairsI], sw[kTeaPairsI];
+    bool any_act = false;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        gi[h] = w.y + il + h * kHalf;
+    for (int h = 0; h < kTeaNI; h++) {
+        gi[h] = w.y + il + h * kTeaLanes;
         act[h] = false;
         pi[h] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (gi[h] < end) {
             pi[h] = B.frame_in[gi[h]];
             act[h] = (B.flags[gi[h]] & kFlagExtra) == 0;
         }
-        nx[h] = f2(-pi[h].x);
-        ny[h] = f2(-pi[h].y);
-        nz[h] = f2(-pi[h].z);
-        sx[h] = sy[h] = sz[h] = sa[h] = sw[h] = f2(0.f);
+        any_act |= act[h];
     }
-    const float a = P.tea_a, inv_a = 1.0f / P.tea_a;
-    const float c075a = 0.75f * a, c05a3 = 0.5f * a * a * a, c15a3 = 1.5f * a * a * a, four_a2 = 4.0f * a * a;
-    const float2 v075a = f2(c075a), v05a3 = f2(c05a3), vn15a3 = f2(-c15a3), two = f2(2.0f), three = f2(3.0f);
-    const bool any_act = act[0] || act[1];
+#pragma unroll
+    for (int p = 0; p < kTeaPairsI; p++) {
+        nx[p] = make_float2(-pi[2 * p].x, -pi[2 * p + 1].x);
+        ny[p] = make_float2(-pi[2 * p].y, -pi[2 * p + 1].y);
+        nz[p] = make_float2(-pi[2 * p].z, -pi[2 * p + 1].z);
+        sx[p] = sy[p] = sz[p] = sa[p] = sw[p] = f2(0.f);
+    }
+    const TeaConst K = tea_const(P.tea_a);
+    const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), two = f2(2.0f), three = f2(3.0f);
     for (int j0 = base; j0 < end; j0 += kTeaTile) {
         tea_tile_load<false>(T, B, j0, end);
         __syncthreads();
         if (any_act) {
             const bool self_tile = (w.y < j0 + kTeaTile) && (w.y + kTeaI > j0);
             if (!self_tile) {
-                float rmin[2] = {3.4e38f, 3.4e38f};
-#pragma unroll 2
-                for (int m = sl; m < kTeaTile / 2; m += SLICES) {
-                    const float2 xj = ld2(T.x, m), yj = ld2(T.y, m), zj = ld2(T.z, m);
+                float rmin[kTeaPairsI];
 #pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        const float2 dx = __fadd2_rn(xj, nx[h]), dy = __fadd2_rn(yj, ny[h]),
-                                     dz = __fadd2_rn(zj, nz[h]);
+                for (int p = 0; p < kTeaPairsI; p++) rmin[p] = 3.4e38f;
+#pragma unroll 2
+                for (int t = sl; t < kTeaTile; t += SLICES) {
+                    const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+#pragma unroll
+                    for (int p = 0; p < kTeaPairsI; p++) {
+                        const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]),
+                                     dz = __fadd2_rn(zj, nz[p]);
                         const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-                        rmin[h] = fminf(rmin[h], fminf(r2.x, r2.y));
+                        rmin[p] = fminf(rmin[p], fminf(r2.x, r2.y));
                         const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
                         const float2 q = __fmul2_rn(rinv, rinv);
-                        const float2 t = __fmul2_rn(q, rinv);
-                        const float2 ar = __fmul2_rn(v075a, rinv);
-                        const float2 cii = __ffma2_rn(v05a3, t, ar);
-                        const float2 crr = __ffma2_rn(vn15a3, t, ar);
+                        const float2 tq = __fmul2_rn(q, rinv);
+                        const float2 cii = __ffma2_rn(vkap, tq, rinv);
+                        const float2 crr = __ffma2_rn(vn2a2, tq, rinv);
                         const float2 crq = __fmul2_rn(crr, q);
                         const float2 bc = __fmul2_rn(__ffma2_rn(two, cii, crr), crq);
-                        sa[h] = __ffma2_rn(cii, cii, sa[h]);
-                        sx[h] = __ffma2_rn(__fmul2_rn(bc, dx), dx, sx[h]);
-                        sy[h] = __ffma2_rn(__fmul2_rn(bc, dy), dy, sy[h]);
-                        sz[h] = __ffma2_rn(__fmul2_rn(bc, dz), dz, sz[h]);
+                        sa[p] = __ffma2_rn(cii, cii, sa[p]);
+                        sx[p] = __ffma2_rn(__fmul2_rn(bc, dx), dx, sx[p]);
+                        sy[p] = __ffma2_rn(__fmul2_rn(bc, dy), dy, sy[p]);
+                        sz[p] = __ffma2_rn(__fmul2_rn(bc, dz), dz, sz[p]);
                         const float2 us = __fadd2_rn(__fadd2_rn(dx, dy), dz);
-                        sw[h] = __ffma2_rn(__fmul2_rn(crq, us), us, __ffma2_rn(three, cii, sw[h]));
+                        sw[p] = __ffma2_rn(__fmul2_rn(crq, us), us, __ffma2_rn(three, cii, sw[p]));
                     }
                 }
                 // overlapping pairs (r <= 2a): replace the far-field terms by the near ones
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    if (!(rmin[h] <= four_a2)) continue;
-                    for (int m = sl; m < kTeaTile / 2; m += SLICES) {
+                for (int p = 0; p < kTeaPairsI; p++) {
+                    if (!(rmin[p] <= K.four_a2)) continue;
+                    for (int t = sl; t < kTeaTile; t += SLICES) {
 #pragma unroll
                         for (int e = 0; e < 2; e++) {
-                            const int t = 2 * m + e;
-                            const float dx = T.x[t] + nx[h].x, dy = T.y[t] + ny[h].x, dz = T.z[t] + nz[h].x;
+                            const float ax = e ? nx[p].y : nx[p].x, ay = e ? ny[p].y : ny[p].x,
+                                        az = e ? nz[p].y : nz[p].x;
+                            const float dx = T.x[t].x + ax, dy = T.y[t].x + ay, dz = T.z[t].x + az;
                             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                            if (!(r2 <= four_a2)) continue;
-                            const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv, ar = c075a * rinv;
-                            const EpsTerms f = eps_terms(dx, dy, dz, fmaf(c05a3, tq, ar), fmaf(-c15a3, tq, ar), q);
-                            const float ra = r2 * rinv * inv_a;
-                            const EpsTerms n =
-                                eps_terms(dx, dy, dz, 1.0f - (9.0f / 32.0f) * ra, (3.0f / 32.0f) * ra, q);
-                            sx[h].x += n.bx - f.bx;
-                            sy[h].x += n.by - f.by;
-                            sz[h].x += n.bz - f.bz;
-                            sa[h].x += n.a2 - f.a2;
-                            sw[h].x += n.w - f.w;
+                            if (!(r2 <= K.four_a2)) continue;
+                            const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
+                            const EpsTerms f = eps_terms(dx, dy, dz, fmaf(K.kap, tq, rinv), fmaf(-K.two_a2, tq, rinv), q);
+                            float cn, rn;
+                            rpy_near(K, r2, rinv, cn, rn);
+                            const EpsTerms n = eps_terms(dx, dy, dz, cn, rn, q);
+                            float2 *tx = &sx[p], *ty = &sy[p], *tz = &sz[p], *ta = &sa[p], *tw = &sw[p];
+                            if (e) {
+                                tx->y += n.bx - f.bx;
+                                ty->y += n.by - f.by;
+                                tz->y += n.bz - f.bz;
+                                ta->y += n.a2 - f.a2;
+                                tw->y += n.w - f.w;
+                            } else {
+                                tx->x += n.bx - f.bx;
+                                ty->x += n.by - f.by;
+                                tz->x += n.bz - f.bz;
+                                ta->x += n.a2 - f.a2;
+                                tw->x += n.w - f.w;
+                            }
                         }
                     }
                 }
             } else {
                 for (int t = sl; t < kTeaTile; t += SLICES) {
 #pragma unroll
-                    for (int h = 0; h < 2; h++) {
+                    for (int h = 0; h < kTeaNI; h++) {
                         if (j0 + t == gi[h]) continue;
-                        const float dx = T.x[t] - pi[h].x, dy = T.y[t] - pi[h].y, dz = T.z[t] - pi[h].z;
+                        const float dx = T.x[t].x - pi[h].x, dy = T.y[t].x - pi[h].y, dz = T.z[t].x - pi[h].z;
                         const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1e-6f);
-                        const float rinv = rsqrt_hw(r2);
-                        const float q = rinv * rinv;
-                        float cii = rinv * fmaf(c05a3, q, c075a);
-                        float crr = rinv * fmaf(-c15a3, q, c075a);
-                        if (r2 <= four_a2) {
-                            const float ra = r2 * rinv * inv_a;
-                            cii = 1.0f - (9.0f / 32.0f) * ra;
-                            crr = (3.0f / 32.0f) * ra;
-                        }
+                        const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
+                        float cii = fmaf(K.kap, tq, rinv), crr = fmaf(-K.two_a2, tq, rinv);
+                        if (r2 <= K.four_a2) rpy_near(K, r2, rinv, cii, crr);
                         const EpsTerms n = eps_terms(dx, dy, dz, cii, crr, q);
-                        sx[h].x += n.bx;
-                        sy[h].x += n.by;
-                        sz[h].x += n.bz;
-                        sa[h].x += n.a2;
-                        sw[h].x += n.w;
+                        const int p = h >> 1;
+                        if (h & 1) {
+                            sx[p].y += n.bx;
+                            sy[p].y += n.by;
+                            sz[p].y += n.bz;
+                            sa[p].y += n.a2;
+                            sw[p].y += n.w;
+                        } else {
+                            sx[p].x += n.bx;
+                            sy[p].x += n.by;
+                            sz[p].x += n.bz;
+                            sa[p].x += n.a2;
+                            sw[p].x += n.w;
+                        }
                     }
                 }
             }
@@ -223,27 +235,31 @@ __global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_eps(KParams P, DevBu
         __syncthreads();
     }
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const float A = sa[h].x + sa[h].y;
-        s_red[(sl * 2 + h) * kHalf + il] =
-            make_float4(sx[h].x + sx[h].y + A, sy[h].x + sy[h].y + A, sz[h].x + sz[h].y + A, sw[h].x + sw[h].y);
+    for (int h = 0; h < kTeaNI; h++) {
+        const int p = h >> 1;
+        const bool hi = h & 1;
+        const float A = hi ? sa[p].y : sa[p].x;
+        s_red[(sl * kTeaNI + h) * kTeaLanes + il] =
+            make_float4((hi ? sx[p].y : sx[p].x) + A, (hi ? sy[p].y : sy[p].x) + A, (hi ? sz[p].y : sz[p].x) + A,
+                        hi ? sw[p].y : sw[p].x);
     }
     __syncthreads();
     if (sl != 0) return;
+    const float c2 = K.c075a * K.c075a;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < kTeaNI; h++) {
         if (gi[h] >= end) continue;
-        float4 acc = s_red[h * kHalf + il];
+        float4 acc = s_red[h * kTeaLanes + il];
         for (int k = 1; k < SLICES; k++) {
-            const float4 v = s_red[(k * 2 + h) * kHalf + il];
+            const float4 v = s_red[(k * kTeaNI + h) * kTeaLanes + il];
             acc.x += v.x;
             acc.y += v.y;
             acc.z += v.z;
             acc.w += v.w;
         }
         if (!act[h]) acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        B.tea_ci[gi[h]] = make_float4(acc.x, acc.y, acc.z, 0.f);
-        B.tea_eps[gi[h]] = acc.w;
+        B.tea_ci[gi[h]] = make_float4(acc.x * c2, acc.y * c2, acc.z * c2, 0.f);
+        B.tea_eps[gi[h]] = acc.w * K.c075a;
     }
 }
 
@@ -303,197 +319,202 @@ __global__ void __launch_bounds__(256) k_tea_beta(KParams P, DevBuffers B, int c
     }
 }
 
-// One pair's contribution T_ij g to f, with d = r_j - r_i and r2 = |d|^2 > 0.
-// Far field (r > 2a, the common case): cii = 0.75 a/r (1 + 2a^2/(3r^2)),
-// crr/r^2 = 0.75 a/r^3 (1 - 2a^2/r^2), written in q = 1/r^2; the overlap
-// branch (r <= 2a) is rare and taken under a warp-divergent branch.
-__device__ __forceinline__ void tea_pair(float dx, float dy, float dz, float gx, float gy, float gz, float a,
-                                         float inv_a, float c075a, float c05a3, float c15a3, float four_a2,
-                                         float &fx, float &fy, float &fz) {
-    const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1e-6f);
-    const float rinv = rsqrt_hw(r2);
-    const float q = rinv * rinv;
-    float cii = rinv * fmaf(c05a3, q, c075a);
-    float crr_r2 = rinv * q * fmaf(-c15a3, q, c075a);
-    if (r2 <= four_a2) {
-        const float ra = r2 * rinv * inv_a;
-        cii = 1.0f - (9.0f / 32.0f) * ra;
-        crr_r2 = (3.0f / 32.0f) * ra * q;
-    }
-    const float s = crr_r2 * fmaf(dx, gx, fmaf(dy, gy, dz * gz));
-    fx = fmaf(cii, gx, fmaf(s, dx, fx));
-    fy = fmaf(cii, gy, fmaf(s, dy, fy));
-    fz = fmaf(cii, gz, fmaf(s, dz, fz));
-}
-
-// Far-field pair term for two beads j (the lanes) against one bead i, with
-// d = r_j - r_i, g = F_j + beta C_i o R_j and, in q = 1/r^2, t = q/r:
-// cii = 0.75 a/r + 0.5 a^3 t, crr/r^2 = t (0.75 a - 1.5 a^3 q); the running
-// minimum of r^2 flags the rare overlapping pairs (r <= 2a) for correction.
-__device__ __forceinline__ void tea_far2(float2 dx, float2 dy, float2 dz, float2 gx, float2 gy, float2 gz,
-                                         float2 c075a, float2 c05a3, float2 nc15a3, float2 &ax, float2 &ay,
-                                         float2 &az, float &rmin) {
-    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-    rmin = fminf(rmin, fminf(r2.x, r2.y));
-    const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-    const float2 q = __fmul2_rn(rinv, rinv);
-    const float2 t = __fmul2_rn(q, rinv);
-    const float2 cii = __ffma2_rn(c05a3, t, __fmul2_rn(c075a, rinv));
-    const float2 crr_r2 = __fmul2_rn(t, __ffma2_rn(nc15a3, q, c075a));
-    const float2 s = __fmul2_rn(crr_r2, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
-    ax = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax));
-    ay = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay));
-    az = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az));
-}
-
-// One lane of tea_far2 in scalar arithmetic (the same operations in the same
-// order, so the value is the one the packed lane added).
-__device__ __forceinline__ float3 tea_far1(float dx, float dy, float dz, float gx, float gy, float gz, float c075a,
-                                           float c05a3, float nc15a3) {
+// ------------------------------------------------------- mobility product
+// Scaled far-field term of one pair in scalar arithmetic, the operations of
+// one lane of the packed loop in the same order.
+__device__ __forceinline__ float3 tea_far1(const TeaConst &K, float dx, float dy, float dz, float gx, float gy,
+                                           float gz) {
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float rinv = rsqrt_hw(r2);
-    const float q = rinv * rinv, t = q * rinv;
-    const float cii = fmaf(c05a3, t, c075a * rinv);
-    const float crr_r2 = t * fmaf(nc15a3, q, c075a);
-    const float s = crr_r2 * fmaf(dx, gx, fmaf(dy, gy, dz * gz));
+    const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
+    const float cii = fmaf(K.kap, tq, rinv);
+    const float cr = tq * fmaf(-K.two_a2, q, 1.0f);
+    const float s = cr * fmaf(dx, gx, fmaf(dy, gy, dz * gz));
+    return make_float3(fmaf(cii, gx, s * dx), fmaf(cii, gy, s * dy), fmaf(cii, gz, s * dz));
+}
+// Scaled term of one pair with both branches (r2 > 0).
+__device__ __forceinline__ float3 tea_pair1(const TeaConst &K, float dx, float dy, float dz, float gx, float gy,
+                                            float gz) {
+    const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1e-6f);
+    const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
+    float cii = fmaf(K.kap, tq, rinv);
+    float cr = tq * fmaf(-K.two_a2, q, 1.0f);
+    if (r2 <= K.four_a2) {
+        float crr;
+        rpy_near(K, r2, rinv, cii, crr);
+        cr = crr * q;
+    }
+    const float s = cr * fmaf(dx, gx, fmaf(dy, gy, dz * gz));
     return make_float3(fmaf(cii, gx, s * dx), fmaf(cii, gy, s * dy), fmaf(cii, gz, s * dz));
 }
 
 // integrateTea_kernel_unlisted + integrateTea_force (src/bdhitea_kernel.cu:104-213):
 // f_i = F_i + C_i o R_i + sum_{j != i, non-extra} T_ij (F_j + beta C_i o R_j),
 // x_i += dt/gammaR f_i; angles by Euler-Maruyama from stream i + nb, which is
-// drawn for every bead.  Reads the current frame, writes the next one.
-// Each thread serves two beads i (il and il + kTeaI/2); slice sl takes the
-// j-pairs sl, sl + SLICES, ... of every tile.  Tiles that do not hold the
-// CTA's own beads run packed over pairs of j with the far-field formula and
-// correct the few overlapping pairs afterwards; the tile with the self pairs
-// runs the scalar formula with both branches.
+// drawn for every bead.  Reads the current frame, writes the next one.  With
+// FEFF the kernel stores f_i instead and moves nothing.
 template <int SLICES, bool FEFF>
-__global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work,
-                                                                  float4 *feff, const int *gate) {
+__global__ void __launch_bounds__(kTeaLanes *SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work,
+                                                                 float4 *feff, const int *gate) {
     if (FEFF && gate && *gate != 0) return;
-    constexpr int kHalf = kTeaI / 2;
     const int2 w = work[blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
-    const int il = threadIdx.x % kHalf, sl = threadIdx.x / kHalf;
+    const int il = threadIdx.x % kTeaLanes, sl = threadIdx.x / kTeaLanes;
     const int nb = P.nb;
     __shared__ TeaTile T;
     __shared__ float4 s_red[kTeaI * SLICES];
 
-    int gi[2];
-    bool act[2];
-    float4 pi[2];
-    float2 ax[2], ay[2], az[2], nx[2], ny[2], nz[2], cbx[2], cby[2], cbz[2];
+    // per packed pair p of beads i (2p, 2p+1): -position, beta C_i, sums
+    float2 nx[kTeaPairsI], ny[kTeaPairsI], nz[kTeaPairsI], cbx[kTeaPairsI], cby[kTeaPairsI], cbz[kTeaPairsI];
+    float2 ax[kTeaPairsI], ay[kTeaPairsI], az[kTeaPairsI];
+    bool any_act = false;
     const float beta = B.tea_beta[traj], b2 = beta * beta;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        gi[h] = w.y + il + h * kHalf;
-        pi[h] = make_float4(0.f, 0.f, 0.f, 0.f);
-        ax[h] = ay[h] = az[h] = f2(0.f);
-        float cx = 0.f, cy = 0.f, cz = 0.f;
-        act[h] = false;
-        if (gi[h] < end) {
-            pi[h] = B.frame_in[gi[h]];
-            act[h] = (B.flags[gi[h]] & kFlagExtra) == 0;
-            const float4 ci = B.tea_ci[gi[h]];
-            cx = 1.0f / sqrtf(1.0f + b2 * ci.x);
-            cy = 1.0f / sqrtf(1.0f + b2 * ci.y);
-            cz = 1.0f / sqrtf(1.0f + b2 * ci.z);
-            if (sl == 0) {
-                const float4 Fi = B.force[gi[h]], Ri = B.tea_r[gi[h]];
-                ax[h].x = Fi.x + Ri.x * cx;
-                ay[h].x = Fi.y + Ri.y * cy;
-                az[h].x = Fi.z + Ri.z * cz;
-            }
+    for (int h = 0; h < kTeaNI; h++) {
+        const int g = w.y + il + h * kTeaLanes;
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f), c = p;
+        if (g < end) {
+            p = B.frame_in[g];
+            any_act |= (B.flags[g] & kFlagExtra) == 0;
+            const float4 ci = B.tea_ci[g];
+            c = make_float4(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
+                            beta / sqrtf(1.0f + b2 * ci.z), 0.f);
         }
-        nx[h] = f2(-pi[h].x);
-        ny[h] = f2(-pi[h].y);
-        nz[h] = f2(-pi[h].z);
-        cbx[h] = f2(cx * beta);
-        cby[h] = f2(cy * beta);
-        cbz[h] = f2(cz * beta);
+        float2 *v[6] = {&nx[h >> 1], &ny[h >> 1], &nz[h >> 1], &cbx[h >> 1], &cby[h >> 1], &cbz[h >> 1]};
+        const float val[6] = {-p.x, -p.y, -p.z, c.x, c.y, c.z};
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            if (h & 1)
+                v[k]->y = val[k];
+            else
+                v[k]->x = val[k];
+        }
     }
-    const float a = P.tea_a, inv_a = 1.0f / P.tea_a;
-    const float c075a = 0.75f * a, c05a3 = 0.5f * a * a * a, c15a3 = 1.5f * a * a * a, four_a2 = 4.0f * a * a;
-    const float2 v075a = f2(c075a), v05a3 = f2(c05a3), vn15a3 = f2(-c15a3);
-    const bool any_act = act[0] || act[1];
+#pragma unroll
+    for (int p = 0; p < kTeaPairsI; p++) ax[p] = ay[p] = az[p] = f2(0.f);
+    const TeaConst K = tea_const(P.tea_a);
+    const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
     for (int j0 = base; j0 < end; j0 += kTeaTile) {
         tea_tile_load<true>(T, B, j0, end);
         __syncthreads();
         if (any_act) {
             const bool self_tile = (w.y < j0 + kTeaTile) && (w.y + kTeaI > j0);
             if (!self_tile) {
-                float rmin[2] = {3.4e38f, 3.4e38f};
-#pragma unroll 2
-                for (int m = sl; m < kTeaTile / 2; m += SLICES) {
-                    const float2 xj = ld2(T.x, m), yj = ld2(T.y, m), zj = ld2(T.z, m);
-                    const float2 fxj = ld2(T.fx, m), fyj = ld2(T.fy, m), fzj = ld2(T.fz, m);
-                    const float2 rxj = ld2(T.rx, m), ryj = ld2(T.ry, m), rzj = ld2(T.rz, m);
+                float rmin[kTeaPairsI];
 #pragma unroll
-                    for (int h = 0; h < 2; h++)
-                        tea_far2(__fadd2_rn(xj, nx[h]), __fadd2_rn(yj, ny[h]), __fadd2_rn(zj, nz[h]),
-                                 __ffma2_rn(rxj, cbx[h], fxj), __ffma2_rn(ryj, cby[h], fyj),
-                                 __ffma2_rn(rzj, cbz[h], fzj), v075a, v05a3, vn15a3, ax[h], ay[h], az[h], rmin[h]);
+                for (int p = 0; p < kTeaPairsI; p++) rmin[p] = 3.4e38f;
+#pragma unroll 2
+                for (int t = sl; t < kTeaTile; t += SLICES) {
+                    const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+                    const float2 fxj = T.fx[t], fyj = T.fy[t], fzj = T.fz[t];
+                    const float2 rxj = T.rx[t], ryj = T.ry[t], rzj = T.rz[t];
+#pragma unroll
+                    for (int p = 0; p < kTeaPairsI; p++) {
+                        const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]),
+                                     dz = __fadd2_rn(zj, nz[p]);
+                        const float2 gx = __ffma2_rn(rxj, cbx[p], fxj), gy = __ffma2_rn(ryj, cby[p], fyj),
+                                     gz = __ffma2_rn(rzj, cbz[p], fzj);
+                        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                        rmin[p] = fminf(rmin[p], fminf(r2.x, r2.y));
+                        const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+                        const float2 q = __fmul2_rn(rinv, rinv);
+                        const float2 tq = __fmul2_rn(q, rinv);
+                        const float2 cii = __ffma2_rn(vkap, tq, rinv);
+                        const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
+                        const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
+                        ax[p] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax[p]));
+                        ay[p] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay[p]));
+                        az[p] = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az[p]));
+                    }
                 }
                 // overlapping pairs (r <= 2a): replace the far-field term by the near one
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    if (!(rmin[h] <= four_a2)) continue;
-                    for (int m = sl; m < kTeaTile / 2; m += SLICES) {
+                for (int p = 0; p < kTeaPairsI; p++) {
+                    if (!(rmin[p] <= K.four_a2)) continue;
+                    for (int t = sl; t < kTeaTile; t += SLICES) {
 #pragma unroll
                         for (int e = 0; e < 2; e++) {
-                            const int t = 2 * m + e;
-                            const float dx = T.x[t] + nx[h].x, dy = T.y[t] + ny[h].x, dz = T.z[t] + nz[h].x;
+                            const float dx = T.x[t].x + (e ? nx[p].y : nx[p].x),
+                                        dy = T.y[t].x + (e ? ny[p].y : ny[p].x),
+                                        dz = T.z[t].x + (e ? nz[p].y : nz[p].x);
                             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                            if (!(r2 <= four_a2)) continue;
-                            const float gx = fmaf(T.rx[t], cbx[h].x, T.fx[t]), gy = fmaf(T.ry[t], cby[h].x, T.fy[t]),
-                                        gz = fmaf(T.rz[t], cbz[h].x, T.fz[t]);
-                            const float3 far = tea_far1(dx, dy, dz, gx, gy, gz, c075a, c05a3, -c15a3);
-                            float nfx = 0.f, nfy = 0.f, nfz = 0.f;
-                            tea_pair(dx, dy, dz, gx, gy, gz, a, inv_a, c075a, c05a3, c15a3, four_a2, nfx, nfy, nfz);
-                            ax[h].x += nfx - far.x;
-                            ay[h].x += nfy - far.y;
-                            az[h].x += nfz - far.z;
+                            if (!(r2 <= K.four_a2)) continue;
+                            const float gx = fmaf(T.rx[t].x, e ? cbx[p].y : cbx[p].x, T.fx[t].x),
+                                        gy = fmaf(T.ry[t].x, e ? cby[p].y : cby[p].x, T.fy[t].x),
+                                        gz = fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fz[t].x);
+                            const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+                            const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
+                            if (e) {
+                                ax[p].y += nr.x - fa.x;
+                                ay[p].y += nr.y - fa.y;
+                                az[p].y += nr.z - fa.z;
+                            } else {
+                                ax[p].x += nr.x - fa.x;
+                                ay[p].x += nr.y - fa.y;
+                                az[p].x += nr.z - fa.z;
+                            }
                         }
                     }
                 }
             } else {
                 for (int t = sl; t < kTeaTile; t += SLICES) {
 #pragma unroll
-                    for (int h = 0; h < 2; h++)
-                        if (j0 + t != gi[h])
-                            tea_pair(T.x[t] - pi[h].x, T.y[t] - pi[h].y, T.z[t] - pi[h].z,
-                                     fmaf(T.rx[t], cbx[h].x, T.fx[t]), fmaf(T.ry[t], cby[h].x, T.fy[t]),
-                                     fmaf(T.rz[t], cbz[h].x, T.fz[t]), a, inv_a, c075a, c05a3, c15a3, four_a2,
-                                     ax[h].x, ay[h].x, az[h].x);
+                    for (int h = 0; h < kTeaNI; h++) {
+                        if (j0 + t == w.y + il + h * kTeaLanes) continue;
+                        const int p = h >> 1;
+                        const bool e = h & 1;
+                        const float3 c = tea_pair1(K, T.x[t].x + (e ? nx[p].y : nx[p].x),
+                                                   T.y[t].x + (e ? ny[p].y : ny[p].x),
+                                                   T.z[t].x + (e ? nz[p].y : nz[p].x),
+                                                   fmaf(T.rx[t].x, e ? cbx[p].y : cbx[p].x, T.fx[t].x),
+                                                   fmaf(T.ry[t].x, e ? cby[p].y : cby[p].x, T.fy[t].x),
+                                                   fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fz[t].x));
+                        if (e) {
+                            ax[p].y += c.x;
+                            ay[p].y += c.y;
+                            az[p].y += c.z;
+                        } else {
+                            ax[p].x += c.x;
+                            ay[p].x += c.y;
+                            az[p].x += c.z;
+                        }
+                    }
                 }
             }
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int h = 0; h < 2; h++)
-        s_red[(sl * 2 + h) * kHalf + il] = make_float4(ax[h].x + ax[h].y, ay[h].x + ay[h].y, az[h].x + az[h].y, 0.f);
+    for (int h = 0; h < kTeaNI; h++) {
+        const int p = h >> 1;
+        const bool hi = h & 1;
+        s_red[(sl * kTeaNI + h) * kTeaLanes + il] =
+            make_float4(hi ? ax[p].y : ax[p].x, hi ? ay[p].y : ay[p].x, hi ? az[p].y : az[p].x, 0.f);
+    }
     __syncthreads();
     if (sl != 0) return;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int g = gi[h];
+    for (int h = 0; h < kTeaNI; h++) {
+        const int g = w.y + il + h * kTeaLanes;
         if (g >= end) continue;
         float sx = 0.f, sy = 0.f, sz = 0.f;
         for (int k = 0; k < SLICES; k++) {
-            const float4 v = s_red[(k * 2 + h) * kHalf + il];
+            const float4 v = s_red[(k * kTeaNI + h) * kTeaLanes + il];
             sx += v.x;
             sy += v.y;
             sz += v.z;
         }
+        // back to units of D_ii, plus the bead's own term F_i + C_i o R_i
+        const float4 ci = B.tea_ci[g], Fi = B.force[g], Ri = B.tea_r[g];
+        sx = fmaf(K.c075a, sx, Fi.x + Ri.x * (1.0f / sqrtf(1.0f + b2 * ci.x)));
+        sy = fmaf(K.c075a, sy, Fi.y + Ri.y * (1.0f / sqrtf(1.0f + b2 * ci.y)));
+        sz = fmaf(K.c075a, sz, Fi.z + Ri.z * (1.0f / sqrtf(1.0f + b2 * ci.z)));
         if (FEFF) {
             feff[g] = make_float4(sx, sy, sz, 0.f);
             continue;
         }
         const int flags = B.flags[g];
         Frame Fr;
-        Fr.p0 = pi[h];
+        Fr.p0 = B.frame_in[g];
         Fr.p1 = B.frame_in[nb + g];
         Fr.p2 = B.frame_in[2 * nb + g];
         Fr.p3 = B.frame_in[3 * nb + g];
@@ -514,7 +535,7 @@ __global__ void __launch_bounds__(kTeaI / 2 * SLICES) k_tea_step(KParams P, DevB
 
 void launch_tea_eps_gated(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
                           int run_if, cudaStream_t s) {
-    const int t = kTeaI / 2 * P.tea_slices;
+    const int t = kTeaLanes * P.tea_slices;
     switch (P.tea_slices) {
         case 1: k_tea_eps<1><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
         case 2: k_tea_eps<2><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
@@ -535,7 +556,7 @@ void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, floa
 template <bool FEFF>
 static void tea_step_dispatch(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, float4 *feff,
                               const int *gate, cudaStream_t s) {
-    const int t = kTeaI / 2 * P.tea_slices;
+    const int t = kTeaLanes * P.tea_slices;
     switch (P.tea_slices) {
         case 1: k_tea_step<1, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
         case 2: k_tea_step<2, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;

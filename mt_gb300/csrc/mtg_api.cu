@@ -420,7 +420,7 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
         // two beads per thread; aim for about two full waves at 64 registers
         const double target = (double)sms * 2048.0;
         int sl = 1;
-        while (sl < 8 && (double)nb / 2 * sl < target) sl <<= 1;
+        while (sl < 8 && (double)nb / 4 * sl < target) sl <<= 1;   // four beads per thread
         e->kp.tea_slices = sl;
     }
 

@@ -191,6 +191,15 @@ __device__ __forceinline__ float norm3_rn(float3 d) {
     return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z)));
 }
 
+// 1/sqrt(x) as the single hardware approximation instruction (a few ulp);
+// pair distances are never subnormal, so the flush-to-zero form gives the
+// same value for them without a subnormal fix-up.
+__device__ __forceinline__ float rsqrt_hw(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Spatial-hash buffers of the cell-list rebuild (kernels_cells.cu).
 struct CellBuffers {
     int nbuckets;          // sum over trajectories of their table sizes
@@ -238,7 +247,7 @@ void launch_energy(const KParams &P, const DevBuffers &B, double *per_bead, doub
 void launch_energy_totals(const KParams &P, const double *partials, const int *work_first, double *per_traj,
                           int *err, cudaStream_t s);
 // TEA kernels run over their own work list: chunks of kTeaChunk beads.
-constexpr int kTeaChunk = 64;
+constexpr int kTeaChunk = 128;
 void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
 void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s);
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);

@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, 
     const int traj = w.x, end = B.off[traj + 1];
     const int base = B.off[traj];
     const int slot = w.y + threadIdx.x;
+    __shared__ int s_bk[27][kTile];
     if (slot >= end) return;
     const float4 pi = C.cell_pos[slot];
     const int word = __float_as_int(pi.w), g = word & kCellIndexMask;
@@ -108,22 +109,31 @@ __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, 
         const int cx = cell_coord(pi.x, inv_cell), cy = cell_coord(pi.y, inv_cell), cz = cell_coord(pi.z, inv_cell);
         const int tb = C.tbase[traj];
         const uint32_t mask = (uint32_t)C.tmask[traj];
+        // the 27 buckets (kept in shared memory for the rolled cell loop) and
+        // a mask of the cells whose bucket an earlier cell already has
         int bk[27];
 #pragma unroll
-        for (int c = 0; c < 27; c++)
+        for (int c = 0; c < 27; c++) {
             bk[c] = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
-        int st_next = C.start[bk[0]], ct_next = C.cnt[bk[0]];
+            s_bk[c][threadIdx.x] = bk[c];
+        }
+        uint32_t dup = 0;
 #pragma unroll
+        for (int c = 1; c < 27; c++) {
+            bool seen = false;
+#pragma unroll
+            for (int v = 0; v < c; v++) seen |= (bk[v] == bk[c]);
+            dup |= (seen ? 1u : 0u) << c;
+        }
+        int st_next = C.start[bk[0]], ct_next = C.cnt[bk[0]];
         for (int c = 0; c < 27; c++) {
             const int st_c = st_next, ct_c = ct_next;
             if (c + 1 < 27) {   // the next cell's range is fetched while this one runs
-                st_next = C.start[bk[c + 1]];
-                ct_next = C.cnt[bk[c + 1]];
+                const int b = s_bk[c + 1][threadIdx.x];
+                st_next = C.start[b];
+                ct_next = C.cnt[b];
             }
-            bool seen = false;   // two cells hashed to one bucket: visit it once
-#pragma unroll
-            for (int v = 0; v < c; v++) seen |= (bk[v] == bk[c]);
-            if (seen || ct_c == 0) continue;
+            if (((dup >> c) & 1u) || ct_c == 0) continue;
             const int s1e = base + st_c + ct_c;
             for (int s = base + st_c; s < s1e; s += 4) {
                 float4 q[4];   // four candidates in flight
@@ -136,7 +146,7 @@ __global__ void __launch_bounds__(kTile) k_descriptors(KParams P, DevBuffers B, 
                     const float ex = q[u].x - pi.x, ey = q[u].y - pi.y, ez = q[u].z - pi.z;
                     const float r2 = ex * ex + ey * ey + ez * ez;
                     if (!(r2 < kDescCut * kDescCut) || !(r2 > 0.f) || (wj & kCellExtraBit) || wj == g) continue;
-                    const float rinv = rsqrtf(r2), r = r2 * rinv;
+                    const float rinv = rsqrt_hw(r2), r = r2 * rinv;
                     const float ux = ex * rinv, uy = ey * rinv, uz = ez * rinv;
                     if (r < 5.0f)
                         desc_add(s0, rinv, ux, uy, uz);
