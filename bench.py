@@ -2,8 +2,14 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl mtg|reference]
 
-One bench step = one pair-list period (``ljpairsupdatefreq`` = 10 MD steps:
-one list rebuild + 10 force/update steps) over the whole batch.  The metric
+The default workload is the headline comparison: exact TEA against learned
+TEA (the surrogate network in the step loop, re-checked by exact TEA every
+100 steps, fallback above 1% RMS mobility error) on 64 trajectories of
+13 PF x 200 monomers + 3000 free monomers; `value` is the learned path's
+monomer-steps/s (the exact path's if the learned one fell back), and the
+line carries both.  One bench step = one re-check period (100 MD steps)
+there, and one pair-list period (``ljpairsupdatefreq`` = 10 MD steps: one
+list rebuild + 10 force/update steps) for the other workloads.  The metric
 is monomer-steps/s = active (non-extra) beads x MD steps / seconds.
 
 value     device time of the K timed bench steps (CUDA events on the engine's
@@ -71,7 +77,7 @@ WORKLOADS = {
                                          samples=1_000_000, epochs=20, batch=4096, lr=1e-3, recheck=100,
                                          max_err=0.01),
 }
-DEFAULT_WORKLOAD = "batched_plain_256x1520"
+DEFAULT_WORKLOAD = "tea_learned_vs_exact_64x5600"
 
 
 # ---------------------------------------------------------------- helpers
@@ -462,10 +468,14 @@ def run_tea_compare(args, spec, dist):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dist.local}")
     active = b.active_beads()
     results = {}
+    tune = None
     for mode in ("exact", "learned"):
         e = engine.Engine(b)
         e.upload_state(b.coords)
-        if mode == "learned":
+        if mode == "exact":   # launch shapes from the autotuner (exact TEA), used by both paths
+            tune = e.autotune(0, 10, cache=TUNE_CACHE, key=tune_key(b, args.workload))
+        else:
+            e.set_tuning(**tune["tuning"])
             e.set_surrogate(surr, recheck_every=period, max_err=spec["max_err"])
         step = 0
         for _ in range(args.warmup):
@@ -535,6 +545,7 @@ def run_tea_compare(args, spec, dist):
             "data": "synthetic",
             "config": {"workload": args.workload, "trajectories_per_gpu": b.ntraj, "beads_per_gpu": b.nbeads,
                        "md_steps_per_bench_step": period, "recheck_every": period, "max_mobility_error": spec["max_err"],
+                       "tuning": tune,
                        "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{dist.ws} (independent trajectories)"},
             "learned_tea": {"value": L["value"], "fell_back": not learned_ok,

@@ -166,6 +166,19 @@ int mtg_seed_rng(mtg_engine *e, int rseed);
 int mtg_download_rng(mtg_engine *e, uint32_t *seeds);
 int mtg_upload_rng(mtg_engine *e, const uint32_t *seeds);
 
+/* Bit-exact restart.  Extends writeRestart / readRestart
+ * (src/preparator.cpp:664-714), which keep the coordinates as "%f" text and
+ * re-seed the noise, with one binary file that holds everything a resumed run
+ * needs to reproduce the uninterrupted run bit for bit: the bead state in
+ * full precision, both HybridTaus streams of every bead, the per-bead flags
+ * (gtp / extra / on_tubule), the neighbour lists of the current pair-list
+ * period and the TEA state (C_i row sums, beta, epsilon).  `step` is the next
+ * step to run.  Reading checks the file's hash and that it belongs to a system
+ * of the same sizes and modes (MTG_E_CONFIG otherwise); the learned-TEA
+ * re-check state is not part of it. */
+int mtg_write_restart(mtg_engine *e, const char *path, long long step);
+int mtg_read_restart(mtg_engine *e, const char *path, long long *step);
+
 /* Host <-> device state, Coord AoS (MTG_COORD_FLOATS floats per bead).  The
  * upload does not wrap angles; the reference wraps them once on the host in
  * initIntegration (src/compute_cuda.cu:1004-1010) and so does the compute()

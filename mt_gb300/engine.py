@@ -27,6 +27,8 @@ EXPORTS = {
     "mtg_seed_rng": (C.c_int, [C.c_void_p, C.c_int]),
     "mtg_download_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "mtg_upload_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
+    "mtg_write_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.c_longlong]),
+    "mtg_read_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_longlong)]),
     "mtg_upload_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "mtg_download_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "mtg_set_keep_forces": (C.c_int, [C.c_void_p, C.c_int]),
@@ -222,6 +224,15 @@ class Engine:
         s = np.ascontiguousarray(seeds, np.uint32)
         assert s.size == 8 * self.nb
         check(self.lib.mtg_upload_rng(self.h, ptr(s, C.c_uint32)))
+
+    def write_restart(self, path: str, step: int):
+        check(self.lib.mtg_write_restart(self.h, os.fsencode(path), step))
+
+    def read_restart(self, path: str) -> int:
+        """Loads the restart file; returns the step to resume from."""
+        st = C.c_longlong()
+        check(self.lib.mtg_read_restart(self.h, os.fsencode(path), C.byref(st)))
+        return st.value
 
     def set_gtp(self, gtp):
         a = np.ascontiguousarray(gtp, np.int32)

@@ -252,3 +252,63 @@ def test_autotune_leaves_the_simulation_unchanged(engine_mod):
     e2.step(0, 20)
     assert np.array_equal(e1.download_state(), e2.download_state())
     assert np.array_equal(e1.download_rng(), e2.download_rng())
+
+
+def _restart_roundtrip(engine_mod, b, tmp_path, n1, n2, mutate=None):
+    """n1 + n2 steps straight vs n1 steps, restart file, a fresh engine, n2 steps."""
+    e1 = engine_mod.Engine(b)
+    e1.upload_state(b.coords)
+    if mutate:
+        mutate(e1)
+    e1.step(0, n1 + n2)
+    ref_state, ref_rng = e1.download_state(), e1.download_rng()
+    e1.close()
+    e2 = engine_mod.Engine(b)
+    e2.upload_state(b.coords)
+    if mutate:
+        mutate(e2)
+    e2.step(0, n1)
+    path = str(tmp_path / "run.mtgrst")
+    e2.write_restart(path, n1)
+    e2.close()
+    e3 = engine_mod.Engine(b)
+    first = e3.read_restart(path)
+    assert first == n1
+    e3.step(first, n2)
+    assert np.array_equal(e3.download_state(), ref_state)
+    assert np.array_equal(e3.download_rng(), ref_rng)
+    e3.close()
+
+
+def test_restart_is_bit_exact_plain(engine_mod, tmp_path):
+    b = small_system(seed=41)
+    # resume in the middle of a pair-list period (the lists come from the file)
+    _restart_roundtrip(engine_mod, b, tmp_path, 15, 17,
+                       mutate=lambda e: e.set_gtp(np.where(np.arange(b.nbeads) % 3 == 0, 1, 0)))
+
+
+def test_restart_is_bit_exact_tea(engine_mod, tmp_path):
+    b = small_system(seed=42, tea=True, tea_epsilon_freq=5)
+    _restart_roundtrip(engine_mod, b, tmp_path, 13, 12)   # between two epsilon steps
+
+
+def test_restart_rejects_other_systems_and_corruption(engine_mod, tmp_path):
+    b = small_system(seed=43)
+    e = engine_mod.Engine(b)
+    e.upload_state(b.coords)
+    e.step(0, 3)
+    path = tmp_path / "a.mtgrst"
+    e.write_restart(str(path), 3)
+    e.close()
+    other = engine_mod.Engine(small_system(seed=43, n_free=60))
+    with pytest.raises(engine_mod.MtgError):
+        other.read_restart(str(path))
+    other.close()
+    raw = bytearray(path.read_bytes())
+    raw[100] ^= 0x40
+    bad = tmp_path / "bad.mtgrst"
+    bad.write_bytes(bytes(raw))
+    e = engine_mod.Engine(b)
+    with pytest.raises(engine_mod.MtgError):
+        e.read_restart(str(bad))
+    e.close()
