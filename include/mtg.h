@@ -196,6 +196,38 @@ int mtg_set_keep_forces(mtg_engine *e, int keep);
 int mtg_set_gtp(mtg_engine *e, const int *gtp);
 int mtg_set_extra(mtg_engine *e, const uint8_t *extra);
 int mtg_set_on_tubule(mtg_engine *e, const int *on_tubule_cur);
+/* Reads the per-bead flags back (each output may be NULL). */
+int mtg_download_flags(mtg_engine *e, int *gtp, uint8_t *extra, int *on_tubule_cur, int *on_tubule_prev);
+
+/* Stride-step analytics of the updater on the device-resident state, so a
+ * stride step does not download the coordinates for them.
+ *
+ * mtg_mt_length: mt_length (src/updater.cpp:154-227).  A bead is on the
+ * tubule when |(x, y)| < R_MT + R_THRES, |(x, y)| > 1 and cos(theta) >
+ * cos(ANG_THRES) (src/mt.h:23-30); sets on_tubule_cur of every bead (after
+ * copying it to on_tubule_prev when save_prev != 0, as the reference's
+ * compute loop does at stride steps after the first, src/compute_cuda.cu:1186)
+ * and writes the per-trajectory counts mt_len[ntraj] (may be NULL). */
+int mtg_mt_length(mtg_engine *e, int save_prev, int *mt_len);
+/* hydrolyse (src/updater.cpp:229-257) in two calls.  The reference draws
+ * prob = rand() / RAND_MAX for every candidate dimer - GTP, not extra, on the
+ * tubule now and at the previous stride - in the order dimer index (outer),
+ * trajectory (inner), and hydrolyses it when prob < 0.02; afterwards every
+ * GDP dimer off the tubule now and before returns to GTP.
+ * mtg_hydrolysis_candidates counts the candidates; the caller draws that many
+ * numbers in the reference's order and passes them to mtg_hydrolyse, which
+ * applies both loops on the device.  events (may be NULL) receives one byte
+ * per slot k * ntraj + t (dimer k of trajectory t; mtg_hydrolysis_slots gives
+ * the number of dimer indices): 0 nothing, 1 hydrolysed, 2 back to GTP.  No
+ * reference counterpart for the split; the effect is the reference's. */
+int mtg_hydrolysis_candidates(mtg_engine *e, int *count);
+int mtg_hydrolyse(mtg_engine *e, const double *prob, int n, int8_t *events, int *n_hydrolysed, int *n_restored);
+int mtg_hydrolysis_slots(const mtg_engine *e, int *max_dimers);
+/* change_conc support (src/updater.cpp:97-152): the extra beads of every
+ * trajectory, and a scatter update of a few beads' state (Coord AoS) and
+ * extra flags, for the dimers it re-inserts (its rand() stays with the caller). */
+int mtg_count_extra(mtg_engine *e, int *n_extra);
+int mtg_set_beads(mtg_engine *e, const int *idx, const float *coords, const uint8_t *extra, int n);
 
 /* Rebuilds the LJ list (LJ_kernel, src/compute_cuda.cu:913-940) and, in
  * assembly mode, the longitudinal and lateral lists (pairs_kernel,

@@ -622,7 +622,8 @@ int mtg_destroy(mtg_engine *e) {
                     e->tea_eps_t, e->stage, e->stage_u8, e->stage_i, e->cell_tbase, e->cell_tmask,
                     e->cell_key, e->cell_bead, e->cell_pos, e->cell_cnt, e->cell_start, e->cell_cursor, e->tea_work,
                     e->surr_desc, e->surr_pred, e->surr_stats, e->surr_gate, e->surr_err, e->surr_part,
-                    e->tea_ci2, e->feff_a, e->feff_b, e->tea_eps2, e->tea_beta2, e->tea_eps_t2};
+                    e->tea_ci2, e->feff_a, e->feff_b, e->tea_eps2, e->tea_beta2, e->tea_eps_t2,
+                    e->hydro_cand, e->hydro_rank, e->hydro_sums, e->hydro_counts, e->hydro_events};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (e->stage_host) cudaFreeHost(e->stage_host);

@@ -75,6 +75,10 @@ struct mtg_engine {
     float4 *tea_ci2 = nullptr, *feff_a = nullptr, *feff_b = nullptr;
     float *tea_eps2 = nullptr, *tea_beta2 = nullptr;
     double *tea_eps_t2 = nullptr;
+    // stride-step analytics (kernels_updater.cu)
+    int *hydro_cand = nullptr, *hydro_rank = nullptr, *hydro_sums = nullptr, *hydro_counts = nullptr;
+    int8_t *hydro_events = nullptr;
+    int hydro_ncand = -1;
 
     mtg::CellBuffers cells() const {
         mtg::CellBuffers c{};

@@ -28,6 +28,15 @@ EXPORTS = {
     "mtg_download_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "mtg_upload_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "mtg_write_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.c_longlong]),
+    "mtg_download_flags": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_uint8), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]),
+    "mtg_mt_length": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "mtg_hydrolysis_candidates": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "mtg_hydrolyse": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int8), C.POINTER(C.c_int),
+                                C.POINTER(C.c_int)]),
+    "mtg_hydrolysis_slots": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "mtg_count_extra": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "mtg_set_beads": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_uint8), C.c_int]),
     "mtg_read_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_longlong)]),
     "mtg_upload_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "mtg_download_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
@@ -233,6 +242,49 @@ class Engine:
         st = C.c_longlong()
         check(self.lib.mtg_read_restart(self.h, os.fsencode(path), C.byref(st)))
         return st.value
+
+    def download_flags(self):
+        """(gtp, extra, on_tubule_cur, on_tubule_prev) per bead."""
+        g = np.zeros(self.nb, np.int32)
+        x = np.zeros(self.nb, np.uint8)
+        c = np.zeros(self.nb, np.int32)
+        p = np.zeros(self.nb, np.int32)
+        check(self.lib.mtg_download_flags(self.h, ptr(g, C.c_int), ptr(x, C.c_uint8), ptr(c, C.c_int),
+                                          ptr(p, C.c_int)))
+        return g, x, c, p
+
+    def mt_length(self, save_prev: bool):
+        out = np.zeros(self.nt, np.int32)
+        check(self.lib.mtg_mt_length(self.h, int(save_prev), ptr(out, C.c_int)))
+        return out
+
+    def hydrolysis_candidates(self) -> int:
+        n = C.c_int()
+        check(self.lib.mtg_hydrolysis_candidates(self.h, C.byref(n)))
+        return n.value
+
+    def hydrolyse(self, prob, events: bool = False):
+        """Applies hydrolysis with one number per candidate; returns
+        (n_hydrolysed, n_restored, events [max_dimers, ntraj] or None)."""
+        p = np.ascontiguousarray(prob, np.float64)
+        md = C.c_int()
+        check(self.lib.mtg_hydrolysis_slots(self.h, C.byref(md)))
+        ev = np.zeros((md.value, self.nt), np.int8) if events else None
+        nh, nr = C.c_int(), C.c_int()
+        check(self.lib.mtg_hydrolyse(self.h, ptr(p, C.c_double), len(p), ptr(ev, C.c_int8), C.byref(nh),
+                                     C.byref(nr)))
+        return nh.value, nr.value, ev
+
+    def count_extra(self):
+        out = np.zeros(self.nt, np.int32)
+        check(self.lib.mtg_count_extra(self.h, ptr(out, C.c_int)))
+        return out
+
+    def set_beads(self, idx, coords, extra=None):
+        i = np.ascontiguousarray(idx, np.int32)
+        c = np.ascontiguousarray(coords, np.float32).reshape(len(i), 7)
+        x = None if extra is None else np.ascontiguousarray(extra, np.uint8)
+        check(self.lib.mtg_set_beads(self.h, ptr(i, C.c_int), ptr(c, C.c_float), ptr(x, C.c_uint8), len(i)))
 
     def set_gtp(self, gtp):
         a = np.ascontiguousarray(gtp, np.int32)
