@@ -2,7 +2,7 @@
 
 A numpy restatement of the reference's mt_length, hydrolyse and the counting
 part of change_conc (src/updater.cpp), on the Coord AoS state
-(x, y, z, fi, psi, theta, w) and per-bead flag arrays, for checking the
+(x, y, z, fi, theta, psi, w) and per-bead flag arrays, for checking the
 device kernels of mt_gb300/csrc/kernels_updater.cu.
 """
 import numpy as np
@@ -16,7 +16,7 @@ R_THRES = R_MON * np.float32(8)  # src/mt.h:30
 def on_tubule(coords):
     """The per-bead test of mt_length (src/updater.cpp:164-168), in FP32."""
     c = np.asarray(coords, np.float32)
-    x, y, theta = c[:, 0], c[:, 1], c[:, 5]
+    x, y, theta = c[:, 0], c[:, 1], c[:, 4]
     rad = np.sqrt(x * x + y * y)
     return (rad < R_MT + R_THRES) & (rad > np.float32(1.0)) & (np.cos(theta) > np.cos(ANG_THRES))
 
@@ -27,7 +27,7 @@ def decision_margin(coords):
     c = np.asarray(coords, np.float64)
     rad = np.sqrt(c[:, 0] ** 2 + c[:, 1] ** 2)
     return np.minimum.reduce([np.abs(rad - float(R_MT + R_THRES)), np.abs(rad - 1.0),
-                              np.abs(np.cos(c[:, 5]) - np.cos(1.0))])
+                              np.abs(np.cos(c[:, 4]) - np.cos(1.0))])
 
 
 def mt_length(coords, offsets, on_cur, save_prev, on_prev):

@@ -20,7 +20,7 @@ def batch_on_and_off_tubule(seed):
     free = np.nonzero(b.fixed == 0)[0]
     pick = rng.choice(free, size=len(free) // 3, replace=False)
     c[pick, 0:2] = rng.uniform(-20, 20, size=(len(pick), 2))
-    c[pick, 5] = rng.uniform(-2.0, 2.0, size=len(pick))
+    c[pick, 4] = rng.uniform(-2.0, 2.0, size=len(pick))   # theta
     return b, c
 
 
