@@ -179,6 +179,27 @@ int mtg_upload_rng(mtg_engine *e, const uint32_t *seeds);
 int mtg_write_restart(mtg_engine *e, const char *path, long long step);
 int mtg_read_restart(mtg_engine *e, const char *path, long long *step);
 
+/* Stride-step outputs without stalling the step loop.  Replaces the
+ * synchronous download of r at stride steps (src/compute_cuda.cu:1177) with
+ * saveCoordDCD (src/preparator.cpp:582-602) and OutputAllEnergies
+ * (src/updater.cpp:3-43): mtg_output_open writes the DCD headers of every
+ * trajectory's coordinate and angle files as createDCD + dcdWriteHeader do
+ * (src/dcdio.cpp:16-154, no unit cell; remark2 NULL = the reference's
+ * "REMARKS DATE: <asctime>"); mtg_output_frame queues the current state
+ * and/or the energy totals: the state is converted on the engine's stream,
+ * copied to pinned memory on a copy stream, and a host thread appends the
+ * frames (dcdWriteFrame's layout; (x, y, z) and (fi, psi, theta)) and prints
+ * the reference's energy lines, while the caller keeps stepping.  Two frames
+ * can be in flight; a third request waits for the older one.
+ * mtg_output_flush waits for all queued output; mtg_output_close flushes
+ * and stops the writer (mtg_destroy closes an open output).  No reference
+ * counterpart for the asynchronous pipeline; the bytes are the reference's. */
+int mtg_output_open(mtg_engine *e, const char *const *xyz_paths, const char *const *ang_paths, int nfile, int npriv,
+                    int nsavc, float delta, const char *remark2);
+int mtg_output_frame(mtg_engine *e, long long step, int frame, int energies);
+int mtg_output_flush(mtg_engine *e, long long *frames_written);
+int mtg_output_close(mtg_engine *e);
+
 /* Host <-> device state, Coord AoS (MTG_COORD_FLOATS floats per bead).  The
  * upload does not wrap angles; the reference wraps them once on the host in
  * initIntegration (src/compute_cuda.cu:1004-1010) and so does the compute()

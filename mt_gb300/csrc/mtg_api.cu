@@ -615,6 +615,7 @@ int mtg_destroy(mtg_engine *e) {
     if (!e) return MTG_OK;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
+    mtg_internal_close_output(e);
     destroy_graphs(e);
     void *ptrs[] = {e->off, e->traj, e->flags, e->harm, e->zs, e->frame[0], e->frame[1], e->force, e->seeds,
                     e->ljc, e->lj, e->lonc, e->lon, e->latc, e->lat, e->err, e->work, e->work_first,

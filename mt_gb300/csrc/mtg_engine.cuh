@@ -79,6 +79,8 @@ struct mtg_engine {
     int *hydro_cand = nullptr, *hydro_rank = nullptr, *hydro_sums = nullptr, *hydro_counts = nullptr;
     int8_t *hydro_events = nullptr;
     int hydro_ncand = -1;
+    // stride-step outputs (output.cu)
+    struct mtg_output *output = nullptr;
 
     mtg::CellBuffers cells() const {
         mtg::CellBuffers c{};
@@ -126,6 +128,7 @@ struct mtg_engine {
 // Records msg as the calling thread's last error (mtg_last_error_string) and
 // returns code.
 int mtg_internal_fail(int code, const char *msg);
+void mtg_internal_close_output(mtg_engine *e);
 
 // learned TEA helpers (surrogate.cu)
 int mtg_surrogate_buffers(mtg_engine *e);

@@ -28,6 +28,11 @@ EXPORTS = {
     "mtg_download_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "mtg_upload_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "mtg_write_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.c_longlong]),
+    "mtg_output_open": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int, C.c_int,
+                                  C.c_int, C.c_float, C.c_char_p]),
+    "mtg_output_frame": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.c_int]),
+    "mtg_output_flush": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "mtg_output_close": (C.c_int, [C.c_void_p]),
     "mtg_download_flags": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_uint8), C.POINTER(C.c_int),
                                      C.POINTER(C.c_int)]),
     "mtg_mt_length": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
@@ -242,6 +247,25 @@ class Engine:
         st = C.c_longlong()
         check(self.lib.mtg_read_restart(self.h, os.fsencode(path), C.byref(st)))
         return st.value
+
+    def output_open(self, xyz_paths, ang_paths, nfile: int, npriv: int, nsavc: int, delta: float,
+                    remark2: str | None = None):
+        """DCD files of every trajectory (coordinates, angles); see mtg_output_open."""
+        xa = (C.c_char_p * self.nt)(*[os.fsencode(p) for p in xyz_paths])
+        aa = (C.c_char_p * self.nt)(*[os.fsencode(p) for p in ang_paths])
+        check(self.lib.mtg_output_open(self.h, xa, aa, nfile, npriv, nsavc, delta,
+                                       None if remark2 is None else remark2.encode()))
+
+    def output_frame(self, step: int, frame: bool = True, energies: bool = False):
+        check(self.lib.mtg_output_frame(self.h, step, int(frame), int(energies)))
+
+    def output_flush(self) -> int:
+        n = C.c_longlong()
+        check(self.lib.mtg_output_flush(self.h, C.byref(n)))
+        return n.value
+
+    def output_close(self):
+        check(self.lib.mtg_output_close(self.h))
 
     def download_flags(self):
         """(gtp, extra, on_tubule_cur, on_tubule_prev) per bead."""
