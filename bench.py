@@ -76,6 +76,12 @@ WORKLOADS = {
                                          train=dict(ntraj=16, n_mon=100, n_free=2000, cube=100.0),
                                          samples=1_000_000, epochs=20, batch=4096, lr=1e-3, recheck=100,
                                          max_err=0.01),
+    # stride-step work on the uneven batch: every 100 steps a DCD frame of
+    # every trajectory, the energy totals, mt_length and hydrolysis; the
+    # asynchronous pipeline and the device analytics against the reference's
+    # synchronous download + host loops
+    "stride_io_ragged_1024": dict(kind="stride", ragged=True, ntraj=1024, pf_range=(8, 120), free_range=(0, 2000),
+                                  cube=150.0, n_mon=64, n_free=1000, stride=100),
 }
 DEFAULT_WORKLOAD = "tea_learned_vs_exact_64x5600"
 
@@ -569,6 +575,98 @@ def run_tea_compare(args, spec, dist):
     return out
 
 
+def run_stride(args, spec, dist):
+    """Throughput with stride-step outputs: (a) mtg_output_frame (pinned
+    double buffers + writer thread) and the device analytics (mt_length,
+    hydrolysis) vs (b) the reference's order: synchronous download of the
+    state and energies, host DCD writes, host mt_length / hydrolyse loops."""
+    import tempfile
+
+    import torch
+
+    from mt_gb300 import build as mbuild
+    from mt_gb300 import engine
+    from oracle import dcd_oracle as D
+    from oracle import updater_oracle as U
+
+    mbuild.build()
+    torch.cuda.set_device(dist.local)
+    seed = 1 + dist.rank
+    b = make_batch(spec, seed)
+    b.params.device = dist.local
+    stride = spec["stride"]
+    active = b.active_beads()
+    tmp = tempfile.mkdtemp(prefix="mtg_stride_")
+    rng = np.random.default_rng(seed)
+    res = {}
+    for mode in ("async", "sync"):
+        e = engine.Engine(b)
+        e.upload_state(b.coords)
+        e.autotune(0, 10, cache=TUNE_CACHE, key=tune_key(b, "ragged_1024"))
+        xyz = [os.path.join(tmp, f"{mode}_xyz{t}.dcd") for t in range(b.ntraj)]
+        ang = [os.path.join(tmp, f"{mode}_ang{t}.dcd") for t in range(b.ntraj)]
+        nfile = args.warmup + args.steps
+        if mode == "async":
+            e.output_open(xyz, ang, nfile, 1, stride, float(b.params.dt), "REMARKS BENCH")
+        else:
+            for t in range(b.ntraj):
+                n = int(b.offsets[t + 1] - b.offsets[t])
+                for path in (xyz[t], ang[t]):
+                    open(path, "wb").write(D.header(n, nfile, 1, stride, float(b.params.dt), "REMARKS BENCH"))
+        on_cur = b.on_tubule.copy()
+        gtp = b.gtp.copy()
+        hook_s = []
+        t0 = None
+        for k in range(args.warmup + args.steps):
+            if k == args.warmup:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+            e.step(k * stride, stride)
+            h0 = time.perf_counter()
+            if mode == "async":
+                e.output_frame((k + 1) * stride, frame=True, energies=True)
+                e.mt_length(save_prev=k > 0)
+                n = e.hydrolysis_candidates()
+                e.hydrolyse(rng.uniform(size=n))
+            else:
+                st = e.download_state()
+                en = e.energies()
+                for t in range(b.ntraj):
+                    a, z = b.offsets[t], b.offsets[t + 1]
+                    with open(xyz[t], "ab") as f:
+                        f.write(D.frame(st[a:z, 0], st[a:z, 1], st[a:z, 2]))
+                    with open(ang[t], "ab") as f:
+                        f.write(D.frame(st[a:z, 3], st[a:z, 5], st[a:z, 4]))
+                lines = "".join(f"Energies[{t}]:\t" + "\t".join(f"{v:f}" for v in u) + "\n" for t, u in enumerate(en))
+                mt_len, on_new, on_prev = U.mt_length(st, b.offsets, on_cur, k > 0, on_cur)
+                on_cur = on_new
+                gtp, _ = U.hydrolyse_vec(b.offsets, gtp, b.extra, on_cur, on_prev, lambda m: rng.uniform(size=m))
+                e.set_gtp(gtp)
+                del lines, mt_len
+            if k >= args.warmup:
+                hook_s.append(time.perf_counter() - h0)
+        if mode == "async":
+            e.output_close()
+        torch.cuda.synchronize()
+        total = time.perf_counter() - t0
+        res[mode] = {"value": active * stride * args.steps / total, "s_per_stride": total / args.steps,
+                     "hook_ms_per_stride": 1e3 * float(np.mean(hook_s))}
+        e.close()
+    import shutil
+    shutil.rmtree(tmp, ignore_errors=True)
+    if dist.rank != 0:
+        return None
+    return {"metric": METRIC, "value": res["async"]["value"], "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * res["async"]["s_per_stride"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "trajectories_per_gpu": b.ntraj, "beads_per_gpu": b.nbeads,
+                       "md_steps_per_bench_step": stride,
+                       "per_stride": "DCD frame of every trajectory (xyz + angles), energy totals, mt_length, "
+                                     "hydrolysis"},
+            "async_device_hooks": res["async"], "sync_host_hooks": res["sync"],
+            "async_over_sync": res["async"]["value"] / res["sync"]["value"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -582,9 +680,14 @@ def main():
     dist = Dist()
     try:
         if args.impl == "reference":
-            run_reference(args, dict(spec, kind="tea") if spec["kind"] == "tea_compare" else spec, dist)
+            run_reference(args, dict(spec, kind="tea") if spec["kind"] == "tea_compare" else
+                          dict(spec, kind="plain") if spec["kind"] == "stride" else spec, dist)
         elif spec["kind"] == "tea_compare":
             out = run_tea_compare(args, spec, dist)
+            if out is not None:
+                print(json.dumps(out))
+        elif spec["kind"] == "stride":
+            out = run_stride(args, spec, dist)
             if out is not None:
                 print(json.dumps(out))
         else:

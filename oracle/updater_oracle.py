@@ -76,3 +76,28 @@ def hydrolyse(offsets, gtp, extra, on_cur, on_prev, prob_source):
 def count_extra(offsets, extra):
     """num_of_extra of change_conc (src/updater.cpp:103-108) per trajectory."""
     return np.array([int(np.count_nonzero(extra[offsets[t]:offsets[t + 1]])) for t in range(len(offsets) - 1)])
+
+
+def hydrolyse_vec(offsets, gtp, extra, on_cur, on_prev, draw):
+    """hydrolyse with numpy (the same decisions as `hydrolyse`): draw(n)
+    returns the n candidates' numbers in the reference's order."""
+    gtp = np.array(gtp, np.int32)
+    offsets = np.asarray(offsets)
+    nt = len(offsets) - 1
+    half = np.diff(offsets) // 2
+    md = int(half.max()) if nt else 0
+    k, t = np.divmod(np.arange(md * nt), nt)          # slot order: dimer outer, trajectory inner
+    ok = k < half[t]
+    k, t = k[ok], t[ok]
+    g = offsets[t] + 2 * k
+    extra = np.asarray(extra).astype(bool)
+    cand = (gtp[g] == 1) & ~extra[g] & (np.asarray(on_cur)[g] * np.asarray(on_prev)[g] == 1)
+    n = int(cand.sum())
+    hyd = np.zeros(len(g), bool)
+    hyd[cand] = np.asarray(draw(n)) < 0.02
+    gtp[g[hyd]] = 0
+    gtp[g[hyd] + 1] = 0
+    back = (gtp[g] == 0) & ~extra[g] & (np.asarray(on_cur)[g] == 0) & (np.asarray(on_prev)[g] == 0)
+    gtp[g[back]] = 1
+    gtp[g[back] + 1] = 1
+    return gtp, n
