@@ -607,7 +607,8 @@ def run_stride(args, spec, dist):
         ang = [os.path.join(tmp, f"{mode}_ang{t}.dcd") for t in range(b.ntraj)]
         nfile = args.warmup + args.steps
         if mode == "async":
-            e.output_open(xyz, ang, nfile, 1, stride, float(b.params.dt), "REMARKS BENCH")
+            e.output_open(xyz, ang, nfile, 1, stride, float(b.params.dt), "REMARKS BENCH",
+                          energy_path=os.path.join(tmp, "energies.txt"))
         else:
             for t in range(b.ntraj):
                 n = int(b.offsets[t + 1] - b.offsets[t])
@@ -638,6 +639,8 @@ def run_stride(args, spec, dist):
                     with open(ang[t], "ab") as f:
                         f.write(D.frame(st[a:z, 3], st[a:z, 5], st[a:z, 4]))
                 lines = "".join(f"Energies[{t}]:\t" + "\t".join(f"{v:f}" for v in u) + "\n" for t, u in enumerate(en))
+                with open(os.path.join(tmp, "energies_sync.txt"), "a") as f:
+                    f.write(lines)
                 mt_len, on_new, on_prev = U.mt_length(st, b.offsets, on_cur, k > 0, on_cur)
                 on_cur = on_new
                 gtp, _ = U.hydrolyse_vec(b.offsets, gtp, b.extra, on_cur, on_prev, lambda m: rng.uniform(size=m))

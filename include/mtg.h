@@ -185,7 +185,8 @@ int mtg_read_restart(mtg_engine *e, const char *path, long long *step);
  * (src/updater.cpp:3-43): mtg_output_open writes the DCD headers of every
  * trajectory's coordinate and angle files as createDCD + dcdWriteHeader do
  * (src/dcdio.cpp:16-154, no unit cell; remark2 NULL = the reference's
- * "REMARKS DATE: <asctime>"); mtg_output_frame queues the current state
+ * "REMARKS DATE: <asctime>"; energy_path NULL = standard output, else the
+ * energy lines are appended to that file); mtg_output_frame queues the current state
  * and/or the energy totals: the state is converted on the engine's stream,
  * copied to pinned memory on a copy stream, and a host thread appends the
  * frames (dcdWriteFrame's layout; (x, y, z) and (fi, psi, theta)) and prints
@@ -195,7 +196,7 @@ int mtg_read_restart(mtg_engine *e, const char *path, long long *step);
  * and stops the writer (mtg_destroy closes an open output).  No reference
  * counterpart for the asynchronous pipeline; the bytes are the reference's. */
 int mtg_output_open(mtg_engine *e, const char *const *xyz_paths, const char *const *ang_paths, int nfile, int npriv,
-                    int nsavc, float delta, const char *remark2);
+                    int nsavc, float delta, const char *remark2, const char *energy_path);
 int mtg_output_frame(mtg_engine *e, long long step, int frame, int energies);
 int mtg_output_flush(mtg_engine *e, long long *frames_written);
 int mtg_output_close(mtg_engine *e);

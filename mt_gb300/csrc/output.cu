@@ -176,6 +176,7 @@ void release(mtg_output *o) {
         if (o->copied[s]) cudaEventDestroy(o->copied[s]);
     }
     if (o->d_ignored_err) cudaFree(o->d_ignored_err);
+    if (o->energy_out && o->energy_out != stdout) std::fclose(o->energy_out);
     if (o->copy) cudaStreamDestroy(o->copy);
     delete o;
 }
@@ -201,7 +202,7 @@ void mtg_internal_close_output(mtg_engine *e) {
 extern "C" {
 
 int mtg_output_open(mtg_engine *e, const char *const *xyz_paths, const char *const *ang_paths, int nfile, int npriv,
-                    int nsavc, float delta, const char *remark2) {
+                    int nsavc, float delta, const char *remark2, const char *energy_path) {
     if (!e || !xyz_paths || !ang_paths) return mtg_internal_fail(MTG_E_CONFIG, "engine or paths is NULL");
     if (e->output) return mtg_internal_fail(MTG_E_STATE, "output already open");
     cudaSetDevice(e->device);
@@ -239,6 +240,14 @@ int mtg_output_open(mtg_engine *e, const char *const *xyz_paths, const char *con
         OCK(cudaMallocHost(&o->h_en[s], sizeof(double) * 7 * (size_t)e->nt));
         OCK(cudaEventCreateWithFlags(&o->converted[s], cudaEventDisableTiming));
         OCK(cudaEventCreateWithFlags(&o->copied[s], cudaEventDisableTiming));
+    }
+    if (energy_path) {
+        o->energy_out = std::fopen(energy_path, "a");
+        if (!o->energy_out) {
+            o->energy_out = stdout;
+            release(o);
+            return mtg_internal_fail(MTG_E_CONFIG, "cannot open the energy file");
+        }
     }
     o->writer = std::thread(writer_loop, o);
     e->output = o;

@@ -29,7 +29,7 @@ EXPORTS = {
     "mtg_upload_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "mtg_write_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.c_longlong]),
     "mtg_output_open": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int, C.c_int,
-                                  C.c_int, C.c_float, C.c_char_p]),
+                                  C.c_int, C.c_float, C.c_char_p, C.c_char_p]),
     "mtg_output_frame": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.c_int]),
     "mtg_output_flush": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "mtg_output_close": (C.c_int, [C.c_void_p]),
@@ -249,12 +249,13 @@ class Engine:
         return st.value
 
     def output_open(self, xyz_paths, ang_paths, nfile: int, npriv: int, nsavc: int, delta: float,
-                    remark2: str | None = None):
+                    remark2: str | None = None, energy_path: str | None = None):
         """DCD files of every trajectory (coordinates, angles); see mtg_output_open."""
         xa = (C.c_char_p * self.nt)(*[os.fsencode(p) for p in xyz_paths])
         aa = (C.c_char_p * self.nt)(*[os.fsencode(p) for p in ang_paths])
         check(self.lib.mtg_output_open(self.h, xa, aa, nfile, npriv, nsavc, delta,
-                                       None if remark2 is None else remark2.encode()))
+                                       None if remark2 is None else remark2.encode(),
+                                       None if energy_path is None else os.fsencode(energy_path)))
 
     def output_frame(self, step: int, frame: bool = True, energies: bool = False):
         check(self.lib.mtg_output_frame(self.h, step, int(frame), int(energies)))
