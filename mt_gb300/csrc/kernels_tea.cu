@@ -11,8 +11,9 @@
 // lanes of a packed operand), so one broadcast 8-byte load feeds a packed
 // pair of beads i.  Away from the CTA's own beads the far-field formula runs
 // for every pair; the few overlapping pairs (r <= 2a) are found through the
-// running minimum of r^2 and corrected afterwards.  The tile that holds the
-// CTA's own beads (the self pairs) runs the scalar formula with both branches.
+// running minimum of r^2 and corrected afterwards.  In the tile that holds
+// the CTA's own beads the self pairs get r^2 = 1e30: their terms are then
+// far below the rounding of the sums, and the correction skips them.
 // Sums are kept in units of 0.75 a (T' = T / (0.75 a)).  The kernels are
 // bound by the FP32 pipe (about 45 FLOP per ordered pair).
 #include "mtg_internal.cuh"
@@ -96,13 +97,51 @@ __device__ __forceinline__ EpsTerms eps_terms(float dx, float dy, float dz, floa
     return {bc * dx * dx, bc * dy * dy, bc * dz * dz, cii * cii, fmaf(crq * us, us, 3.0f * cii)};
 }
 
+// The packed pass of one tile of the epsilon pass (self pairs pushed to
+// r^2 = 1e30 when SELF), running minimum of r^2 per bead pair.
+template <int SLICES, bool SELF>
+__device__ __forceinline__ void tea_eps_tile(const TeaTile &T, int sl, int self_t, const float2 (&nx)[kTeaPairsI],
+                                             const float2 (&ny)[kTeaPairsI], const float2 (&nz)[kTeaPairsI],
+                                             float2 vkap, float2 vn2a2, float2 two, float2 three,
+                                             float2 (&sx)[kTeaPairsI], float2 (&sy)[kTeaPairsI],
+                                             float2 (&sz)[kTeaPairsI], float2 (&sa)[kTeaPairsI],
+                                             float2 (&sw)[kTeaPairsI], float (&rmin)[kTeaPairsI]) {
+#pragma unroll 2
+    for (int t = sl; t < kTeaTile; t += SLICES) {
+        const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+#pragma unroll
+        for (int p = 0; p < kTeaPairsI; p++) {
+            const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
+            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            if (SELF) {
+                if (t == self_t + kTeaLanes * 2 * p) r2.x = 1e30f;
+                if (t == self_t + kTeaLanes * (2 * p + 1)) r2.y = 1e30f;
+            }
+            rmin[p] = fminf(rmin[p], fminf(r2.x, r2.y));
+            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+            const float2 q = __fmul2_rn(rinv, rinv);
+            const float2 tq = __fmul2_rn(q, rinv);
+            const float2 cii = __ffma2_rn(vkap, tq, rinv);
+            const float2 crr = __ffma2_rn(vn2a2, tq, rinv);
+            const float2 crq = __fmul2_rn(crr, q);
+            const float2 bc = __fmul2_rn(__ffma2_rn(two, cii, crr), crq);
+            sa[p] = __ffma2_rn(cii, cii, sa[p]);
+            sx[p] = __ffma2_rn(__fmul2_rn(bc, dx), dx, sx[p]);
+            sy[p] = __ffma2_rn(__fmul2_rn(bc, dy), dy, sy[p]);
+            sz[p] = __ffma2_rn(__fmul2_rn(bc, dz), dz, sz[p]);
+            const float2 us = __fadd2_rn(__fadd2_rn(dx, dy), dz);
+            sw[p] = __ffma2_rn(__fmul2_rn(crq, us), us, __ffma2_rn(three, cii, sw[p]));
+        }
+    }
+}
+
 // integrateTea_epsilon_unlisted (src/bdhitea_kernel.cu:84-101): per bead i,
 // sum over non-extra j != i of the row sums of squared entries (-> tea_ci)
 // and of all nine entries (-> tea_eps).  With T = cii I + crr u u^T the row
 // sums of squares are cii^2 + (2 cii + crr) crr u_c^2 and the sum of all
 // entries is 3 cii + crr (u_x + u_y + u_z)^2.
 template <int SLICES>
-__global__ void __launch_bounds__(kTeaLanes *SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work,
+__global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work,
                                                                 const int *gate, int run_if) {
     if (gate && *gate != run_if) return;
     const int2 w = work[blockIdx.x];
@@ -140,93 +179,48 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES) k_tea_eps(KParams P, DevBuf
         tea_tile_load<false>(T, B, j0, end);
         __syncthreads();
         if (any_act) {
+            // self pairs: as in k_tea_step
             const bool self_tile = (w.y < j0 + kTeaTile) && (w.y + kTeaI > j0);
-            if (!self_tile) {
-                float rmin[kTeaPairsI];
+            const int self_t = self_tile ? w.y - j0 + il : -(1 << 30);
+            float rmin[kTeaPairsI];
 #pragma unroll
-                for (int p = 0; p < kTeaPairsI; p++) rmin[p] = 3.4e38f;
-#pragma unroll 2
-                for (int t = sl; t < kTeaTile; t += SLICES) {
-                    const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+            for (int p = 0; p < kTeaPairsI; p++) rmin[p] = 3.4e38f;
+            if (self_tile)
+                tea_eps_tile<SLICES, true>(T, sl, self_t, nx, ny, nz, vkap, vn2a2, two, three, sx, sy, sz, sa, sw,
+                                           rmin);
+            else
+                tea_eps_tile<SLICES, false>(T, sl, self_t, nx, ny, nz, vkap, vn2a2, two, three, sx, sy, sz, sa, sw,
+                                            rmin);
+            // overlapping pairs (r <= 2a): replace the far-field terms by the near ones
 #pragma unroll
-                    for (int p = 0; p < kTeaPairsI; p++) {
-                        const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]),
-                                     dz = __fadd2_rn(zj, nz[p]);
-                        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-                        rmin[p] = fminf(rmin[p], fminf(r2.x, r2.y));
-                        const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-                        const float2 q = __fmul2_rn(rinv, rinv);
-                        const float2 tq = __fmul2_rn(q, rinv);
-                        const float2 cii = __ffma2_rn(vkap, tq, rinv);
-                        const float2 crr = __ffma2_rn(vn2a2, tq, rinv);
-                        const float2 crq = __fmul2_rn(crr, q);
-                        const float2 bc = __fmul2_rn(__ffma2_rn(two, cii, crr), crq);
-                        sa[p] = __ffma2_rn(cii, cii, sa[p]);
-                        sx[p] = __ffma2_rn(__fmul2_rn(bc, dx), dx, sx[p]);
-                        sy[p] = __ffma2_rn(__fmul2_rn(bc, dy), dy, sy[p]);
-                        sz[p] = __ffma2_rn(__fmul2_rn(bc, dz), dz, sz[p]);
-                        const float2 us = __fadd2_rn(__fadd2_rn(dx, dy), dz);
-                        sw[p] = __ffma2_rn(__fmul2_rn(crq, us), us, __ffma2_rn(three, cii, sw[p]));
-                    }
-                }
-                // overlapping pairs (r <= 2a): replace the far-field terms by the near ones
-#pragma unroll
-                for (int p = 0; p < kTeaPairsI; p++) {
-                    if (!(rmin[p] <= K.four_a2)) continue;
-                    for (int t = sl; t < kTeaTile; t += SLICES) {
-#pragma unroll
-                        for (int e = 0; e < 2; e++) {
-                            const float ax = e ? nx[p].y : nx[p].x, ay = e ? ny[p].y : ny[p].x,
-                                        az = e ? nz[p].y : nz[p].x;
-                            const float dx = T.x[t].x + ax, dy = T.y[t].x + ay, dz = T.z[t].x + az;
-                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                            if (!(r2 <= K.four_a2)) continue;
-                            const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
-                            const EpsTerms f = eps_terms(dx, dy, dz, fmaf(K.kap, tq, rinv), fmaf(-K.two_a2, tq, rinv), q);
-                            float cn, rn;
-                            rpy_near(K, r2, rinv, cn, rn);
-                            const EpsTerms n = eps_terms(dx, dy, dz, cn, rn, q);
-                            float2 *tx = &sx[p], *ty = &sy[p], *tz = &sz[p], *ta = &sa[p], *tw = &sw[p];
-                            if (e) {
-                                tx->y += n.bx - f.bx;
-                                ty->y += n.by - f.by;
-                                tz->y += n.bz - f.bz;
-                                ta->y += n.a2 - f.a2;
-                                tw->y += n.w - f.w;
-                            } else {
-                                tx->x += n.bx - f.bx;
-                                ty->x += n.by - f.by;
-                                tz->x += n.bz - f.bz;
-                                ta->x += n.a2 - f.a2;
-                                tw->x += n.w - f.w;
-                            }
-                        }
-                    }
-                }
-            } else {
+            for (int p = 0; p < kTeaPairsI; p++) {
+                if (!(rmin[p] <= K.four_a2)) continue;
                 for (int t = sl; t < kTeaTile; t += SLICES) {
 #pragma unroll
-                    for (int h = 0; h < kTeaNI; h++) {
-                        if (j0 + t == gi[h]) continue;
-                        const float dx = T.x[t].x - pi[h].x, dy = T.y[t].x - pi[h].y, dz = T.z[t].x - pi[h].z;
-                        const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1e-6f);
+                    for (int e = 0; e < 2; e++) {
+                        if (t == self_t + kTeaLanes * (2 * p + e)) continue;
+                        const float ax = e ? nx[p].y : nx[p].x, ay = e ? ny[p].y : ny[p].x,
+                                    az = e ? nz[p].y : nz[p].x;
+                        const float dx = T.x[t].x + ax, dy = T.y[t].x + ay, dz = T.z[t].x + az;
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        if (!(r2 <= K.four_a2)) continue;
                         const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
-                        float cii = fmaf(K.kap, tq, rinv), crr = fmaf(-K.two_a2, tq, rinv);
-                        if (r2 <= K.four_a2) rpy_near(K, r2, rinv, cii, crr);
-                        const EpsTerms n = eps_terms(dx, dy, dz, cii, crr, q);
-                        const int p = h >> 1;
-                        if (h & 1) {
-                            sx[p].y += n.bx;
-                            sy[p].y += n.by;
-                            sz[p].y += n.bz;
-                            sa[p].y += n.a2;
-                            sw[p].y += n.w;
+                        const EpsTerms f = eps_terms(dx, dy, dz, fmaf(K.kap, tq, rinv), fmaf(-K.two_a2, tq, rinv), q);
+                        float cn, rn;
+                        rpy_near(K, r2, rinv, cn, rn);
+                        const EpsTerms n = eps_terms(dx, dy, dz, cn, rn, q);
+                        if (e) {
+                            sx[p].y += n.bx - f.bx;
+                            sy[p].y += n.by - f.by;
+                            sz[p].y += n.bz - f.bz;
+                            sa[p].y += n.a2 - f.a2;
+                            sw[p].y += n.w - f.w;
                         } else {
-                            sx[p].x += n.bx;
-                            sy[p].x += n.by;
-                            sz[p].x += n.bz;
-                            sa[p].x += n.a2;
-                            sw[p].x += n.w;
+                            sx[p].x += n.bx - f.bx;
+                            sy[p].x += n.by - f.by;
+                            sz[p].x += n.bz - f.bz;
+                            sa[p].x += n.a2 - f.a2;
+                            sw[p].x += n.w - f.w;
                         }
                     }
                 }
@@ -347,13 +341,51 @@ __device__ __forceinline__ float3 tea_pair1(const TeaConst &K, float dx, float d
     return make_float3(fmaf(cii, gx, s * dx), fmaf(cii, gy, s * dy), fmaf(cii, gz, s * dz));
 }
 
+// The packed pass of one tile: far-field terms of every pair (self pairs
+// pushed to r^2 = 1e30 when SELF), running minimum of r^2 per bead pair.
+template <int SLICES, bool SELF>
+__device__ __forceinline__ void tea_step_tile(const TeaTile &T, int sl, int self_t, const float2 (&nx)[kTeaPairsI],
+                                              const float2 (&ny)[kTeaPairsI], const float2 (&nz)[kTeaPairsI],
+                                              const float2 (&cbx)[kTeaPairsI], const float2 (&cby)[kTeaPairsI],
+                                              const float2 (&cbz)[kTeaPairsI], float2 vkap, float2 vn2a2,
+                                              float2 one, float2 (&ax)[kTeaPairsI], float2 (&ay)[kTeaPairsI],
+                                              float2 (&az)[kTeaPairsI], float (&rmin)[kTeaPairsI]) {
+#pragma unroll 2
+    for (int t = sl; t < kTeaTile; t += SLICES) {
+        const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+        const float2 fxj = T.fx[t], fyj = T.fy[t], fzj = T.fz[t];
+        const float2 rxj = T.rx[t], ryj = T.ry[t], rzj = T.rz[t];
+#pragma unroll
+        for (int p = 0; p < kTeaPairsI; p++) {
+            const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
+            const float2 gx = __ffma2_rn(rxj, cbx[p], fxj), gy = __ffma2_rn(ryj, cby[p], fyj),
+                         gz = __ffma2_rn(rzj, cbz[p], fzj);
+            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            if (SELF) {
+                if (t == self_t + kTeaLanes * 2 * p) r2.x = 1e30f;
+                if (t == self_t + kTeaLanes * (2 * p + 1)) r2.y = 1e30f;
+            }
+            rmin[p] = fminf(rmin[p], fminf(r2.x, r2.y));
+            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+            const float2 q = __fmul2_rn(rinv, rinv);
+            const float2 tq = __fmul2_rn(q, rinv);
+            const float2 cii = __ffma2_rn(vkap, tq, rinv);
+            const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
+            const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
+            ax[p] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax[p]));
+            ay[p] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay[p]));
+            az[p] = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az[p]));
+        }
+    }
+}
+
 // integrateTea_kernel_unlisted + integrateTea_force (src/bdhitea_kernel.cu:104-213):
 // f_i = F_i + C_i o R_i + sum_{j != i, non-extra} T_ij (F_j + beta C_i o R_j),
 // x_i += dt/gammaR f_i; angles by Euler-Maruyama from stream i + nb, which is
 // drawn for every bead.  Reads the current frame, writes the next one.  With
 // FEFF the kernel stores f_i instead and moves nothing.
 template <int SLICES, bool FEFF>
-__global__ void __launch_bounds__(kTeaLanes *SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work,
+__global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work,
                                                                  float4 *feff, const int *gate) {
     if (FEFF && gate && *gate != 0) return;
     const int2 w = work[blockIdx.x];
@@ -397,85 +429,46 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES) k_tea_step(KParams P, DevBu
         tea_tile_load<true>(T, B, j0, end);
         __syncthreads();
         if (any_act) {
+            // the tile that holds this CTA's beads: bead h of this thread sits
+            // at tile index self_t + 32 h, and its self pair gets r^2 = 1e30
+            // (a far-away term that is below the rounding of the sums)
             const bool self_tile = (w.y < j0 + kTeaTile) && (w.y + kTeaI > j0);
-            if (!self_tile) {
-                float rmin[kTeaPairsI];
+            const int self_t = self_tile ? w.y - j0 + il : -(1 << 30);
+            float rmin[kTeaPairsI];
 #pragma unroll
-                for (int p = 0; p < kTeaPairsI; p++) rmin[p] = 3.4e38f;
-#pragma unroll 2
-                for (int t = sl; t < kTeaTile; t += SLICES) {
-                    const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
-                    const float2 fxj = T.fx[t], fyj = T.fy[t], fzj = T.fz[t];
-                    const float2 rxj = T.rx[t], ryj = T.ry[t], rzj = T.rz[t];
+            for (int p = 0; p < kTeaPairsI; p++) rmin[p] = 3.4e38f;
+            if (self_tile)
+                tea_step_tile<SLICES, true>(T, sl, self_t, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az,
+                                            rmin);
+            else
+                tea_step_tile<SLICES, false>(T, sl, self_t, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az,
+                                             rmin);
+            // overlapping pairs (r <= 2a): replace the far-field term by the near one
 #pragma unroll
-                    for (int p = 0; p < kTeaPairsI; p++) {
-                        const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]),
-                                     dz = __fadd2_rn(zj, nz[p]);
-                        const float2 gx = __ffma2_rn(rxj, cbx[p], fxj), gy = __ffma2_rn(ryj, cby[p], fyj),
-                                     gz = __ffma2_rn(rzj, cbz[p], fzj);
-                        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-                        rmin[p] = fminf(rmin[p], fminf(r2.x, r2.y));
-                        const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-                        const float2 q = __fmul2_rn(rinv, rinv);
-                        const float2 tq = __fmul2_rn(q, rinv);
-                        const float2 cii = __ffma2_rn(vkap, tq, rinv);
-                        const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
-                        const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
-                        ax[p] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax[p]));
-                        ay[p] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay[p]));
-                        az[p] = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az[p]));
-                    }
-                }
-                // overlapping pairs (r <= 2a): replace the far-field term by the near one
-#pragma unroll
-                for (int p = 0; p < kTeaPairsI; p++) {
-                    if (!(rmin[p] <= K.four_a2)) continue;
-                    for (int t = sl; t < kTeaTile; t += SLICES) {
-#pragma unroll
-                        for (int e = 0; e < 2; e++) {
-                            const float dx = T.x[t].x + (e ? nx[p].y : nx[p].x),
-                                        dy = T.y[t].x + (e ? ny[p].y : ny[p].x),
-                                        dz = T.z[t].x + (e ? nz[p].y : nz[p].x);
-                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                            if (!(r2 <= K.four_a2)) continue;
-                            const float gx = fmaf(T.rx[t].x, e ? cbx[p].y : cbx[p].x, T.fx[t].x),
-                                        gy = fmaf(T.ry[t].x, e ? cby[p].y : cby[p].x, T.fy[t].x),
-                                        gz = fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fz[t].x);
-                            const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
-                            const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
-                            if (e) {
-                                ax[p].y += nr.x - fa.x;
-                                ay[p].y += nr.y - fa.y;
-                                az[p].y += nr.z - fa.z;
-                            } else {
-                                ax[p].x += nr.x - fa.x;
-                                ay[p].x += nr.y - fa.y;
-                                az[p].x += nr.z - fa.z;
-                            }
-                        }
-                    }
-                }
-            } else {
+            for (int p = 0; p < kTeaPairsI; p++) {
+                if (!(rmin[p] <= K.four_a2)) continue;
                 for (int t = sl; t < kTeaTile; t += SLICES) {
 #pragma unroll
-                    for (int h = 0; h < kTeaNI; h++) {
-                        if (j0 + t == w.y + il + h * kTeaLanes) continue;
-                        const int p = h >> 1;
-                        const bool e = h & 1;
-                        const float3 c = tea_pair1(K, T.x[t].x + (e ? nx[p].y : nx[p].x),
-                                                   T.y[t].x + (e ? ny[p].y : ny[p].x),
-                                                   T.z[t].x + (e ? nz[p].y : nz[p].x),
-                                                   fmaf(T.rx[t].x, e ? cbx[p].y : cbx[p].x, T.fx[t].x),
-                                                   fmaf(T.ry[t].x, e ? cby[p].y : cby[p].x, T.fy[t].x),
-                                                   fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fz[t].x));
+                    for (int e = 0; e < 2; e++) {
+                        if (t == self_t + kTeaLanes * (2 * p + e)) continue;
+                        const float dx = T.x[t].x + (e ? nx[p].y : nx[p].x),
+                                    dy = T.y[t].x + (e ? ny[p].y : ny[p].x),
+                                    dz = T.z[t].x + (e ? nz[p].y : nz[p].x);
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        if (!(r2 <= K.four_a2)) continue;
+                        const float gx = fmaf(T.rx[t].x, e ? cbx[p].y : cbx[p].x, T.fx[t].x),
+                                    gy = fmaf(T.ry[t].x, e ? cby[p].y : cby[p].x, T.fy[t].x),
+                                    gz = fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fz[t].x);
+                        const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+                        const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
                         if (e) {
-                            ax[p].y += c.x;
-                            ay[p].y += c.y;
-                            az[p].y += c.z;
+                            ax[p].y += nr.x - fa.x;
+                            ay[p].y += nr.y - fa.y;
+                            az[p].y += nr.z - fa.z;
                         } else {
-                            ax[p].x += c.x;
-                            ay[p].x += c.y;
-                            az[p].x += c.z;
+                            ax[p].x += nr.x - fa.x;
+                            ay[p].x += nr.y - fa.y;
+                            az[p].x += nr.z - fa.z;
                         }
                     }
                 }
