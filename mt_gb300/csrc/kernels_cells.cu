@@ -172,71 +172,92 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
     int lo_buf[kCellMaxLong], la_buf[kCellMaxLat];
     int nlj = 0, nlo = 0, nla = 0;
     bool overflow = false;
-    // the 27 buckets and their ranges, all lookups issued before any is used
-    int bk[27], st[27], ct[27];
+    // the 27 buckets (in shared memory for the rolled cell loop), a mask of
+    // the cells whose bucket an earlier cell already has, and each cell's
+    // range fetched while the previous cell runs
+    __shared__ int s_bk[27][kTile];
+    uint32_t dup = 0;
+    {
+        int bk[27];
 #pragma unroll
-    for (int c = 0; c < 27; c++) bk[c] = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
+        for (int c = 0; c < 27; c++) {
+            bk[c] = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
+            s_bk[c][threadIdx.x] = bk[c];
+        }
 #pragma unroll
-    for (int c = 0; c < 27; c++) {
-        st[c] = start[bk[c]];
-        ct[c] = cnt[bk[c]];
+        for (int c = 1; c < 27; c++) {
+            bool seen = false;
+#pragma unroll
+            for (int v = 0; v < c; v++) seen |= (bk[v] == bk[c]);
+            dup |= (seen ? 1u : 0u) << c;
+        }
     }
+    int st_next = start[s_bk[0][threadIdx.x]], ct_next = cnt[s_bk[0][threadIdx.x]];
     for (int c = 0; c < 27; c++) {
-        if (ct[c] == 0) continue;
-        const int bkt = bk[c];
-        bool seen = false;   // two cells hashed to one bucket: visit it once
-        for (int v = 0; v < c; v++) seen |= (bk[v] == bkt);
-        if (seen) continue;
-        const int s0 = base + st[c], s1 = s0 + ct[c];
-        for (int s = s0; s < s1; s++) {
-            const float4 q = cell_pos[s];
-            const int jg = __float_as_int(q.w) & kCellIndexMask;
-            const int jl = jg - base;
-            const float cd = centre_dist(pi, q);
-            if (do_lj && jl != il && cd < P.ljcut) {
-                if (nlj >= P.maxLJ) {
-                    overflow = true;
-                } else if (nlj < kLocalLJ) {
-                    lj_buf[nlj] = jl;
-                } else {
-                    if (nlj == kLocalLJ)  // spill the local part first
-                        for (int k = 0; k < kLocalLJ; k++) B.lj[k * nb + g] = lj_buf[k];
-                    B.lj[nlj * nb + g] = jl;
-                }
-                nlj++;
-            }
-            if (do_pairs && cd < kPairReach && jl != hpart) {
-                const float4 pj = fr[jg];   // the exact state (q carries the index in w)
-                const float rmon = h0 < 0 ? -2.0f : 2.0f;
-                const int fj = B.flags[jg];
-                if (((flags ^ fj) & kFlagBeta) != 0) {
-                    const float4 ui = fr[nb + g], uj = fr[nb + jg];
-                    const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
-                    if (norm3_rn(site_delta(pi, pj, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) <
-                        2.5f) {
-                        if (nlo < P.maxLong)
-                            lo_buf[nlo] = jl;
-                        else
-                            overflow = true;
-                        nlo++;
+        const int st_c = st_next, ct_c = ct_next;
+        if (c + 1 < 27) {
+            const int b = s_bk[c + 1][threadIdx.x];
+            st_next = start[b];
+            ct_next = cnt[b];
+        }
+        if (((dup >> c) & 1u) || ct_c == 0) continue;
+        const int s0 = base + st_c, s1 = s0 + ct_c;
+        for (int s4 = s0; s4 < s1; s4 += 4) {
+            float4 qq[4];   // four candidates in flight
+#pragma unroll
+            for (int u = 0; u < 4; u++) qq[u] = s4 + u < s1 ? cell_pos[s4 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (s4 + u >= s1) break;
+                const float4 q = qq[u];
+                const int jg = __float_as_int(q.w) & kCellIndexMask;
+                const int jl = jg - base;
+                const float cd = centre_dist(pi, q);
+                if (do_lj && jl != il && cd < P.ljcut) {
+                    if (nlj >= P.maxLJ) {
+                        overflow = true;
+                    } else if (nlj < kLocalLJ) {
+                        lj_buf[nlj] = jl;
+                    } else {
+                        if (nlj == kLocalLJ)  // spill the local part first
+                            for (int k = 0; k < kLocalLJ; k++) B.lj[k * nb + g] = lj_buf[k];
+                        B.lj[nlj * nb + g] = jl;
                     }
+                    nlj++;
                 }
-                if (jl != il) {
-                    const float4 li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
-                    const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
-                    if (norm3_rn(site_delta(pi, pj, f3(li1), f3(l2))) < 2.5f) {
-                        if (nla < P.maxLat)
-                            la_buf[nla] = 2 * jl;       // orientation 0 -> -j
-                        else
-                            overflow = true;
-                        nla++;
+                if (do_pairs && cd < kPairReach && jl != hpart) {
+                    const float4 pj = fr[jg];   // the exact state (q carries the index in w)
+                    const float rmon = h0 < 0 ? -2.0f : 2.0f;
+                    const int fj = B.flags[jg];
+                    if (((flags ^ fj) & kFlagBeta) != 0) {
+                        const float4 ui = fr[nb + g], uj = fr[nb + jg];
+                        const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
+                        if (norm3_rn(site_delta(pi, pj, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) <
+                            2.5f) {
+                            if (nlo < P.maxLong)
+                                lo_buf[nlo] = jl;
+                            else
+                                overflow = true;
+                            nlo++;
+                        }
                     }
-                    if (norm3_rn(site_delta(pi, pj, f3(li2), f3(l1))) < 2.5f) {
-                        if (nla < P.maxLat)
-                            la_buf[nla] = 2 * jl + 1;   // orientation 1 -> +j
-                        else
-                            overflow = true;
-                        nla++;
+                    if (jl != il) {
+                        const float4 li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
+                        const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
+                        if (norm3_rn(site_delta(pi, pj, f3(li1), f3(l2))) < 2.5f) {
+                            if (nla < P.maxLat)
+                                la_buf[nla] = 2 * jl;       // orientation 0 -> -j
+                            else
+                                overflow = true;
+                            nla++;
+                        }
+                        if (norm3_rn(site_delta(pi, pj, f3(li2), f3(l1))) < 2.5f) {
+                            if (nla < P.maxLat)
+                                la_buf[nla] = 2 * jl + 1;   // orientation 1 -> +j
+                            else
+                                overflow = true;
+                            nla++;
+                        }
                     }
                 }
             }

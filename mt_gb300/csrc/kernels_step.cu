@@ -52,10 +52,23 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
     const float3 uzi = f3(Fi.p1);
     const bool off_tub = (flags & kFlagOnTubule) == 0;
 
-    // harmonic bond inside the dimer (:69-182)
+    // Every list count and the first entries of every list are requested
+    // before any is used (entries past a count are in bounds and ignored):
+    // the dependent chain index -> neighbour state starts for all lists at once.
     const int hc = (flags >> kHarmShift) & 7;
+    const int nl = P.maxLong > 0 ? B.lonc[g] : 0;
+    const int nt = P.maxLat > 0 ? B.latc[g] : 0;
+    const int nlj = P.lj_on ? B.ljc[g] : 0;
+    const int e_h0 = B.harm[g * P.maxH];
+    const int e_l0 = P.maxLong > 0 ? B.lon[g] : 0;
+    const int e_t0 = P.maxLat > 0 ? B.lat[g] : 0;
+    int jj0[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) jj0[u] = (P.lj_on && u < P.maxLJ) ? B.lj[u * nb + g] : 0;
+
+    // harmonic bond inside the dimer (:69-182)
     for (int k = 0; k < hc; k++) {
-        const int e = B.harm[g * P.maxH + k];
+        const int e = k == 0 ? e_h0 : B.harm[g * P.maxH + k];
         const float rmon = e < 0 ? 2.0f : -2.0f;
         const int pj = base + (e < 0 ? -e : e);
         const float4 rj = fr[pj], uj = fr[nb + pj];
@@ -71,9 +84,8 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         }
     }
     // Morse longitudinal (:187-301)
-    const int nl = B.lonc[g];
     for (int k = 0; k < nl; k++) {
-        const int e = B.lon[k * nb + g];
+        const int e = k == 0 ? e_l0 : B.lon[k * nb + g];
         const float rmon = e < 0 ? 2.0f : -2.0f;
         const int pj = base + (e < 0 ? -e : e);
         const float4 rj = fr[pj], uj = fr[nb + pj];
@@ -98,9 +110,8 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         }
     }
     // Morse lateral (:303-467)
-    const int nt = B.latc[g];
     for (int k = 0; k < nt; k++) {
-        const int e = B.lat[k * nb + g];
+        const int e = k == 0 ? e_t0 : B.lat[k * nb + g];
         const bool neg = e <= 0;
         int j = e < 0 ? -e : e;
         if (j == kZeroCode) j = 0;
@@ -121,12 +132,12 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
     if (P.lj_on) {
         // four neighbours per round: their indices, then their positions, are
         // all in flight before the first is used
-        const int n = B.ljc[g];
-        for (int k0 = 0; k0 < n; k0 += 4) {
+        for (int k0 = 0; k0 < nlj; k0 += 4) {
             int jj[4];
             float4 rj[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) jj[u] = k0 + u < n ? B.lj[(k0 + u) * nb + g] : -1;
+            for (int u = 0; u < 4; u++)
+                jj[u] = k0 + u < nlj ? (k0 == 0 ? jj0[u] : B.lj[(k0 + u) * nb + g]) : -1;
 #pragma unroll
             for (int u = 0; u < 4; u++) rj[u] = jj[u] >= 0 ? fr[base + jj[u]] : Fi.p0;
 #pragma unroll

@@ -462,6 +462,12 @@ class Surrogate:
             self.lib.mtg_surrogate_destroy(self.h)
             self.h = None
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     def __del__(self):
         try:
             self.close()
