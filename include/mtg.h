@@ -369,12 +369,16 @@ int mtg_surrogate_status(mtg_engine *e, int *fell_back, int *rechecks, double *l
 /* Launch shapes of the engine's kernels.  list_method as
  * mtg_set_list_method (1 tiles, 2 cells); step_block: threads per CTA of the
  * fused plain step (64, 128, 256); tea_slices: threads per bead in the
- * all-pairs TEA kernels (1, 2, 4, 8).  No reference counterpart (the
- * reference launches everything with 32-thread blocks, src/mt.h:34). */
+ * all-pairs TEA kernels (1, 2, 4, 8); tea_jparts: parts the j range of a
+ * trajectory is split into (1, 2, 3, 4: more CTAs, so the last wave of a
+ * launch is fuller; the parts' sums meet in a second kernel).  No reference
+ * counterpart (the reference launches everything with 32-thread blocks,
+ * src/mt.h:34). */
 typedef struct {
     int list_method;
     int step_block;
     int tea_slices;
+    int tea_jparts;
 } mtg_tuning;
 int mtg_get_tuning(mtg_engine *e, mtg_tuning *t);
 int mtg_set_tuning(mtg_engine *e, const mtg_tuning *t);

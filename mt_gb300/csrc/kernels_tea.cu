@@ -97,6 +97,25 @@ __device__ __forceinline__ EpsTerms eps_terms(float dx, float dy, float dz, floa
     return {bc * dx * dx, bc * dy * dy, bc * dz * dz, cii * cii, fmaf(crq * us, us, 3.0f * cii)};
 }
 
+// Range of beads j of part `part` of `parts` of a trajectory [base, end):
+// whole tiles, the parts as equal as the tile count allows.
+__device__ __forceinline__ void tea_jrange(int base, int end, int part, int parts, int &jb, int &je) {
+    const int ntiles = (end - base + kTeaTile - 1) / kTeaTile;
+    const int per = (ntiles + parts - 1) / parts;
+    jb = min(end, base + part * per * kTeaTile);
+    je = min(end, base + (part + 1) * per * kTeaTile);
+}
+
+// Stores the epsilon-pass result of bead g from its scaled sums
+// (x, y, z: row sums of squares; w: sum of all entries).
+__device__ __forceinline__ void eps_store(const KParams &P, const DevBuffers &B, int g, bool active, float4 acc,
+                                          const TeaConst &K) {
+    const float c2 = K.c075a * K.c075a;
+    if (!active) acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    B.tea_ci[g] = make_float4(acc.x * c2, acc.y * c2, acc.z * c2, 0.f);
+    B.tea_eps[g] = acc.w * K.c075a;
+}
+
 // The packed pass of one tile of the epsilon pass (self pairs pushed to
 // r^2 = 1e30 when SELF), running minimum of r^2 per bead pair.
 template <int SLICES, bool SELF>
@@ -140,12 +159,15 @@ __device__ __forceinline__ void tea_eps_tile(const TeaTile &T, int sl, int self_
 // and of all nine entries (-> tea_eps).  With T = cii I + crr u u^T the row
 // sums of squares are cii^2 + (2 cii + crr) crr u_c^2 and the sum of all
 // entries is 3 cii + crr (u_x + u_y + u_z)^2.
-template <int SLICES>
+template <int SLICES, bool SPLIT>
 __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work,
                                                                 const int *gate, int run_if) {
     if (gate && *gate != run_if) return;
-    const int2 w = work[blockIdx.x];
+    const int part = SPLIT ? (int)(blockIdx.x % P.tea_jparts) : 0;
+    const int2 w = work[SPLIT ? blockIdx.x / P.tea_jparts : blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
+    int jb, je;
+    tea_jrange(base, end, part, SPLIT ? P.tea_jparts : 1, jb, je);
     const int il = threadIdx.x % kTeaLanes, sl = threadIdx.x / kTeaLanes;
     __shared__ TeaTile T;
     __shared__ float4 s_red[kTeaI * SLICES];
@@ -175,7 +197,7 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KPar
     }
     const TeaConst K = tea_const(P.tea_a);
     const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), two = f2(2.0f), three = f2(3.0f);
-    for (int j0 = base; j0 < end; j0 += kTeaTile) {
+    for (int j0 = jb; j0 < je; j0 += kTeaTile) {
         tea_tile_load<false>(T, B, j0, end);
         __syncthreads();
         if (any_act) {
@@ -239,7 +261,6 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KPar
     }
     __syncthreads();
     if (sl != 0) return;
-    const float c2 = K.c075a * K.c075a;
 #pragma unroll
     for (int h = 0; h < kTeaNI; h++) {
         if (gi[h] >= end) continue;
@@ -251,10 +272,27 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KPar
             acc.z += v.z;
             acc.w += v.w;
         }
-        if (!act[h]) acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        B.tea_ci[gi[h]] = make_float4(acc.x * c2, acc.y * c2, acc.z * c2, 0.f);
-        B.tea_eps[gi[h]] = acc.w * K.c075a;
+        if (SPLIT)
+            B.tea_part[(size_t)part * P.nb + gi[h]] = acc;
+        else
+            eps_store(P, B, gi[h], act[h], acc, K);
     }
+}
+
+// Sums of the parts of a split epsilon pass.
+__global__ void k_tea_eps_finish(KParams P, DevBuffers B, const int *gate, int run_if) {
+    if (gate && *gate != run_if) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= P.nb) return;
+    float4 acc = B.tea_part[g];
+    for (int k = 1; k < P.tea_jparts; k++) {
+        const float4 v = B.tea_part[(size_t)k * P.nb + g];
+        acc.x += v.x;
+        acc.y += v.y;
+        acc.z += v.z;
+        acc.w += v.w;
+    }
+    eps_store(P, B, g, (B.flags[g] & kFlagExtra) == 0, acc, tea_const(P.tea_a));
 }
 
 // updateTea's reduction (src/bdhitea.cu:75-116), in FP64 on the device: one
@@ -379,17 +417,54 @@ __device__ __forceinline__ void tea_step_tile(const TeaTile &T, int sl, int self
     }
 }
 
+// The update of bead g from its scaled mobility sums (sx, sy, sz): back to
+// units of D_ii, plus the bead's own term F_i + C_i o R_i; FEFF stores f_i.
+template <bool FEFF>
+__device__ __forceinline__ void tea_bead_update(const KParams &P, const DevBuffers &B, int g, float sx, float sy,
+                                                float sz, float b2, const TeaConst &K, float4 *feff) {
+    const int nb = P.nb;
+    const float4 ci = B.tea_ci[g], Fi = B.force[g], Ri = B.tea_r[g];
+    sx = fmaf(K.c075a, sx, Fi.x + Ri.x * (1.0f / sqrtf(1.0f + b2 * ci.x)));
+    sy = fmaf(K.c075a, sy, Fi.y + Ri.y * (1.0f / sqrtf(1.0f + b2 * ci.y)));
+    sz = fmaf(K.c075a, sz, Fi.z + Ri.z * (1.0f / sqrtf(1.0f + b2 * ci.z)));
+    if (FEFF) {
+        feff[g] = make_float4(sx, sy, sz, 0.f);
+        return;
+    }
+    const int flags = B.flags[g];
+    Frame Fr;
+    Fr.p0 = B.frame_in[g];
+    Fr.p1 = B.frame_in[nb + g];
+    Fr.p2 = B.frame_in[2 * nb + g];
+    Fr.p3 = B.frame_in[3 * nb + g];
+    uint4 s2 = B.seeds[nb + g];
+    const float4 ga = gauss4(s2);
+    B.seeds[nb + g] = s2;
+    if (!(flags & (kFlagExtra | kFlagFixed))) {
+        const float4 fa = B.force[nb + g];  // (ffi, ftheta, fpsi)
+        const float x = Fr.p0.x + P.kr * sx, y = Fr.p0.y + P.kr * sy, z = Fr.p0.z + P.kr * sz;
+        const float fi = Fr.p0.w + (P.kfi * fa.x + P.nfi * ga.x);
+        const float psi = Fr.p1.w + (P.kfi * fa.z + P.nfi * ga.y);
+        const float th = Fr.p2.w + (P.kth * fa.y + P.varTheta * ga.z);
+        Fr = make_frame(P, x, y, z, fi, th, psi);
+    }
+    store_frame(B.frame_out, nb, g, Fr);
+}
+
 // integrateTea_kernel_unlisted + integrateTea_force (src/bdhitea_kernel.cu:104-213):
 // f_i = F_i + C_i o R_i + sum_{j != i, non-extra} T_ij (F_j + beta C_i o R_j),
 // x_i += dt/gammaR f_i; angles by Euler-Maruyama from stream i + nb, which is
 // drawn for every bead.  Reads the current frame, writes the next one.  With
 // FEFF the kernel stores f_i instead and moves nothing.
-template <int SLICES, bool FEFF>
+template <int SLICES, bool FEFF, bool SPLIT>
 __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work,
                                                                  float4 *feff, const int *gate) {
     if (FEFF && gate && *gate != 0) return;
-    const int2 w = work[blockIdx.x];
+    const int part = SPLIT ? (int)(blockIdx.x % P.tea_jparts) : 0;
+    const int2 w = work[SPLIT ? blockIdx.x / P.tea_jparts : blockIdx.x];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
+    int jb, je;
+    tea_jrange(base, end, part, SPLIT ? P.tea_jparts : 1, jb, je);
     const int il = threadIdx.x % kTeaLanes, sl = threadIdx.x / kTeaLanes;
     const int nb = P.nb;
     __shared__ TeaTile T;
@@ -425,7 +500,7 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KPa
     for (int p = 0; p < kTeaPairsI; p++) ax[p] = ay[p] = az[p] = f2(0.f);
     const TeaConst K = tea_const(P.tea_a);
     const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
-    for (int j0 = base; j0 < end; j0 += kTeaTile) {
+    for (int j0 = jb; j0 < je; j0 += kTeaTile) {
         tea_tile_load<true>(T, B, j0, end);
         __syncthreads();
         if (any_act) {
@@ -496,44 +571,49 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KPa
             sy += v.y;
             sz += v.z;
         }
-        // back to units of D_ii, plus the bead's own term F_i + C_i o R_i
-        const float4 ci = B.tea_ci[g], Fi = B.force[g], Ri = B.tea_r[g];
-        sx = fmaf(K.c075a, sx, Fi.x + Ri.x * (1.0f / sqrtf(1.0f + b2 * ci.x)));
-        sy = fmaf(K.c075a, sy, Fi.y + Ri.y * (1.0f / sqrtf(1.0f + b2 * ci.y)));
-        sz = fmaf(K.c075a, sz, Fi.z + Ri.z * (1.0f / sqrtf(1.0f + b2 * ci.z)));
-        if (FEFF) {
-            feff[g] = make_float4(sx, sy, sz, 0.f);
-            continue;
-        }
-        const int flags = B.flags[g];
-        Frame Fr;
-        Fr.p0 = B.frame_in[g];
-        Fr.p1 = B.frame_in[nb + g];
-        Fr.p2 = B.frame_in[2 * nb + g];
-        Fr.p3 = B.frame_in[3 * nb + g];
-        uint4 s2 = B.seeds[nb + g];
-        const float4 ga = gauss4(s2);
-        B.seeds[nb + g] = s2;
-        if (!(flags & (kFlagExtra | kFlagFixed))) {
-            const float4 fa = B.force[nb + g];  // (ffi, ftheta, fpsi)
-            const float x = Fr.p0.x + P.kr * sx, y = Fr.p0.y + P.kr * sy, z = Fr.p0.z + P.kr * sz;
-            const float fi = Fr.p0.w + (P.kfi * fa.x + P.nfi * ga.x);
-            const float psi = Fr.p1.w + (P.kfi * fa.z + P.nfi * ga.y);
-            const float th = Fr.p2.w + (P.kth * fa.y + P.varTheta * ga.z);
-            Fr = make_frame(P, x, y, z, fi, th, psi);
-        }
-        store_frame(B.frame_out, nb, g, Fr);
+        if (SPLIT)
+            B.tea_part[(size_t)part * nb + g] = make_float4(sx, sy, sz, 0.f);
+        else
+            tea_bead_update<FEFF>(P, B, g, sx, sy, sz, b2, K, feff);
     }
+}
+
+// Sums of the parts of a split mobility product, then the bead's update.
+template <bool FEFF>
+__global__ void k_tea_step_finish(KParams P, DevBuffers B, float4 *feff, const int *gate) {
+    if (FEFF && gate && *gate != 0) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= P.nb) return;
+    float4 acc = B.tea_part[g];
+    for (int k = 1; k < P.tea_jparts; k++) {
+        const float4 v = B.tea_part[(size_t)k * P.nb + g];
+        acc.x += v.x;
+        acc.y += v.y;
+        acc.z += v.z;
+    }
+    const float beta = B.tea_beta[B.traj[g]];
+    tea_bead_update<FEFF>(P, B, g, acc.x, acc.y, acc.z, beta * beta, tea_const(P.tea_a), feff);
 }
 
 void launch_tea_eps_gated(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
                           int run_if, cudaStream_t s) {
     const int t = kTeaLanes * P.tea_slices;
+    if (P.tea_jparts > 1) {
+        const int grid = nwork * P.tea_jparts;
+        switch (P.tea_slices) {
+            case 1: k_tea_eps<1, true><<<grid, t, 0, s>>>(P, B, work, gate, run_if); break;
+            case 2: k_tea_eps<2, true><<<grid, t, 0, s>>>(P, B, work, gate, run_if); break;
+            case 4: k_tea_eps<4, true><<<grid, t, 0, s>>>(P, B, work, gate, run_if); break;
+            default: k_tea_eps<8, true><<<grid, t, 0, s>>>(P, B, work, gate, run_if); break;
+        }
+        k_tea_eps_finish<<<(P.nb + 255) / 256, 256, 0, s>>>(P, B, gate, run_if);
+        return;
+    }
     switch (P.tea_slices) {
-        case 1: k_tea_eps<1><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
-        case 2: k_tea_eps<2><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
-        case 4: k_tea_eps<4><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
-        default: k_tea_eps<8><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
+        case 1: k_tea_eps<1, false><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
+        case 2: k_tea_eps<2, false><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
+        case 4: k_tea_eps<4, false><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
+        default: k_tea_eps<8, false><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
     }
 }
 void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
@@ -550,11 +630,22 @@ template <bool FEFF>
 static void tea_step_dispatch(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, float4 *feff,
                               const int *gate, cudaStream_t s) {
     const int t = kTeaLanes * P.tea_slices;
+    if (P.tea_jparts > 1) {
+        const int grid = nwork * P.tea_jparts;
+        switch (P.tea_slices) {
+            case 1: k_tea_step<1, FEFF, true><<<grid, t, 0, s>>>(P, B, work, feff, gate); break;
+            case 2: k_tea_step<2, FEFF, true><<<grid, t, 0, s>>>(P, B, work, feff, gate); break;
+            case 4: k_tea_step<4, FEFF, true><<<grid, t, 0, s>>>(P, B, work, feff, gate); break;
+            default: k_tea_step<8, FEFF, true><<<grid, t, 0, s>>>(P, B, work, feff, gate); break;
+        }
+        k_tea_step_finish<FEFF><<<(P.nb + 255) / 256, 256, 0, s>>>(P, B, feff, gate);
+        return;
+    }
     switch (P.tea_slices) {
-        case 1: k_tea_step<1, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
-        case 2: k_tea_step<2, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
-        case 4: k_tea_step<4, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
-        default: k_tea_step<8, FEFF><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
+        case 1: k_tea_step<1, FEFF, false><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
+        case 2: k_tea_step<2, FEFF, false><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
+        case 4: k_tea_step<4, FEFF, false><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
+        default: k_tea_step<8, FEFF, false><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
     }
 }
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {

@@ -422,6 +422,7 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
         int sl = 1;
         while (sl < 8 && (double)nb / 4 * sl < target) sl <<= 1;   // four beads per thread
         e->kp.tea_slices = sl;
+        e->kp.tea_jparts = 1;
     }
 
 #define ALLOC(ptr, n)                         \
@@ -465,6 +466,7 @@ int mtg_create_batch(const mtg_params *p, const mtg_batch_topology *t, mtg_engin
         ALLOC(e->tea_eps, nb);
         ALLOC(e->tea_beta, nt);
         ALLOC(e->tea_eps_t, nt);
+        ALLOC(e->tea_part, (size_t)kTeaMaxParts * nb);
     }
     // spatial-hash tables of the cell-list rebuild
     std::vector<int> tbase(nt + 1, 0), tmask(nt, 0);
@@ -624,7 +626,8 @@ int mtg_destroy(mtg_engine *e) {
                     e->cell_key, e->cell_bead, e->cell_pos, e->cell_cnt, e->cell_start, e->cell_cursor, e->tea_work,
                     e->surr_desc, e->surr_pred, e->surr_stats, e->surr_gate, e->surr_err, e->surr_part,
                     e->tea_ci2, e->feff_a, e->feff_b, e->tea_eps2, e->tea_beta2, e->tea_eps_t2,
-                    e->hydro_cand, e->hydro_rank, e->hydro_sums, e->hydro_counts, e->hydro_events};
+                    e->hydro_cand, e->hydro_rank, e->hydro_sums, e->hydro_counts, e->hydro_events,
+                    e->tea_part};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (e->stage_host) cudaFreeHost(e->stage_host);
@@ -914,6 +917,7 @@ int mtg_get_tuning(mtg_engine *e, mtg_tuning *t) {
     t->list_method = e->use_cells ? 2 : 1;
     t->step_block = e->kp.step_block;
     t->tea_slices = e->kp.tea_slices;
+    t->tea_jparts = e->kp.tea_jparts;
     return MTG_OK;
 }
 
@@ -923,10 +927,12 @@ int mtg_set_tuning(mtg_engine *e, const mtg_tuning *t) {
         return fail(MTG_E_CONFIG, "step_block must be 64, 128 or 256");
     if (t->tea_slices != 1 && t->tea_slices != 2 && t->tea_slices != 4 && t->tea_slices != 8)
         return fail(MTG_E_CONFIG, "tea_slices must be 1, 2, 4 or 8");
+    if (t->tea_jparts < 1 || t->tea_jparts > kTeaMaxParts) return fail(MTG_E_CONFIG, "tea_jparts must be 1..4");
     int rc = mtg_set_list_method(e, t->list_method);
     if (rc) return rc;
     e->kp.step_block = t->step_block;
     e->kp.tea_slices = t->tea_slices;
+    e->kp.tea_jparts = t->tea_jparts;
     destroy_graphs(e);
     return MTG_OK;
 }
@@ -952,9 +958,10 @@ int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tunin
         if (lm == 2 && (!cells_ok || !lists)) continue;
         if (lm == 1 && !lists && !cands.empty()) continue;
         if (e->p.hdi_on) {
-            for (int sl : {1, 2, 4, 8}) cands.push_back({lm, orig.step_block, sl});
+            for (int sl : {1, 2, 4, 8})
+                for (int jp = 1; jp <= kTeaMaxParts; jp++) cands.push_back({lm, orig.step_block, sl, jp});
         } else {
-            for (int bs : {64, 128, 256}) cands.push_back({lm, bs, orig.tea_slices});
+            for (int bs : {64, 128, 256}) cands.push_back({lm, bs, orig.tea_slices, orig.tea_jparts});
         }
     }
     float best_t = 3.4e38f;

@@ -37,6 +37,7 @@ struct mtg_engine {
     float4 *tea_r = nullptr, *tea_ci = nullptr;
     float *tea_eps = nullptr, *tea_beta = nullptr;
     double *tea_eps_t = nullptr;
+    float4 *tea_part = nullptr;    // kTeaMaxParts * nb partial sums (split TEA kernels)
     float *stage = nullptr;        // 7*nb floats for host <-> device Coord transfers
     void *stage_host = nullptr;    // pinned mirror of stage
     uint8_t *stage_u8 = nullptr;
@@ -115,6 +116,7 @@ struct mtg_engine {
         b.latc = latc;
         b.lat = lat;
         b.err = err;
+        b.tea_part = tea_part;
         b.tea_r = tea_r;
         b.tea_ci = tea_ci;
         b.tea_eps = tea_eps;

@@ -61,6 +61,7 @@ struct KParams {
     // TEA
     float tea_a, tea_var;
     int tea_slices;        // threads per bead i in the all-pairs TEA kernels (1, 2, 4 or 8)
+    int tea_jparts;        // parts of a trajectory's j range (1..kTeaMaxParts), summed by a second kernel
     int step_block;        // threads per CTA of the fused plain step (64, 128 or 256)
 };
 
@@ -83,6 +84,7 @@ struct DevBuffers {
     float *tea_eps;        // per-bead epsilon sums
     float *tea_beta;       // [nt]
     double *tea_eps_t;     // [nt]
+    float4 *tea_part;      // [kTeaMaxParts][nb] partial sums of the split all-pairs kernels
 };
 
 // ------------------------------------------------------------------ RNG
@@ -248,6 +250,7 @@ void launch_energy_totals(const KParams &P, const double *partials, const int *w
                           int *err, cudaStream_t s);
 // TEA kernels run over their own work list: chunks of kTeaChunk beads.
 constexpr int kTeaChunk = 128;
+constexpr int kTeaMaxParts = 4;
 void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);
 void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s);
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s);

@@ -385,10 +385,11 @@ class Engine:
     def tuning(self) -> dict:
         t = MtgTuning()
         check(self.lib.mtg_get_tuning(self.h, C.byref(t)))
-        return {"list_method": t.list_method, "step_block": t.step_block, "tea_slices": t.tea_slices}
+        return {"list_method": t.list_method, "step_block": t.step_block, "tea_slices": t.tea_slices,
+                "tea_jparts": t.tea_jparts}
 
-    def set_tuning(self, list_method: int, step_block: int, tea_slices: int):
-        t = MtgTuning(list_method, step_block, tea_slices)
+    def set_tuning(self, list_method: int, step_block: int, tea_slices: int, tea_jparts: int = 1):
+        t = MtgTuning(list_method, step_block, tea_slices, tea_jparts)
         check(self.lib.mtg_set_tuning(self.h, C.byref(t)))
 
     def autotune(self, first_step: int, trial_steps: int, cache: str | None = None, key: str | None = None):
@@ -406,7 +407,8 @@ class Engine:
         t = MtgTuning()
         ms = C.c_float()
         check(self.lib.mtg_autotune(self.h, C.c_longlong(first_step), trial_steps, C.byref(t), C.byref(ms)))
-        entry = {"tuning": {"list_method": t.list_method, "step_block": t.step_block, "tea_slices": t.tea_slices},
+        entry = {"tuning": {"list_method": t.list_method, "step_block": t.step_block, "tea_slices": t.tea_slices,
+                            "tea_jparts": t.tea_jparts},
                  "trial_ms": ms.value, "cached": False}
         if cache and key:
             try:

@@ -312,3 +312,23 @@ def test_restart_rejects_other_systems_and_corruption(engine_mod, tmp_path):
     with pytest.raises(engine_mod.MtgError):
         e.read_restart(str(bad))
     e.close()
+
+
+def test_tea_split_j_range_matches(engine_mod):
+    """Splitting each trajectory's j range over several CTAs (tea_jparts)
+    changes only the summation order of the all-pairs kernels."""
+    b = system_with_margin(seed=44, tea=True, tea_epsilon_freq=2, n_free=300)
+    ref = None
+    for jp in (1, 2, 3, 4):
+        e = make_engine(engine_mod, b)
+        t = e.tuning()
+        e.set_tuning(t["list_method"], t["step_block"], 2, jp)
+        e.step(0, 4)
+        x = e.download_state()
+        rng = e.download_rng()
+        if ref is None:
+            ref = (x, rng)
+        else:
+            assert np.array_equal(rng, ref[1])
+            np.testing.assert_allclose(x[:, :6], ref[0][:, :6], rtol=0, atol=2e-5)
+        e.close()
