@@ -342,7 +342,7 @@ int mtg_surrogate_destroy(mtg_surrogate *s);
 int mtg_surrogate_get_params(mtg_surrogate *s, float *params, float *norm);
 int mtg_surrogate_set_params(mtg_surrogate *s, const float *params, const float *norm);
 /* Fits the normalisation to (X [n*32] raw features, T [n*4] targets), then
- * trains with Adam (mini-batches of `batch`, a multiple of 128; samples
+ * trains with Adam (mini-batches of `batch`, a multiple of 32; samples
  * shuffled per epoch with `seed`).  loss_per_epoch [epochs] (may be NULL):
  * mean squared error in normalised target units. */
 int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n, int epochs, int batch, float lr,

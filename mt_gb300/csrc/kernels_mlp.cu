@@ -2,7 +2,7 @@
 // with SiLU activations, BF16 weights and activations, FP32 accumulation on
 // the tensor cores, trained with Adam on FP32 master weights.
 //
-// One CTA handles 128 samples; each of its 8 warps owns 16 rows and keeps
+// One CTA handles kRows samples; each of its warps owns 16 rows and keeps
 // them through all layers, so layers need no CTA barrier.  Weights live in
 // shared memory, K-contiguous and padded by 8 elements per row so that the
 // fragment loads of the m16n8k16 MMA are bank-conflict free.
@@ -23,8 +23,8 @@ namespace mlp {
 
 namespace {
 
-constexpr int kRows = 128;   // samples per CTA
-constexpr int kWarps = 8;
+constexpr int kRows = 32;    // samples per CTA (a 4096-sample batch spreads over 128 CTAs)
+constexpr int kWarps = kRows / 16;
 constexpr int kPadIn = kIn + 8;    // 40
 constexpr int kPadH = kHid + 8;    // 136
 constexpr int kPadRows = kRows + 8;
@@ -82,6 +82,16 @@ __device__ __forceinline__ void warp_gemm(float (&acc)[NT][4], const __nv_bfloat
     }
 }
 
+// Copies a [rows][cols] BF16 matrix (row-major, cols a multiple of 8) into
+// shared memory rows of ld elements, 16 bytes per thread and step.
+__device__ __forceinline__ void stage_rows(__nv_bfloat16 *dst, int ld, const __nv_bfloat16 *src, int rows, int cols) {
+    const int vpr = cols / 8;
+    for (int i = threadIdx.x; i < rows * vpr; i += blockDim.x) {
+        const int r = i / vpr, c = (i % vpr) * 8;
+        *reinterpret_cast<uint4 *>(dst + r * ld + c) = *reinterpret_cast<const uint4 *>(src + (size_t)r * cols + c);
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- forward
@@ -101,11 +111,9 @@ __global__ void __launch_bounds__(kRows * 2) k_mlp_forward(const Weights W, cons
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int row0 = blockIdx.x * kRows;
     // weights (BF16, N-major) and biases
-    for (int i = tid; i < kHid * kIn; i += blockDim.x) sW1[(i / kIn) * kPadIn + i % kIn] = W.w1[i];
-    for (int i = tid; i < kHid * kHid; i += blockDim.x) {
-        sW2[(i / kHid) * kPadH + i % kHid] = W.w2[i];
-        sW3[(i / kHid) * kPadH + i % kHid] = W.w3[i];
-    }
+    stage_rows(sW1, kPadIn, W.w1, kHid, kIn);
+    stage_rows(sW2, kPadH, W.w2, kHid, kHid);
+    stage_rows(sW3, kPadH, W.w3, kHid, kHid);
     for (int i = tid; i < 8 * kHid; i += blockDim.x)
         sW4[(i / kHid) * kPadH + i % kHid] = (i / kHid) < kOut ? W.w4[i] : __float2bfloat16(0.f);
     for (int i = tid; i < 3 * kHid; i += blockDim.x) sb[i] = W.b[i];
@@ -192,10 +200,8 @@ __global__ void __launch_bounds__(kRows * 2) k_mlp_backward(const Weights W, con
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int row0 = blockIdx.x * kRows;
     const float scale = 2.0f / ((float)n * kOut);
-    for (int i = tid; i < kHid * kHid; i += blockDim.x) {
-        sW2t[(i / kHid) * kPadH + i % kHid] = W.w2t[i];
-        sW3t[(i / kHid) * kPadH + i % kHid] = W.w3t[i];
-    }
+    stage_rows(sW2t, kPadH, W.w2t, kHid, kHid);
+    stage_rows(sW3t, kPadH, W.w3t, kHid, kHid);
     for (int i = tid; i < kHid * 24; i += blockDim.x) {
         const int in = i / 24, o = i % 24;
         sW4t[i] = o < kOut ? W.w4t[in * kOut + o] : __float2bfloat16(0.f);

@@ -510,7 +510,7 @@ int mtg_surrogate_loss_grad(mtg_surrogate *s, const float *X, const float *T, in
 int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n, int epochs, int batch, float lr,
                         int seed, float *loss_per_epoch) {
     if (!s || !X || !T || n <= 0 || epochs <= 0 || batch <= 0) return sfail(MTG_E_CONFIG, "bad arguments");
-    if (batch % mlp::rows_per_cta() != 0) return sfail(MTG_E_CONFIG, "batch must be a multiple of 128");
+    if (batch % mlp::rows_per_cta() != 0) return sfail(MTG_E_CONFIG, "batch must be a multiple of the rows per CTA (32)");
     SCK(cudaSetDevice(s->device));
     // normalisation
     for (int k = 0; k < mlp::kIn; k++) {
