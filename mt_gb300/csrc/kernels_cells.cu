@@ -139,6 +139,7 @@ constexpr int kLocalLJ = 64;   // LJ hits sorted in local memory; more are sorte
 // Thread per bead: candidates are read from the bucket-ordered position copy
 // (one contiguous 16 B load each); the rare assembly candidates (< 6.6 nm)
 // also read the neighbour's site planes.
+template <bool PAIRS>
 __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B, const int2 *work, const int *tbase,
                                                          const int *tmask, const int *start, const int *cnt,
                                                          const float4 *cell_pos, float inv_cell) {
@@ -151,10 +152,10 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
     const int flags = B.flags[g];
     const bool extra_i = (flags & kFlagExtra) != 0;
     const bool do_lj = P.lj_on && !extra_i;
-    const bool do_pairs = P.is_assembly && !extra_i;
+    const bool do_pairs = PAIRS && P.is_assembly && !extra_i;
     if (!do_lj && !do_pairs) {
         if (P.lj_on) B.ljc[g] = 0;
-        if (P.is_assembly) {
+        if (PAIRS && P.is_assembly) {
             B.lonc[g] = 0;
             B.latc[g] = 0;
         }
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
         }
         B.ljc[g] = n;
     }
-    if (P.is_assembly) {
+    if (PAIRS && P.is_assembly) {
         const int n1 = min(nlo, P.maxLong), n2 = min(nla, P.maxLat);
         isort(lo_buf, n1);
         isort(la_buf, n2);
@@ -286,6 +287,80 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
         B.lonc[g] = n1;
         B.latc[g] = n2;
     }
+    if (overflow) atomicOr(B.err, kErrOverflow);
+}
+
+// Longitudinal and lateral lists (pairs_kernel, src/compute_cuda.cu:527-674)
+// from the bead's LJ list: every assembly candidate (centre distance below
+// kPairReach) is in the LJ list when the LJ cutoff is longer, and the LJ list
+// is in ascending j, so the lists come out in the reference's order without a
+// sort.  Runs after k_cell_lists<false>.
+__global__ void __launch_bounds__(kTile) k_pairs_from_lj(KParams P, DevBuffers B) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= P.nb) return;
+    const int nb = P.nb;
+    const int flags = B.flags[g];
+    if (flags & kFlagExtra) {
+        B.lonc[g] = 0;
+        B.latc[g] = 0;
+        return;
+    }
+    const float4 *fr = B.frame_in;
+    const int base = B.off[B.traj[g]], il = g - base;
+    const float4 pi = fr[g], ui = fr[nb + g], li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
+    const int h0 = B.harm[g * P.maxH];
+    const int hpart = h0 < 0 ? -h0 : h0;
+    const float rmon = h0 < 0 ? -2.0f : 2.0f;
+    const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
+    const int n = min(B.ljc[g], P.maxLJ);
+    int nlo = 0, nla = 0;
+    bool overflow = false;
+    for (int k0 = 0; k0 < n; k0 += 4) {
+        int jj[4];
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u < n ? B.lj[(k0 + u) * nb + g] : -1;
+#pragma unroll
+        for (int u = 0; u < 4; u++) q[u] = jj[u] >= 0 ? fr[base + jj[u]] : pi;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int jl = jj[u];
+            if (jl < 0 || jl == hpart || !(centre_dist(pi, q[u]) < kPairReach)) continue;
+            const int jg = base + jl;
+            const float4 pj = q[u];
+            const int fj = B.flags[jg];
+            if (((flags ^ fj) & kFlagBeta) != 0) {
+                const float4 uj = fr[nb + jg];
+                if (norm3_rn(site_delta(pi, pj, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) < 2.5f) {
+                    if (nlo < P.maxLong)
+                        B.lon[nlo * nb + g] = h0 < 0 ? jl : -jl;
+                    else
+                        overflow = true;
+                    nlo++;
+                }
+            }
+            if (jl != il) {
+                const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
+                const int code = jl != 0 ? jl : kZeroCode;
+                if (norm3_rn(site_delta(pi, pj, f3(li1), f3(l2))) < 2.5f) {
+                    if (nla < P.maxLat)
+                        B.lat[nla * nb + g] = -code;   // orientation 0 -> -j
+                    else
+                        overflow = true;
+                    nla++;
+                }
+                if (norm3_rn(site_delta(pi, pj, f3(li2), f3(l1))) < 2.5f) {
+                    if (nla < P.maxLat)
+                        B.lat[nla * nb + g] = code;    // orientation 1 -> +j
+                    else
+                        overflow = true;
+                    nla++;
+                }
+            }
+        }
+    }
+    B.lonc[g] = min(nlo, P.maxLong);
+    B.latc[g] = min(nla, P.maxLat);
     if (overflow) atomicOr(B.err, kErrOverflow);
 }
 
@@ -313,7 +388,13 @@ void launch_rebuild_cells(const KParams &P, const DevBuffers &B, const CellBuffe
                           cudaStream_t s) {
     const float reach = fmaxf(P.lj_on ? P.ljcut : 0.f, P.is_assembly ? kPairReach : 0.f);
     const float inv = bin_beads(P, B, C, reach, false, s);   // the lists are sorted afterwards
-    k_cell_lists<<<nwork, kTile, 0, s>>>(P, B, work, C.tbase, C.tmask, C.start, C.cnt, C.cell_pos, inv);
+    if (P.is_assembly && P.lj_on && P.ljcut >= kPairReach) {
+        // LJ lists from the cells, then the assembly lists from the LJ lists
+        k_cell_lists<false><<<nwork, kTile, 0, s>>>(P, B, work, C.tbase, C.tmask, C.start, C.cnt, C.cell_pos, inv);
+        k_pairs_from_lj<<<nblk(P.nb, kTile), kTile, 0, s>>>(P, B);
+    } else {
+        k_cell_lists<true><<<nwork, kTile, 0, s>>>(P, B, work, C.tbase, C.tmask, C.start, C.cnt, C.cell_pos, inv);
+    }
 }
 
 }  // namespace mtg
