@@ -42,3 +42,31 @@ def test_async_dcd_and_energy_output(engine_mod, tmp_path, capfd):
         assert open(xyz[t], "rb").read() == expect[t][0]
         assert open(ang[t], "rb").read() == expect[t][1]
     assert printed == lines
+
+
+def test_dcd_frames_read_back_for_reanalysis(engine_mod, tmp_path):
+    """The written frames read back (mt_gb300.dcd) as the states of those
+    steps, and their energies re-evaluated on the GPU match the run's."""
+    from mt_gb300 import dcd
+    b = small_system(seed=52, ntr=2)
+    stride, frames = 4, 3
+    xyz = [str(tmp_path / f"x{t}.dcd") for t in range(b.ntraj)]
+    ang = [str(tmp_path / f"a{t}.dcd") for t in range(b.ntraj)]
+    e = engine_mod.Engine(b)
+    e.upload_state(b.coords)
+    e.output_open(xyz, ang, frames, 1, stride, 100.0, "REMARKS TEST", energy_path=str(tmp_path / "en.txt"))
+    states, energies = [], []
+    for k in range(frames):
+        e.step(k * stride, stride)
+        e.output_frame((k + 1) * stride)
+        states.append(e.download_state())
+        e.rebuild_pairs()
+        energies.append(e.energies())
+    e.output_close()
+    back = list(dcd.read_batch(xyz, ang))
+    assert len(back) == frames
+    for k in range(frames):
+        np.testing.assert_array_equal(back[k][:, :6], states[k][:, :6])
+    again = dcd.analyse(e, xyz, ang)
+    np.testing.assert_allclose(again, np.array(energies), rtol=1e-12, atol=1e-9)
+    e.close()
