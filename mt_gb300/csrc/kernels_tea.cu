@@ -25,7 +25,7 @@ constexpr int kTeaPairsI = kTeaNI / 2;      // packed pairs of them
 constexpr int kTeaLanes = 32;               // threads per slice
 constexpr int kTeaI = kTeaChunk;            // beads i per CTA
 static_assert(kTeaI == kTeaLanes * kTeaNI, "chunk = lanes x beads per thread");
-constexpr int kTeaTile = 256;               // beads j per tile
+constexpr int kTeaTile = 128;               // beads j per tile
 constexpr float kFarAway = 1.0e18f;         // position of padding and extra beads j
 
 // Tile of the all-pairs kernels, every value duplicated into both lanes.
