@@ -66,6 +66,17 @@ cudaError_t launch_loss_sum(const float *part, int nparts, float *out, cudaStrea
 cudaError_t prepare_tc();
 cudaError_t launch_infer_tc(const Weights &W, const float *X, int n, const float *norm, float *Y, int *err,
                             cudaStream_t s);
+// Training on the tcgen05 tensor cores: the forward pass with the
+// pre-activations Z [n][3][kHid] (rows of X gathered through idx, may be
+// NULL), and the backward pass (kernels_mlp_train_tc.cu) writing per-CTA
+// partial gradients G [backward_parts(n)][kParams] and loss sums.
+cudaError_t launch_forward_tc(const Weights &W, const float *X, const int *idx, int n, const float *norm, float *Y,
+                              float *Z, int *err, cudaStream_t s);
+cudaError_t prepare_backward_tc();
+int backward_parts(int n);
+cudaError_t launch_backward_tc(const Weights &W, const float *X, const int *idx, const float *norm, const float *T,
+                               int n, const float *Y, const float *Z, float *G, float *loss_part, int *err,
+                               cudaStream_t s);
 
 }  // namespace mlp
 }  // namespace mtg

@@ -471,7 +471,7 @@ int mtg_surrogate_predict(mtg_surrogate *s, const float *X, int n, float *Y) {
 int mtg_surrogate_loss_grad(mtg_surrogate *s, const float *X, const float *T, int n, double *loss, float *grad) {
     if (!s || !X || !T || n <= 0) return sfail(MTG_E_CONFIG, "bad arguments");
     SCK(cudaSetDevice(s->device));
-    const int parts = (n + mlp::rows_per_cta() - 1) / mlp::rows_per_cta();
+    const int parts = mlp::backward_parts(n);
     std::vector<float> Tn((size_t)n * mlp::kOut);
     for (int i = 0; i < n; i++)
         for (int k = 0; k < mlp::kOut; k++)
@@ -485,12 +485,19 @@ int mtg_surrogate_loss_grad(mtg_surrogate *s, const float *X, const float *T, in
     SCK(cudaMalloc(&dL, sizeof(float) * parts));
     SCK(cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * mlp::kIn, cudaMemcpyHostToDevice, s->stream));
     SCK(cudaMemcpyAsync(dT, Tn.data(), sizeof(float) * Tn.size(), cudaMemcpyHostToDevice, s->stream));
-    SCK(mlp::launch_forward(s->W, dX, nullptr, n, s->norm, dY, dZ, s->stream));
-    SCK(mlp::launch_backward(s->W, dX, nullptr, s->norm, dT, n, dY, dZ, dG, dL, s->stream));
+    SCK(mlp::launch_forward_tc(s->W, dX, nullptr, n, s->norm, dY, dZ, s->err, s->stream));
+    SCK(mlp::launch_backward_tc(s->W, dX, nullptr, s->norm, dT, n, dY, dZ, dG, dL, s->err, s->stream));
     std::vector<float> G((size_t)parts * mlp::kParams), L(parts);
+    int herr = 0;
     SCK(cudaMemcpyAsync(G.data(), dG, sizeof(float) * G.size(), cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaMemcpyAsync(L.data(), dL, sizeof(float) * parts, cudaMemcpyDeviceToHost, s->stream));
+    SCK(cudaMemcpyAsync(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaStreamSynchronize(s->stream));
+    if (herr) {
+        for (float *p : {dX, dT, dY, dZ, dG, dL}) cudaFree(p);
+        cudaMemsetAsync(s->err, 0, sizeof(int), s->stream);
+        return sfail(MTG_E_TIMEOUT, "a bounded wait for the tensor cores ran out");
+    }
     for (float *p : {dX, dT, dY, dZ, dG, dL}) cudaFree(p);
     double l = 0.0;
     for (float v : L) l += v;
@@ -510,7 +517,7 @@ int mtg_surrogate_loss_grad(mtg_surrogate *s, const float *X, const float *T, in
 int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n, int epochs, int batch, float lr,
                         int seed, float *loss_per_epoch) {
     if (!s || !X || !T || n <= 0 || epochs <= 0 || batch <= 0) return sfail(MTG_E_CONFIG, "bad arguments");
-    if (batch % mlp::rows_per_cta() != 0) return sfail(MTG_E_CONFIG, "batch must be a multiple of the rows per CTA (32)");
+    if (batch % 32 != 0) return sfail(MTG_E_CONFIG, "batch must be a multiple of 32");
     SCK(cudaSetDevice(s->device));
     // normalisation
     for (int k = 0; k < mlp::kIn; k++) {
@@ -542,7 +549,7 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
     }
     int rc = upload_norms(s);
     if (rc) return rc;
-    const int parts = batch / mlp::rows_per_cta();
+    const int parts = mlp::backward_parts(batch);
     const int nbatches = n / batch;
     if (nbatches == 0) return sfail(MTG_E_CONFIG, "fewer samples than one batch");
     float *dX, *dT, *dY, *dZ, *dG, *dL, *dLsum;
@@ -565,8 +572,9 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
         SCK(cudaMemcpyAsync(dIdx, perm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
         for (int b = 0; b < nbatches; b++) {
             const int *idx = dIdx + (size_t)b * batch;
-            SCK(mlp::launch_forward(s->W, dX, idx, batch, s->norm, dY, dZ, s->stream));
-            SCK(mlp::launch_backward(s->W, dX, idx, s->norm, dT, batch, dY, dZ, dG, dL + (size_t)b * parts, s->stream));
+            SCK(mlp::launch_forward_tc(s->W, dX, idx, batch, s->norm, dY, dZ, s->err, s->stream));
+            SCK(mlp::launch_backward_tc(s->W, dX, idx, s->norm, dT, batch, dY, dZ, dG, dL + (size_t)b * parts, s->err,
+                                        s->stream));
             SCK(mlp::launch_adam(s->W, dG, parts, lr, ++s->adam_step, s->stream));
         }
         SCK(mlp::launch_loss_sum(dL, parts * nbatches, dLsum + ep, s->stream));
@@ -575,10 +583,16 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
         SCK(cudaStreamSynchronize(s->stream));
     }
     std::vector<float> ls(epochs);
+    int herr = 0;
     SCK(cudaMemcpyAsync(ls.data(), dLsum, sizeof(float) * epochs, cudaMemcpyDeviceToHost, s->stream));
+    SCK(cudaMemcpyAsync(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaStreamSynchronize(s->stream));
     for (float *p : {dX, dT, dY, dZ, dG, dL, dLsum}) cudaFree(p);
     cudaFree(dIdx);
+    if (herr) {
+        cudaMemsetAsync(s->err, 0, sizeof(int), s->stream);
+        return sfail(MTG_E_TIMEOUT, "a bounded wait for the tensor cores ran out");
+    }
     if (loss_per_epoch)
         for (int ep = 0; ep < epochs; ep++) loss_per_epoch[ep] = ls[ep] / ((float)nbatches * batch * mlp::kOut);
     return MTG_OK;
