@@ -47,16 +47,6 @@ __device__ __forceinline__ void refresh_one(const Weights &W, int i, float w) {
     }
 }
 
-int rows_per_cta();
-// Raises the kernels' dynamic shared-memory limits (once per device, before
-// any launch or stream capture).
-cudaError_t prepare();
-// norm (may be NULL): [kIn] means then [kIn] inverse standard deviations of
-// the raw features in X.
-cudaError_t launch_forward(const Weights &W, const float *X, const int *idx, int n, const float *norm, float *Y,
-                           float *Z, cudaStream_t s);
-cudaError_t launch_backward(const Weights &W, const float *X, const int *idx, const float *norm, const float *T, int n,
-                            const float *Y, const float *Z, float *G, float *loss_part, cudaStream_t s);
 cudaError_t launch_adam(const Weights &W, const float *G, int nparts, float lr, int step, cudaStream_t s);
 cudaError_t launch_refresh(const Weights &W, cudaStream_t s);
 cudaError_t launch_loss_sum(const float *part, int nparts, float *out, cudaStream_t s);

@@ -350,7 +350,6 @@ int mtg_surrogate_create(int device, int seed, mtg_surrogate **out) {
     if (!out) return sfail(MTG_E_CONFIG, "out is NULL");
     *out = nullptr;
     SCK(cudaSetDevice(device));
-    SCK(mlp::prepare());
     SCK(mlp::prepare_tc());
     auto *s = new mtg_surrogate();
     s->device = device;
