@@ -23,6 +23,7 @@ namespace mtg {
 constexpr int kTeaNI = 4;                   // beads i per thread
 constexpr int kTeaPairsI = kTeaNI / 2;      // packed pairs of them
 constexpr int kTeaLanes = 32;               // threads per slice
+constexpr int kTeaSeg = 4;                  // segments of a thread's j values, each with its own r^2 minimum
 constexpr int kTeaI = kTeaChunk;            // beads i per CTA
 static_assert(kTeaI == kTeaLanes * kTeaNI, "chunk = lanes x beads per thread");
 constexpr int kTeaTile = 128;               // beads j per tile
@@ -106,6 +107,28 @@ __device__ __forceinline__ void tea_jrange(int base, int end, int part, int part
     je = min(end, base + (part + 1) * per * kTeaTile);
 }
 
+// Work item and j part of this CTA.  The first P.tea_nhead items run whole;
+// with SPLIT every later item runs as P.tea_jparts CTAs over parts of its j
+// range, so that the last waves of a launch are made of short CTAs.
+template <bool SPLIT>
+__device__ __forceinline__ void tea_item(const KParams &P, int &item, int &part, int &parts) {
+    item = (int)blockIdx.x;
+    part = 0;
+    parts = 1;
+    if (SPLIT && item >= P.tea_nhead) {
+        const int k = item - P.tea_nhead;
+        item = P.tea_nhead + k / P.tea_jparts;
+        part = k % P.tea_jparts;
+        parts = P.tea_jparts;
+    }
+}
+// Bead of a finish kernel (one CTA of kTeaChunk threads per split item), or -1.
+__device__ __forceinline__ int tea_tail_bead(const KParams &P, const DevBuffers &B, const int2 *work) {
+    const int2 w = work[P.tea_nhead + blockIdx.x];
+    const int g = w.y + (int)threadIdx.x;
+    return g < B.off[w.x + 1] ? g : -1;
+}
+
 // Stores the epsilon-pass result of bead g from its scaled sums
 // (x, y, z: row sums of squares; w: sum of all entries).
 __device__ __forceinline__ void eps_store(const KParams &P, const DevBuffers &B, int g, bool active, float4 acc,
@@ -124,32 +147,37 @@ __device__ __forceinline__ void tea_eps_tile(const TeaTile &T, int sl, int self_
                                              float2 vkap, float2 vn2a2, float2 two, float2 three,
                                              float2 (&sx)[kTeaPairsI], float2 (&sy)[kTeaPairsI],
                                              float2 (&sz)[kTeaPairsI], float2 (&sa)[kTeaPairsI],
-                                             float2 (&sw)[kTeaPairsI], float (&rmin)[kTeaPairsI]) {
-#pragma unroll 2
-    for (int t = sl; t < kTeaTile; t += SLICES) {
-        const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+                                             float2 (&sw)[kTeaPairsI], float (&rmin)[kTeaPairsI][kTeaSeg]) {
+    constexpr int kLen = kTeaTile / SLICES / kTeaSeg;
 #pragma unroll
-        for (int p = 0; p < kTeaPairsI; p++) {
-            const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
-            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-            if (SELF) {
-                if (t == self_t + kTeaLanes * 2 * p) r2.x = 1e30f;
-                if (t == self_t + kTeaLanes * (2 * p + 1)) r2.y = 1e30f;
+    for (int sg = 0; sg < kTeaSeg; sg++) {
+#pragma unroll 2
+        for (int k = 0; k < kLen; k++) {
+            const int t = sl + (sg * kLen + k) * SLICES;
+            const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+#pragma unroll
+            for (int p = 0; p < kTeaPairsI; p++) {
+                const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
+                float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                if (SELF) {
+                    if (t == self_t + kTeaLanes * 2 * p) r2.x = 1e30f;
+                    if (t == self_t + kTeaLanes * (2 * p + 1)) r2.y = 1e30f;
+                }
+                rmin[p][sg] = fmin3(rmin[p][sg], r2.x, r2.y);
+                const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+                const float2 q = __fmul2_rn(rinv, rinv);
+                const float2 tq = __fmul2_rn(q, rinv);
+                const float2 cii = __ffma2_rn(vkap, tq, rinv);
+                const float2 crr = __ffma2_rn(vn2a2, tq, rinv);
+                const float2 crq = __fmul2_rn(crr, q);
+                const float2 bc = __fmul2_rn(__ffma2_rn(two, cii, crr), crq);
+                sa[p] = __ffma2_rn(cii, cii, sa[p]);
+                sx[p] = __ffma2_rn(__fmul2_rn(bc, dx), dx, sx[p]);
+                sy[p] = __ffma2_rn(__fmul2_rn(bc, dy), dy, sy[p]);
+                sz[p] = __ffma2_rn(__fmul2_rn(bc, dz), dz, sz[p]);
+                const float2 us = __fadd2_rn(__fadd2_rn(dx, dy), dz);
+                sw[p] = __ffma2_rn(__fmul2_rn(crq, us), us, __ffma2_rn(three, cii, sw[p]));
             }
-            rmin[p] = fminf(rmin[p], fminf(r2.x, r2.y));
-            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-            const float2 q = __fmul2_rn(rinv, rinv);
-            const float2 tq = __fmul2_rn(q, rinv);
-            const float2 cii = __ffma2_rn(vkap, tq, rinv);
-            const float2 crr = __ffma2_rn(vn2a2, tq, rinv);
-            const float2 crq = __fmul2_rn(crr, q);
-            const float2 bc = __fmul2_rn(__ffma2_rn(two, cii, crr), crq);
-            sa[p] = __ffma2_rn(cii, cii, sa[p]);
-            sx[p] = __ffma2_rn(__fmul2_rn(bc, dx), dx, sx[p]);
-            sy[p] = __ffma2_rn(__fmul2_rn(bc, dy), dy, sy[p]);
-            sz[p] = __ffma2_rn(__fmul2_rn(bc, dz), dz, sz[p]);
-            const float2 us = __fadd2_rn(__fadd2_rn(dx, dy), dz);
-            sw[p] = __ffma2_rn(__fmul2_rn(crq, us), us, __ffma2_rn(three, cii, sw[p]));
         }
     }
 }
@@ -163,11 +191,12 @@ template <int SLICES, bool SPLIT>
 __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KParams P, DevBuffers B, const int2 *work,
                                                                 const int *gate, int run_if) {
     if (gate && *gate != run_if) return;
-    const int part = SPLIT ? (int)(blockIdx.x % P.tea_jparts) : 0;
-    const int2 w = work[SPLIT ? blockIdx.x / P.tea_jparts : blockIdx.x];
+    int item, part, parts;
+    tea_item<SPLIT>(P, item, part, parts);
+    const int2 w = work[item];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
     int jb, je;
-    tea_jrange(base, end, part, SPLIT ? P.tea_jparts : 1, jb, je);
+    tea_jrange(base, end, part, parts, jb, je);
     const int il = threadIdx.x % kTeaLanes, sl = threadIdx.x / kTeaLanes;
     __shared__ TeaTile T;
     __shared__ float4 s_red[kTeaI * SLICES];
@@ -204,9 +233,11 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KPar
             // self pairs: as in k_tea_step
             const bool self_tile = (w.y < j0 + kTeaTile) && (w.y + kTeaI > j0);
             const int self_t = self_tile ? w.y - j0 + il : -(1 << 30);
-            float rmin[kTeaPairsI];
+            float rmin[kTeaPairsI][kTeaSeg];
 #pragma unroll
-            for (int p = 0; p < kTeaPairsI; p++) rmin[p] = 3.4e38f;
+            for (int p = 0; p < kTeaPairsI; p++)
+#pragma unroll
+                for (int sg = 0; sg < kTeaSeg; sg++) rmin[p][sg] = 3.4e38f;
             if (self_tile)
                 tea_eps_tile<SLICES, true>(T, sl, self_t, nx, ny, nz, vkap, vn2a2, two, three, sx, sy, sz, sa, sw,
                                            rmin);
@@ -216,33 +247,41 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KPar
             // overlapping pairs (r <= 2a): replace the far-field terms by the near ones
 #pragma unroll
             for (int p = 0; p < kTeaPairsI; p++) {
-                if (!(rmin[p] <= K.four_a2)) continue;
-                for (int t = sl; t < kTeaTile; t += SLICES) {
+                unsigned segs = 0;
 #pragma unroll
-                    for (int e = 0; e < 2; e++) {
-                        if (t == self_t + kTeaLanes * (2 * p + e)) continue;
-                        const float ax = e ? nx[p].y : nx[p].x, ay = e ? ny[p].y : ny[p].x,
-                                    az = e ? nz[p].y : nz[p].x;
-                        const float dx = T.x[t].x + ax, dy = T.y[t].x + ay, dz = T.z[t].x + az;
-                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        if (!(r2 <= K.four_a2)) continue;
-                        const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
-                        const EpsTerms f = eps_terms(dx, dy, dz, fmaf(K.kap, tq, rinv), fmaf(-K.two_a2, tq, rinv), q);
-                        float cn, rn;
-                        rpy_near(K, r2, rinv, cn, rn);
-                        const EpsTerms n = eps_terms(dx, dy, dz, cn, rn, q);
-                        if (e) {
-                            sx[p].y += n.bx - f.bx;
-                            sy[p].y += n.by - f.by;
-                            sz[p].y += n.bz - f.bz;
-                            sa[p].y += n.a2 - f.a2;
-                            sw[p].y += n.w - f.w;
-                        } else {
-                            sx[p].x += n.bx - f.bx;
-                            sy[p].x += n.by - f.by;
-                            sz[p].x += n.bz - f.bz;
-                            sa[p].x += n.a2 - f.a2;
-                            sw[p].x += n.w - f.w;
+                for (int sg = 0; sg < kTeaSeg; sg++) segs |= (rmin[p][sg] <= K.four_a2 ? 1u : 0u) << sg;
+                constexpr int kLen = kTeaTile / SLICES / kTeaSeg;
+                while (segs) {  // the segments that hold an overlapping pair
+                    const int sg = __ffs(segs) - 1;
+                    segs &= segs - 1;
+                    for (int k = 0; k < kLen; k++) {
+                        const int t = sl + (sg * kLen + k) * SLICES;
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            if (t == self_t + kTeaLanes * (2 * p + e)) continue;
+                            const float ax = e ? nx[p].y : nx[p].x, ay = e ? ny[p].y : ny[p].x,
+                                        az = e ? nz[p].y : nz[p].x;
+                            const float dx = T.x[t].x + ax, dy = T.y[t].x + ay, dz = T.z[t].x + az;
+                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                            if (!(r2 <= K.four_a2)) continue;
+                            const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
+                            const EpsTerms f = eps_terms(dx, dy, dz, fmaf(K.kap, tq, rinv), fmaf(-K.two_a2, tq, rinv), q);
+                            float cn, rn;
+                            rpy_near(K, r2, rinv, cn, rn);
+                            const EpsTerms n = eps_terms(dx, dy, dz, cn, rn, q);
+                            if (e) {
+                                sx[p].y += n.bx - f.bx;
+                                sy[p].y += n.by - f.by;
+                                sz[p].y += n.bz - f.bz;
+                                sa[p].y += n.a2 - f.a2;
+                                sw[p].y += n.w - f.w;
+                            } else {
+                                sx[p].x += n.bx - f.bx;
+                                sy[p].x += n.by - f.by;
+                                sz[p].x += n.bz - f.bz;
+                                sa[p].x += n.a2 - f.a2;
+                                sw[p].x += n.w - f.w;
+                            }
                         }
                     }
                 }
@@ -272,7 +311,7 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KPar
             acc.z += v.z;
             acc.w += v.w;
         }
-        if (SPLIT)
+        if (SPLIT && parts > 1)
             B.tea_part[(size_t)part * P.nb + gi[h]] = acc;
         else
             eps_store(P, B, gi[h], act[h], acc, K);
@@ -280,10 +319,10 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KPar
 }
 
 // Sums of the parts of a split epsilon pass.
-__global__ void k_tea_eps_finish(KParams P, DevBuffers B, const int *gate, int run_if) {
+__global__ void k_tea_eps_finish(KParams P, DevBuffers B, const int2 *work, const int *gate, int run_if) {
     if (gate && *gate != run_if) return;
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= P.nb) return;
+    const int g = tea_tail_bead(P, B, work);
+    if (g < 0) return;
     float4 acc = B.tea_part[g];
     for (int k = 1; k < P.tea_jparts; k++) {
         const float4 v = B.tea_part[(size_t)k * P.nb + g];
@@ -387,32 +426,37 @@ __device__ __forceinline__ void tea_step_tile(const TeaTile &T, int sl, int self
                                               const float2 (&cbx)[kTeaPairsI], const float2 (&cby)[kTeaPairsI],
                                               const float2 (&cbz)[kTeaPairsI], float2 vkap, float2 vn2a2,
                                               float2 one, float2 (&ax)[kTeaPairsI], float2 (&ay)[kTeaPairsI],
-                                              float2 (&az)[kTeaPairsI], float (&rmin)[kTeaPairsI]) {
-#pragma unroll 2
-    for (int t = sl; t < kTeaTile; t += SLICES) {
-        const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
-        const float2 fxj = T.fx[t], fyj = T.fy[t], fzj = T.fz[t];
-        const float2 rxj = T.rx[t], ryj = T.ry[t], rzj = T.rz[t];
+                                              float2 (&az)[kTeaPairsI], float (&rmin)[kTeaPairsI][kTeaSeg]) {
+    constexpr int kLen = kTeaTile / SLICES / kTeaSeg;
 #pragma unroll
-        for (int p = 0; p < kTeaPairsI; p++) {
-            const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
-            const float2 gx = __ffma2_rn(rxj, cbx[p], fxj), gy = __ffma2_rn(ryj, cby[p], fyj),
-                         gz = __ffma2_rn(rzj, cbz[p], fzj);
-            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-            if (SELF) {
-                if (t == self_t + kTeaLanes * 2 * p) r2.x = 1e30f;
-                if (t == self_t + kTeaLanes * (2 * p + 1)) r2.y = 1e30f;
+    for (int sg = 0; sg < kTeaSeg; sg++) {
+#pragma unroll 2
+        for (int k = 0; k < kLen; k++) {
+            const int t = sl + (sg * kLen + k) * SLICES;
+            const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+            const float2 fxj = T.fx[t], fyj = T.fy[t], fzj = T.fz[t];
+            const float2 rxj = T.rx[t], ryj = T.ry[t], rzj = T.rz[t];
+#pragma unroll
+            for (int p = 0; p < kTeaPairsI; p++) {
+                const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
+                const float2 gx = __ffma2_rn(rxj, cbx[p], fxj), gy = __ffma2_rn(ryj, cby[p], fyj),
+                             gz = __ffma2_rn(rzj, cbz[p], fzj);
+                float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                if (SELF) {
+                    if (t == self_t + kTeaLanes * 2 * p) r2.x = 1e30f;
+                    if (t == self_t + kTeaLanes * (2 * p + 1)) r2.y = 1e30f;
+                }
+                rmin[p][sg] = fmin3(rmin[p][sg], r2.x, r2.y);
+                const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+                const float2 q = __fmul2_rn(rinv, rinv);
+                const float2 tq = __fmul2_rn(q, rinv);
+                const float2 cii = __ffma2_rn(vkap, tq, rinv);
+                const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
+                const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
+                ax[p] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax[p]));
+                ay[p] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay[p]));
+                az[p] = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az[p]));
             }
-            rmin[p] = fminf(rmin[p], fminf(r2.x, r2.y));
-            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-            const float2 q = __fmul2_rn(rinv, rinv);
-            const float2 tq = __fmul2_rn(q, rinv);
-            const float2 cii = __ffma2_rn(vkap, tq, rinv);
-            const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
-            const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
-            ax[p] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax[p]));
-            ay[p] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay[p]));
-            az[p] = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az[p]));
         }
     }
 }
@@ -460,11 +504,12 @@ template <int SLICES, bool FEFF, bool SPLIT>
 __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work,
                                                                  float4 *feff, const int *gate) {
     if (FEFF && gate && *gate != 0) return;
-    const int part = SPLIT ? (int)(blockIdx.x % P.tea_jparts) : 0;
-    const int2 w = work[SPLIT ? blockIdx.x / P.tea_jparts : blockIdx.x];
+    int item, part, parts;
+    tea_item<SPLIT>(P, item, part, parts);
+    const int2 w = work[item];
     const int traj = w.x, base = B.off[traj], end = B.off[traj + 1];
     int jb, je;
-    tea_jrange(base, end, part, SPLIT ? P.tea_jparts : 1, jb, je);
+    tea_jrange(base, end, part, parts, jb, je);
     const int il = threadIdx.x % kTeaLanes, sl = threadIdx.x / kTeaLanes;
     const int nb = P.nb;
     __shared__ TeaTile T;
@@ -509,9 +554,11 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KPa
             // (a far-away term that is below the rounding of the sums)
             const bool self_tile = (w.y < j0 + kTeaTile) && (w.y + kTeaI > j0);
             const int self_t = self_tile ? w.y - j0 + il : -(1 << 30);
-            float rmin[kTeaPairsI];
+            float rmin[kTeaPairsI][kTeaSeg];
 #pragma unroll
-            for (int p = 0; p < kTeaPairsI; p++) rmin[p] = 3.4e38f;
+            for (int p = 0; p < kTeaPairsI; p++)
+#pragma unroll
+                for (int sg = 0; sg < kTeaSeg; sg++) rmin[p][sg] = 3.4e38f;
             if (self_tile)
                 tea_step_tile<SLICES, true>(T, sl, self_t, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az,
                                             rmin);
@@ -521,29 +568,37 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KPa
             // overlapping pairs (r <= 2a): replace the far-field term by the near one
 #pragma unroll
             for (int p = 0; p < kTeaPairsI; p++) {
-                if (!(rmin[p] <= K.four_a2)) continue;
-                for (int t = sl; t < kTeaTile; t += SLICES) {
+                unsigned segs = 0;
 #pragma unroll
-                    for (int e = 0; e < 2; e++) {
-                        if (t == self_t + kTeaLanes * (2 * p + e)) continue;
-                        const float dx = T.x[t].x + (e ? nx[p].y : nx[p].x),
-                                    dy = T.y[t].x + (e ? ny[p].y : ny[p].x),
-                                    dz = T.z[t].x + (e ? nz[p].y : nz[p].x);
-                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        if (!(r2 <= K.four_a2)) continue;
-                        const float gx = fmaf(T.rx[t].x, e ? cbx[p].y : cbx[p].x, T.fx[t].x),
-                                    gy = fmaf(T.ry[t].x, e ? cby[p].y : cby[p].x, T.fy[t].x),
-                                    gz = fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fz[t].x);
-                        const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
-                        const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
-                        if (e) {
-                            ax[p].y += nr.x - fa.x;
-                            ay[p].y += nr.y - fa.y;
-                            az[p].y += nr.z - fa.z;
-                        } else {
-                            ax[p].x += nr.x - fa.x;
-                            ay[p].x += nr.y - fa.y;
-                            az[p].x += nr.z - fa.z;
+                for (int sg = 0; sg < kTeaSeg; sg++) segs |= (rmin[p][sg] <= K.four_a2 ? 1u : 0u) << sg;
+                constexpr int kLen = kTeaTile / SLICES / kTeaSeg;
+                while (segs) {  // the segments that hold an overlapping pair
+                    const int sg = __ffs(segs) - 1;
+                    segs &= segs - 1;
+                    for (int k = 0; k < kLen; k++) {
+                        const int t = sl + (sg * kLen + k) * SLICES;
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            if (t == self_t + kTeaLanes * (2 * p + e)) continue;
+                            const float dx = T.x[t].x + (e ? nx[p].y : nx[p].x),
+                                        dy = T.y[t].x + (e ? ny[p].y : ny[p].x),
+                                        dz = T.z[t].x + (e ? nz[p].y : nz[p].x);
+                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                            if (!(r2 <= K.four_a2)) continue;
+                            const float gx = fmaf(T.rx[t].x, e ? cbx[p].y : cbx[p].x, T.fx[t].x),
+                                        gy = fmaf(T.ry[t].x, e ? cby[p].y : cby[p].x, T.fy[t].x),
+                                        gz = fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fz[t].x);
+                            const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+                            const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
+                            if (e) {
+                                ax[p].y += nr.x - fa.x;
+                                ay[p].y += nr.y - fa.y;
+                                az[p].y += nr.z - fa.z;
+                            } else {
+                                ax[p].x += nr.x - fa.x;
+                                ay[p].x += nr.y - fa.y;
+                                az[p].x += nr.z - fa.z;
+                            }
                         }
                     }
                 }
@@ -571,7 +626,7 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KPa
             sy += v.y;
             sz += v.z;
         }
-        if (SPLIT)
+        if (SPLIT && parts > 1)
             B.tea_part[(size_t)part * nb + g] = make_float4(sx, sy, sz, 0.f);
         else
             tea_bead_update<FEFF>(P, B, g, sx, sy, sz, b2, K, feff);
@@ -580,10 +635,10 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KPa
 
 // Sums of the parts of a split mobility product, then the bead's update.
 template <bool FEFF>
-__global__ void k_tea_step_finish(KParams P, DevBuffers B, float4 *feff, const int *gate) {
+__global__ void k_tea_step_finish(KParams P, DevBuffers B, const int2 *work, float4 *feff, const int *gate) {
     if (FEFF && gate && *gate != 0) return;
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= P.nb) return;
+    const int g = tea_tail_bead(P, B, work);
+    if (g < 0) return;
     float4 acc = B.tea_part[g];
     for (int k = 1; k < P.tea_jparts; k++) {
         const float4 v = B.tea_part[(size_t)k * P.nb + g];
@@ -595,25 +650,43 @@ __global__ void k_tea_step_finish(KParams P, DevBuffers B, float4 *feff, const i
     tea_bead_update<FEFF>(P, B, g, acc.x, acc.y, acc.z, beta * beta, tea_const(P.tea_a), feff);
 }
 
-void launch_tea_eps_gated(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
-                          int run_if, cudaStream_t s) {
-    const int t = kTeaLanes * P.tea_slices;
+// CTAs of kernel k that fit on the device at once.
+template <typename Kern>
+static int tea_slots(Kern k, int threads) {
+    int dev = 0, sms = 1, occ = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, threads, 0);
+    return (occ > 0 ? occ : 1) * sms;
+}
+// Items run whole: all but the last one to two waves' worth; grid of the launch.
+static int tea_split_grid(KParams &Q, int nwork, int slots) {
+    const int full = nwork / slots;
+    Q.tea_nhead = full >= 2 ? (full - 1) * slots : 0;
+    return Q.tea_nhead + (nwork - Q.tea_nhead) * Q.tea_jparts;
+}
+
+template <int SL>
+static void tea_eps_launch(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
+                           int run_if, cudaStream_t s) {
+    const int t = kTeaLanes * SL;
+    KParams Q = P;
     if (P.tea_jparts > 1) {
-        const int grid = nwork * P.tea_jparts;
-        switch (P.tea_slices) {
-            case 1: k_tea_eps<1, true><<<grid, t, 0, s>>>(P, B, work, gate, run_if); break;
-            case 2: k_tea_eps<2, true><<<grid, t, 0, s>>>(P, B, work, gate, run_if); break;
-            case 4: k_tea_eps<4, true><<<grid, t, 0, s>>>(P, B, work, gate, run_if); break;
-            default: k_tea_eps<8, true><<<grid, t, 0, s>>>(P, B, work, gate, run_if); break;
-        }
-        k_tea_eps_finish<<<(P.nb + 255) / 256, 256, 0, s>>>(P, B, gate, run_if);
+        const int grid = tea_split_grid(Q, nwork, tea_slots(k_tea_eps<SL, true>, t));
+        k_tea_eps<SL, true><<<grid, t, 0, s>>>(Q, B, work, gate, run_if);
+        if (nwork > Q.tea_nhead) k_tea_eps_finish<<<nwork - Q.tea_nhead, kTeaChunk, 0, s>>>(Q, B, work, gate, run_if);
         return;
     }
+    Q.tea_nhead = nwork;
+    k_tea_eps<SL, false><<<nwork, t, 0, s>>>(Q, B, work, gate, run_if);
+}
+void launch_tea_eps_gated(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
+                          int run_if, cudaStream_t s) {
     switch (P.tea_slices) {
-        case 1: k_tea_eps<1, false><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
-        case 2: k_tea_eps<2, false><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
-        case 4: k_tea_eps<4, false><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
-        default: k_tea_eps<8, false><<<nwork, t, 0, s>>>(P, B, work, gate, run_if); break;
+        case 1: tea_eps_launch<1>(P, B, work, nwork, gate, run_if, s); break;
+        case 2: tea_eps_launch<2>(P, B, work, nwork, gate, run_if, s); break;
+        case 4: tea_eps_launch<4>(P, B, work, nwork, gate, run_if, s); break;
+        default: tea_eps_launch<8>(P, B, work, nwork, gate, run_if, s); break;
     }
 }
 void launch_tea_eps(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
@@ -626,26 +699,28 @@ void launch_tea_beta_gated(const KParams &P, const DevBuffers &B, int capricious
 void launch_tea_beta(const KParams &P, const DevBuffers &B, int capricious, float epsmax, cudaStream_t s) {
     launch_tea_beta_gated(P, B, capricious, epsmax, nullptr, 0, s);
 }
+template <int SL, bool FEFF>
+static void tea_step_launch(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, float4 *feff,
+                            const int *gate, cudaStream_t s) {
+    const int t = kTeaLanes * SL;
+    KParams Q = P;
+    if (P.tea_jparts > 1) {
+        const int grid = tea_split_grid(Q, nwork, tea_slots(k_tea_step<SL, FEFF, true>, t));
+        k_tea_step<SL, FEFF, true><<<grid, t, 0, s>>>(Q, B, work, feff, gate);
+        if (nwork > Q.tea_nhead) k_tea_step_finish<FEFF><<<nwork - Q.tea_nhead, kTeaChunk, 0, s>>>(Q, B, work, feff, gate);
+        return;
+    }
+    Q.tea_nhead = nwork;
+    k_tea_step<SL, FEFF, false><<<nwork, t, 0, s>>>(Q, B, work, feff, gate);
+}
 template <bool FEFF>
 static void tea_step_dispatch(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, float4 *feff,
                               const int *gate, cudaStream_t s) {
-    const int t = kTeaLanes * P.tea_slices;
-    if (P.tea_jparts > 1) {
-        const int grid = nwork * P.tea_jparts;
-        switch (P.tea_slices) {
-            case 1: k_tea_step<1, FEFF, true><<<grid, t, 0, s>>>(P, B, work, feff, gate); break;
-            case 2: k_tea_step<2, FEFF, true><<<grid, t, 0, s>>>(P, B, work, feff, gate); break;
-            case 4: k_tea_step<4, FEFF, true><<<grid, t, 0, s>>>(P, B, work, feff, gate); break;
-            default: k_tea_step<8, FEFF, true><<<grid, t, 0, s>>>(P, B, work, feff, gate); break;
-        }
-        k_tea_step_finish<FEFF><<<(P.nb + 255) / 256, 256, 0, s>>>(P, B, feff, gate);
-        return;
-    }
     switch (P.tea_slices) {
-        case 1: k_tea_step<1, FEFF, false><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
-        case 2: k_tea_step<2, FEFF, false><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
-        case 4: k_tea_step<4, FEFF, false><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
-        default: k_tea_step<8, FEFF, false><<<nwork, t, 0, s>>>(P, B, work, feff, gate); break;
+        case 1: tea_step_launch<1, FEFF>(P, B, work, nwork, feff, gate, s); break;
+        case 2: tea_step_launch<2, FEFF>(P, B, work, nwork, feff, gate, s); break;
+        case 4: tea_step_launch<4, FEFF>(P, B, work, nwork, feff, gate, s); break;
+        default: tea_step_launch<8, FEFF>(P, B, work, nwork, feff, gate, s); break;
     }
 }
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {

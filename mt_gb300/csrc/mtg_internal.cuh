@@ -62,6 +62,7 @@ struct KParams {
     float tea_a, tea_var;
     int tea_slices;        // threads per bead i in the all-pairs TEA kernels (1, 2, 4 or 8)
     int tea_jparts;        // parts of a trajectory's j range (1..kTeaMaxParts), summed by a second kernel
+    int tea_nhead;         // work items run whole before the split tail (set by the TEA launchers)
     int step_block;        // threads per CTA of the fused plain step (64, 128 or 256)
 };
 
@@ -199,6 +200,13 @@ __device__ __forceinline__ float norm3_rn(float3 d) {
 __device__ __forceinline__ float rsqrt_hw(float x) {
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// min(a, b, c) as one three-input instruction (sm_100 and later).
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float y;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(y) : "f"(a), "f"(b), "f"(c));
     return y;
 }
 
