@@ -29,14 +29,20 @@ static_assert(kTeaI == kTeaLanes * kTeaNI, "chunk = lanes x beads per thread");
 constexpr int kTeaTile = 128;               // beads j per tile
 constexpr float kFarAway = 1.0e18f;         // position of padding and extra beads j
 
-// Tile of the all-pairs kernels, every value duplicated into both lanes.
-// Beads past the trajectory's end and extra beads sit far away with zero F
-// and R: every term they give is zero or below the rounding of the sums.
+// Tile of the all-pairs kernels, every value duplicated into both lanes of
+// a packed pair and two pairs per 16-byte word, so that a bead j takes five
+// shared-memory loads (two without F and R).  Beads past the trajectory's end
+// and extra beads sit far away with zero F and R: every term they give is
+// zero or below the rounding of the sums.
 struct TeaTile {
-    float2 x[kTeaTile], y[kTeaTile], z[kTeaTile];
-    float2 fx[kTeaTile], fy[kTeaTile], fz[kTeaTile];
-    float2 rx[kTeaTile], ry[kTeaTile], rz[kTeaTile];
+    float4 xy[kTeaTile];   // x x y y
+    float4 zf[kTeaTile];   // z z Fx Fx
+    float4 fyz[kTeaTile];  // Fy Fy Fz Fz
+    float4 rxy[kTeaTile];  // Rx Rx Ry Ry
+    float2 rz[kTeaTile];   // Rz Rz
 };
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 
@@ -52,15 +58,11 @@ __device__ __forceinline__ void tea_tile_load(TeaTile &T, const DevBuffers &B, i
                 R = B.tea_r[jg];
             }
         }
-        T.x[k] = f2(p.x);
-        T.y[k] = f2(p.y);
-        T.z[k] = f2(p.z);
+        T.xy[k] = make_float4(p.x, p.x, p.y, p.y);
+        T.zf[k] = make_float4(p.z, p.z, F.x, F.x);
         if (WITH_FR) {
-            T.fx[k] = f2(F.x);
-            T.fy[k] = f2(F.y);
-            T.fz[k] = f2(F.z);
-            T.rx[k] = f2(R.x);
-            T.ry[k] = f2(R.y);
+            T.fyz[k] = make_float4(F.y, F.y, F.z, F.z);
+            T.rxy[k] = make_float4(R.x, R.x, R.y, R.y);
             T.rz[k] = f2(R.z);
         }
     }
@@ -154,7 +156,8 @@ __device__ __forceinline__ void tea_eps_tile(const TeaTile &T, int sl, int self_
 #pragma unroll 2
         for (int k = 0; k < kLen; k++) {
             const int t = sl + (sg * kLen + k) * SLICES;
-            const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
+            const float4 a = T.xy[t];
+            const float2 xj = lo2(a), yj = hi2(a), zj = lo2(T.zf[t]);
 #pragma unroll
             for (int p = 0; p < kTeaPairsI; p++) {
                 const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_eps(KPar
                             if (t == self_t + kTeaLanes * (2 * p + e)) continue;
                             const float ax = e ? nx[p].y : nx[p].x, ay = e ? ny[p].y : ny[p].x,
                                         az = e ? nz[p].y : nz[p].x;
-                            const float dx = T.x[t].x + ax, dy = T.y[t].x + ay, dz = T.z[t].x + az;
+                            const float dx = T.xy[t].x + ax, dy = T.xy[t].z + ay, dz = T.zf[t].x + az;
                             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                             if (!(r2 <= K.four_a2)) continue;
                             const float rinv = rsqrt_hw(r2), q = rinv * rinv, tq = q * rinv;
@@ -433,9 +436,10 @@ __device__ __forceinline__ void tea_step_tile(const TeaTile &T, int sl, int self
 #pragma unroll 2
         for (int k = 0; k < kLen; k++) {
             const int t = sl + (sg * kLen + k) * SLICES;
-            const float2 xj = T.x[t], yj = T.y[t], zj = T.z[t];
-            const float2 fxj = T.fx[t], fyj = T.fy[t], fzj = T.fz[t];
-            const float2 rxj = T.rx[t], ryj = T.ry[t], rzj = T.rz[t];
+            const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
+            const float2 xj = lo2(a), yj = hi2(a), zj = lo2(b);
+            const float2 fxj = hi2(b), fyj = lo2(c), fzj = hi2(c);
+            const float2 rxj = lo2(d), ryj = hi2(d), rzj = T.rz[t];
 #pragma unroll
             for (int p = 0; p < kTeaPairsI; p++) {
                 const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
@@ -580,14 +584,14 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KPa
 #pragma unroll
                         for (int e = 0; e < 2; e++) {
                             if (t == self_t + kTeaLanes * (2 * p + e)) continue;
-                            const float dx = T.x[t].x + (e ? nx[p].y : nx[p].x),
-                                        dy = T.y[t].x + (e ? ny[p].y : ny[p].x),
-                                        dz = T.z[t].x + (e ? nz[p].y : nz[p].x);
+                            const float dx = T.xy[t].x + (e ? nx[p].y : nx[p].x),
+                                        dy = T.xy[t].z + (e ? ny[p].y : ny[p].x),
+                                        dz = T.zf[t].x + (e ? nz[p].y : nz[p].x);
                             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                             if (!(r2 <= K.four_a2)) continue;
-                            const float gx = fmaf(T.rx[t].x, e ? cbx[p].y : cbx[p].x, T.fx[t].x),
-                                        gy = fmaf(T.ry[t].x, e ? cby[p].y : cby[p].x, T.fy[t].x),
-                                        gz = fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fz[t].x);
+                            const float gx = fmaf(T.rxy[t].x, e ? cbx[p].y : cbx[p].x, T.zf[t].z),
+                                        gy = fmaf(T.rxy[t].z, e ? cby[p].y : cby[p].x, T.fyz[t].x),
+                                        gz = fmaf(T.rz[t].x, e ? cbz[p].y : cbz[p].x, T.fyz[t].z);
                             const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
                             const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
                             if (e) {
