@@ -433,7 +433,7 @@ __device__ __forceinline__ void tea_step_tile(const TeaTile &T, int sl, int self
     constexpr int kLen = kTeaTile / SLICES / kTeaSeg;
 #pragma unroll
     for (int sg = 0; sg < kTeaSeg; sg++) {
-#pragma unroll 2
+#pragma unroll(kLen <= 8 ? kLen : 2)
         for (int k = 0; k < kLen; k++) {
             const int t = sl + (sg * kLen + k) * SLICES;
             const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
