@@ -332,3 +332,28 @@ def test_tea_split_j_range_matches(engine_mod):
             assert np.array_equal(rng, ref[1])
             np.testing.assert_allclose(x[:, :6], ref[0][:, :6], rtol=0, atol=2e-5)
         e.close()
+
+
+def test_tea_split_tail_on_a_large_batch(engine_mod):
+    """With more than two waves of work items the TEA launchers run the first
+    items whole and split only the last ones over several CTAs; the result
+    equals the unsplit launch up to the summation order."""
+    from mt_gb300 import synth
+    p = synth.default_params(seed=45, hdi_on=1, tea_a=2.0, tea_epsilon_freq=2)
+    b = synth.uniform_batch(p, 48, 100, 3000, seed=45, cube=150.0)
+    assert b.nbeads // 48 // 128 * 48 >= 2 * 5 * 152   # items >= two waves of 5 CTAs on 152 SMs
+    ref = None
+    for jp in (1, 3):
+        e = make_engine(engine_mod, b)
+        t = e.tuning()
+        e.set_tuning(t["list_method"], t["step_block"], 4, jp)
+        e.step(0, 2)
+        x = e.download_state()
+        rng = e.download_rng()
+        if ref is None:
+            ref = (x, rng)
+        else:
+            assert np.array_equal(rng, ref[1])
+            # lattice z reaches 400 nm, where one FP32 ulp is 3.05e-5
+            np.testing.assert_allclose(x[:, :6], ref[0][:, :6], rtol=2.5e-7, atol=2e-5)
+        e.close()
