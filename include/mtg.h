@@ -370,8 +370,10 @@ int mtg_surrogate_status(mtg_engine *e, int *fell_back, int *rechecks, double *l
  * mtg_set_list_method (1 tiles, 2 cells); step_block: threads per CTA of the
  * fused plain step (64, 128, 256); tea_slices: threads per bead in the
  * all-pairs TEA kernels (1, 2, 4, 8); tea_jparts: parts the j range of a
- * trajectory is split into (1, 2, 3, 4: more CTAs, so the last wave of a
- * launch is fuller; the parts' sums meet in a second kernel).  No reference
+ * work item is split into (1, 2, 3, 4).  With more than one part, the items
+ * of the last one to two waves of a launch (all items of a launch shorter
+ * than two waves) run as that many shorter CTAs, so the last waves are
+ * fuller; the parts' sums meet in a second kernel.  No reference
  * counterpart (the reference launches everything with 32-thread blocks,
  * src/mt.h:34). */
 typedef struct {

@@ -61,7 +61,7 @@ struct KParams {
     // TEA
     float tea_a, tea_var;
     int tea_slices;        // threads per bead i in the all-pairs TEA kernels (1, 2, 4 or 8)
-    int tea_jparts;        // parts of a trajectory's j range (1..kTeaMaxParts), summed by a second kernel
+    int tea_jparts;        // parts of a split work item's j range (1..kTeaMaxParts), summed by a second kernel
     int tea_nhead;         // work items run whole before the split tail (set by the TEA launchers)
     int step_block;        // threads per CTA of the fused plain step (64, 128 or 256)
 };
