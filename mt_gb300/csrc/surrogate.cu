@@ -518,34 +518,35 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
     if (!s || !X || !T || n <= 0 || epochs <= 0 || batch <= 0) return sfail(MTG_E_CONFIG, "bad arguments");
     if (batch % 32 != 0) return sfail(MTG_E_CONFIG, "batch must be a multiple of 32");
     SCK(cudaSetDevice(s->device));
-    // normalisation
+    // normalisation: per-column mean and standard deviation, two row-major passes
+    auto moments = [n](const float *A, int cols, std::vector<double> &mean, std::vector<double> &sd) {
+        mean.assign(cols, 0.0);
+        sd.assign(cols, 0.0);
+        for (size_t i = 0; i < (size_t)n; i++)
+            for (int k = 0; k < cols; k++) mean[k] += A[i * cols + k];
+        for (int k = 0; k < cols; k++) mean[k] /= n;
+        for (size_t i = 0; i < (size_t)n; i++)
+            for (int k = 0; k < cols; k++) {
+                const double d = A[i * cols + k] - mean[k];
+                sd[k] += d * d;
+            }
+        for (int k = 0; k < cols; k++) sd[k] = std::sqrt(sd[k] / n);
+    };
+    std::vector<double> mean, sd;
+    moments(X, mlp::kIn, mean, sd);
     for (int k = 0; k < mlp::kIn; k++) {
-        double m = 0, v = 0;
-        for (int i = 0; i < n; i++) m += X[(size_t)i * mlp::kIn + k];
-        m /= n;
-        for (int i = 0; i < n; i++) {
-            const double d = X[(size_t)i * mlp::kIn + k] - m;
-            v += d * d;
-        }
-        const double sd = std::sqrt(v / n);
-        s->h_norm[k] = (float)m;
-        s->h_norm[mlp::kIn + k] = sd > 1e-12 ? (float)(1.0 / sd) : 1.0f;
+        s->h_norm[k] = (float)mean[k];
+        s->h_norm[mlp::kIn + k] = sd[k] > 1e-12 ? (float)(1.0 / sd[k]) : 1.0f;
     }
+    moments(T, mlp::kOut, mean, sd);
     std::vector<float> Tn((size_t)n * mlp::kOut);
     for (int k = 0; k < mlp::kOut; k++) {
-        double m = 0, v = 0;
-        for (int i = 0; i < n; i++) m += T[(size_t)i * mlp::kOut + k];
-        m /= n;
-        for (int i = 0; i < n; i++) {
-            const double d = T[(size_t)i * mlp::kOut + k] - m;
-            v += d * d;
-        }
-        const double sd = std::sqrt(v / n);
-        s->h_ynorm[k] = (float)m;
-        s->h_ynorm[mlp::kOut + k] = sd > 1e-12 ? (float)sd : 1.0f;
-        for (int i = 0; i < n; i++)
-            Tn[(size_t)i * mlp::kOut + k] = (float)((T[(size_t)i * mlp::kOut + k] - m) / s->h_ynorm[mlp::kOut + k]);
+        s->h_ynorm[k] = (float)mean[k];
+        s->h_ynorm[mlp::kOut + k] = sd[k] > 1e-12 ? (float)sd[k] : 1.0f;
     }
+    for (size_t i = 0; i < (size_t)n; i++)
+        for (int k = 0; k < mlp::kOut; k++)
+            Tn[i * mlp::kOut + k] = (float)((T[i * mlp::kOut + k] - mean[k]) / s->h_ynorm[mlp::kOut + k]);
     int rc = upload_norms(s);
     if (rc) return rc;
     const int parts = mlp::backward_parts(batch);
@@ -563,12 +564,23 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
     SCK(cudaMalloc(&dIdx, sizeof(int) * (size_t)n));
     SCK(cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * mlp::kIn, cudaMemcpyHostToDevice, s->stream));
     SCK(cudaMemcpyAsync(dT, Tn.data(), sizeof(float) * Tn.size(), cudaMemcpyHostToDevice, s->stream));
-    std::vector<int> perm(n);
-    std::iota(perm.begin(), perm.end(), 0);
+    // The host shuffles epoch ep + 1 while the device runs epoch ep: two host
+    // permutations, the one being refilled last read by the copy of two
+    // epochs ago (waited for through its event); dIdx itself is rewritten in
+    // stream order after the previous epoch's kernels.
+    std::vector<int> perm[2] = {std::vector<int>(n), std::vector<int>(n)};
+    std::iota(perm[1].begin(), perm[1].end(), 0);
+    cudaEvent_t copied[2];
+    SCK(cudaEventCreateWithFlags(&copied[0], cudaEventDisableTiming));
+    SCK(cudaEventCreateWithFlags(&copied[1], cudaEventDisableTiming));
     std::mt19937 rng((uint32_t)seed);
     for (int ep = 0; ep < epochs; ep++) {
-        std::shuffle(perm.begin(), perm.end(), rng);
-        SCK(cudaMemcpyAsync(dIdx, perm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+        const int k = ep & 1;
+        if (ep >= 2) SCK(cudaEventSynchronize(copied[k]));
+        perm[k] = perm[k ^ 1];
+        std::shuffle(perm[k].begin(), perm[k].end(), rng);
+        SCK(cudaMemcpyAsync(dIdx, perm[k].data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+        SCK(cudaEventRecord(copied[k], s->stream));
         for (int b = 0; b < nbatches; b++) {
             const int *idx = dIdx + (size_t)b * batch;
             SCK(mlp::launch_forward_tc(s->W, dX, idx, batch, s->norm, dY, dZ, s->err, s->stream));
@@ -577,15 +589,14 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
             SCK(mlp::launch_adam(s->W, dG, parts, lr, ++s->adam_step, s->stream));
         }
         SCK(mlp::launch_loss_sum(dL, parts * nbatches, dLsum + ep, s->stream));
-        // the per-epoch loss buffer is read back after the epoch's last use of the
-        // index array; keep the host copy of perm alive until then
-        SCK(cudaStreamSynchronize(s->stream));
     }
     std::vector<float> ls(epochs);
     int herr = 0;
     SCK(cudaMemcpyAsync(ls.data(), dLsum, sizeof(float) * epochs, cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaMemcpyAsync(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaStreamSynchronize(s->stream));
+    cudaEventDestroy(copied[0]);
+    cudaEventDestroy(copied[1]);
     for (float *p : {dX, dT, dY, dZ, dG, dL, dLsum}) cudaFree(p);
     cudaFree(dIdx);
     if (herr) {
