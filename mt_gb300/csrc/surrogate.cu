@@ -552,16 +552,31 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
     const int parts = mlp::backward_parts(batch);
     const int nbatches = n / batch;
     if (nbatches == 0) return sfail(MTG_E_CONFIG, "fewer samples than one batch");
-    float *dX, *dT, *dY, *dZ, *dG, *dL, *dLsum;
-    int *dIdx;
-    SCK(cudaMalloc(&dX, sizeof(float) * (size_t)n * mlp::kIn));
-    SCK(cudaMalloc(&dT, sizeof(float) * (size_t)n * mlp::kOut));
-    SCK(cudaMalloc(&dY, sizeof(float) * (size_t)batch * mlp::kOut));
-    SCK(cudaMalloc(&dZ, sizeof(float) * (size_t)batch * 3 * mlp::kHid));
-    SCK(cudaMalloc(&dG, sizeof(float) * (size_t)parts * mlp::kParams));
-    SCK(cudaMalloc(&dL, sizeof(float) * (size_t)parts * nbatches));
-    SCK(cudaMalloc(&dLsum, sizeof(float) * epochs));
-    SCK(cudaMalloc(&dIdx, sizeof(int) * (size_t)n));
+    // scratch of the run, released on every return (cudaFree waits for the
+    // device, so no kernel still reads it)
+    struct Scratch {
+        float *X = nullptr, *T = nullptr, *Y = nullptr, *Z = nullptr, *G = nullptr, *L = nullptr, *Lsum = nullptr;
+        int *idx = nullptr;
+        cudaEvent_t copied[2] = {nullptr, nullptr};
+        ~Scratch() {
+            for (float *p : {X, T, Y, Z, G, L, Lsum})
+                if (p) cudaFree(p);
+            if (idx) cudaFree(idx);
+            for (cudaEvent_t ev : copied)
+                if (ev) cudaEventDestroy(ev);
+        }
+    } S;
+    SCK(cudaMalloc(&S.X, sizeof(float) * (size_t)n * mlp::kIn));
+    SCK(cudaMalloc(&S.T, sizeof(float) * (size_t)n * mlp::kOut));
+    SCK(cudaMalloc(&S.Y, sizeof(float) * (size_t)batch * mlp::kOut));
+    SCK(cudaMalloc(&S.Z, sizeof(float) * (size_t)batch * 3 * mlp::kHid));
+    SCK(cudaMalloc(&S.G, sizeof(float) * (size_t)parts * mlp::kParams));
+    SCK(cudaMalloc(&S.L, sizeof(float) * (size_t)parts * nbatches));
+    SCK(cudaMalloc(&S.Lsum, sizeof(float) * epochs));
+    SCK(cudaMalloc(&S.idx, sizeof(int) * (size_t)n));
+    float *dX = S.X, *dT = S.T, *dY = S.Y, *dZ = S.Z, *dG = S.G, *dL = S.L, *dLsum = S.Lsum;
+    int *dIdx = S.idx;
+    cudaEvent_t *copied = S.copied;
     SCK(cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * mlp::kIn, cudaMemcpyHostToDevice, s->stream));
     SCK(cudaMemcpyAsync(dT, Tn.data(), sizeof(float) * Tn.size(), cudaMemcpyHostToDevice, s->stream));
     // The host shuffles epoch ep + 1 while the device runs epoch ep: two host
@@ -570,7 +585,6 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
     // stream order after the previous epoch's kernels.
     std::vector<int> perm[2] = {std::vector<int>(n), std::vector<int>(n)};
     std::iota(perm[1].begin(), perm[1].end(), 0);
-    cudaEvent_t copied[2];
     SCK(cudaEventCreateWithFlags(&copied[0], cudaEventDisableTiming));
     SCK(cudaEventCreateWithFlags(&copied[1], cudaEventDisableTiming));
     std::mt19937 rng((uint32_t)seed);
@@ -595,10 +609,6 @@ int mtg_surrogate_train(mtg_surrogate *s, const float *X, const float *T, int n,
     SCK(cudaMemcpyAsync(ls.data(), dLsum, sizeof(float) * epochs, cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaMemcpyAsync(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaStreamSynchronize(s->stream));
-    cudaEventDestroy(copied[0]);
-    cudaEventDestroy(copied[1]);
-    for (float *p : {dX, dT, dY, dZ, dG, dL, dLsum}) cudaFree(p);
-    cudaFree(dIdx);
     if (herr) {
         cudaMemsetAsync(s->err, 0, sizeof(int), s->stream);
         return sfail(MTG_E_TIMEOUT, "a bounded wait for the tensor cores ran out");
