@@ -46,7 +46,7 @@ struct __align__(128) TcBwdSmem {
     __nv_bfloat16 ones[kOutPad * kTcRows];  // B of the bias sums: row 0 ones, the rest zero
     float nrm[2 * kIn];
     float red[kTcThreads / 32];
-    float db4[kOutPad];
+    float db4[kTcThreads / 32][kOutPad];   // per warp, summed in a fixed order
     uint64_t mbar;
     uint32_t tmem_base;
 };
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(const Weights
         put_bf16(S.dyt, core_off(r, k, kTcRows), 0.f);   // rows >= kOut stay zero
     }
     for (int i = tid; i < 2 * kIn; i += blockDim.x) S.nrm[i] = norm ? norm[i] : (i < kIn ? 0.f : 1.f);
-    if (tid < kOutPad) S.db4[tid] = 0.f;
+    if (tid < (kTcThreads / 32) * kOutPad) S.db4[tid / kOutPad][tid % kOutPad] = 0.f;
     const uint32_t mbar = smem_u32(&S.mbar);
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(1) : "memory");
@@ -151,10 +151,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(const Weights
     };
     // dZ of this thread's row from dH in TMEM and z of the layer; writes dz
     // (unless last) and dzt
+    // 32 pre-activations of this thread's row, all requested before any is used
+    auto load_z32 = [&](int layer, int gr, int c0, float (&z)[32]) {
+        const float4 *zr = reinterpret_cast<const float4 *>(Z + ((size_t)gr * 3 + layer) * kHid + c0);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const float4 v = gr < n ? __ldg(zr + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+            z[4 * q] = v.x;
+            z[4 * q + 1] = v.y;
+            z[4 * q + 2] = v.z;
+            z[4 * q + 3] = v.w;
+        }
+    };
     auto dz_rows = [&](int layer, int gr, bool write_dz) {
-        const float *zr = Z + ((size_t)gr * 3 + layer) * kHid;
         for (int c0 = 0; c0 < kHid; c0 += 32) {
-            float dh[32];
+            float dh[32], z[32];
+            load_z32(layer, gr, c0, z);
             tmem_row32(lane_base, kColDH + (uint32_t)c0, dh);
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -162,7 +174,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(const Weights
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
                     const int c = c0 + q * 8 + j;
-                    d[j] = gr < n ? dh[q * 8 + j] * dsilu_tanh(zr[c]) : 0.f;
+                    d[j] = gr < n ? dh[q * 8 + j] * dsilu_tanh(z[q * 8 + j]) : 0.f;
                     put_bf16(S.dzt, core_off(c, r, kTcRows), d[j]);
                 }
                 if (write_dz) {
@@ -178,8 +190,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(const Weights
     };
     // H^T of this thread's row: silu(z) of the layer
     auto ht_rows = [&](int layer, int gr) {
-        const float *zr = Z + ((size_t)gr * 3 + layer) * kHid;
-        for (int c = 0; c < kHid; c++) put_bf16(S.ht, core_off(c, r, kTcRows), gr < n ? silu_tanh(zr[c]) : 0.f);
+        for (int c0 = 0; c0 < kHid; c0 += 32) {
+            float z[32];
+            load_z32(layer, gr, c0, z);
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+                put_bf16(S.ht, core_off(c0 + j, r, kTcRows), gr < n ? silu_tanh(z[j]) : 0.f);
+        }
     };
 
     int it = 0;
@@ -210,7 +227,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(const Weights
                 put_bf16(S.dyt, core_off(c, r, kTcRows), d[c]);
                 float s = d[c];
                 for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                if (lane == 0) atomicAdd(&S.db4[c], s);
+                if (lane == 0) S.db4[warp][c] += s;
             }
             ht_rows(2, gr);
         }
@@ -238,8 +255,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(const Weights
         dz_rows(0, gr, false);
         {
             const int src = gr < n ? (idx ? idx[gr] : gr) : 0;
+            const float4 *xr = reinterpret_cast<const float4 *>(X + (size_t)src * kIn);
+            float x[kIn];
+#pragma unroll
+            for (int q = 0; q < kIn / 4; q++) {
+                const float4 v = __ldg(xr + q);
+                x[4 * q] = v.x;
+                x[4 * q + 1] = v.y;
+                x[4 * q + 2] = v.z;
+                x[4 * q + 3] = v.w;
+            }
+#pragma unroll
             for (int c = 0; c < kIn; c++) {
-                const float v = gr < n ? (X[(size_t)src * kIn + c] - S.nrm[c]) * S.nrm[kIn + c] : 0.f;
+                const float v = gr < n ? (x[c] - S.nrm[c]) * S.nrm[kIn + c] : 0.f;
                 put_bf16(S.xt, core_off(c, r, kTcRows), v);
             }
         }
@@ -284,7 +312,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(const Weights
             }
         }
         __syncthreads();
-        if (tid < kOut) Gc[kOffB + 3 * kHid + tid] = S.db4[tid];
+        if (tid < kOut) {
+            float b = 0.f;
+            for (int w = 0; w < kTcThreads / 32; w++) b += S.db4[w][tid];
+            Gc[kOffB + 3 * kHid + tid] = b;
+        }
         for (int s = 16; s > 0; s >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, s);
         if (lane == 0) S.red[warp] = lsum;
         __syncthreads();

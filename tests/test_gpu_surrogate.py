@@ -102,6 +102,21 @@ def test_training_reduces_loss_and_beats_the_mean_predictor(engine_mod):
     assert mse_net < 0.5 * mse_mean, (mse_net, mse_mean)
 
 
+def test_training_is_deterministic(engine_mod):
+    """Same data, seeds and batch: the same weights, bit for bit (every
+    gradient reduction runs in a fixed order)."""
+    rng = np.random.default_rng(9)
+    X = rng.normal(2.0, 1.5, size=(3000, M.IN)).astype(np.float32)
+    T = rng.normal(0.9, 0.05, size=(3000, M.OUT)).astype(np.float32)
+    runs = []
+    for _ in range(2):
+        with engine_mod.Surrogate(seed=11) as s:
+            losses = s.train(X, T, epochs=3, batch=512, lr=1e-3, seed=2)
+            runs.append((losses, s.params()[0]))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
+
+
 def test_fallback_at_first_recheck_reproduces_exact_tea(engine_mod):
     """With max_err = 0 the first re-check (step 0) falls back and replaces the
     network's C_i and beta by the exact ones at once: the run is then the
