@@ -407,6 +407,11 @@ int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *devic
 #define MTG_KERNEL_KINDS 8
 int mtg_set_kernel_timing(mtg_engine *e, int on);
 int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int reset);
+/* Kernel launches replayed from the engine's step graphs since the last
+ * reset: every kernel node of a captured list-period graph counts once per
+ * replay (memset and event nodes do not).  Steps enqueued outside a graph
+ * (ranges shorter than a period) are not counted here. */
+int mtg_graph_kernel_launches(mtg_engine *e, long long *launches, int reset);
 
 /* Measured FP32 FMA throughput of `device` in TFLOP/s: the best of
  * register-resident chains of scalar and of packed FP32x2 FMAs over 8 CTAs

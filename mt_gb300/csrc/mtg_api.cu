@@ -203,11 +203,26 @@ void destroy_graphs(mtg_engine *e) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+    e->graph_kernels[0] = e->graph_kernels[1] = 0;
     e->direct_base = 0;
     e->graph_slot_count[0] = e->graph_slot_count[1] = 0;
 }
 
 namespace {
+
+// Kernel nodes of a captured graph.
+long long count_kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+    long long k = 0;
+    for (size_t i = 0; i < n; i++) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+    }
+    return k;
+}
 
 // The list rebuild with the engine's method.
 void launch_lists(mtg_engine *e) {
@@ -845,6 +860,7 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
                 if (ce != cudaSuccess) return fail(MTG_E_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
                 if (e->timing) e->graph_slot_count[cur0] = e->capture_next - e->graph_slot_base[cur0];
                 e->cur = cur0;
+                e->graph_kernels[cur0] = count_kernel_nodes(g);
                 CK(cudaGraphInstantiate(&ge, g, 0));
                 cudaGraphDestroy(g);
             }
@@ -856,6 +872,7 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
                     if (!seen) e->used_slots.push_back(slot);
                 }
             CK(cudaGraphLaunch(ge, e->stream));
+            e->graph_kernel_launches += e->graph_kernels[e->cur];
             if (period & 1) e->cur ^= 1;
             if (p.lj_on || p.is_assembly) e->lists_valid = true;
             s += period;
@@ -1016,6 +1033,13 @@ int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int r
             e->kt_count[k] = 0;
         }
     }
+    return MTG_OK;
+}
+
+int mtg_graph_kernel_launches(mtg_engine *e, long long *launches, int reset) {
+    if (!e) return fail(MTG_E_CONFIG, "engine is NULL");
+    if (launches) *launches = e->graph_kernel_launches;
+    if (reset) e->graph_kernel_launches = 0;
     return MTG_OK;
 }
 

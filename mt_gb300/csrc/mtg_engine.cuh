@@ -45,6 +45,8 @@ struct mtg_engine {
     int device = 0;
     // graphs: [parity]
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_kernels[2] = {0, 0};      // kernel nodes of each captured graph
+    long long graph_kernel_launches = 0;      // kernel nodes replayed since the last reset
     int graph_period = 0;
     // per-kernel timing (see mtg_set_kernel_timing)
     bool timing = false;

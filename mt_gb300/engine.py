@@ -60,6 +60,7 @@ EXPORTS = {
     "mtg_step_timed": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_float)]),
     "mtg_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "mtg_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
+    "mtg_graph_kernel_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int]),
     "mtg_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "mtg_host_free": (C.c_int, [C.c_void_p]),
     "mtg_energies_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -381,6 +382,12 @@ class Engine:
         n = (C.c_longlong * len(KERNEL_KINDS))()
         check(self.lib.mtg_kernel_times(self.h, t, n, int(reset)))
         return {k: (t[i], n[i]) for i, k in enumerate(KERNEL_KINDS)}
+
+    def graph_kernel_launches(self, reset: bool = False) -> int:
+        """Kernel nodes replayed from the step graphs since the last reset."""
+        n = C.c_longlong(0)
+        check(self.lib.mtg_graph_kernel_launches(self.h, C.byref(n), int(reset)))
+        return n.value
 
     def tuning(self) -> dict:
         t = MtgTuning()

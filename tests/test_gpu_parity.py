@@ -357,3 +357,21 @@ def test_tea_split_tail_on_a_large_batch(engine_mod):
             # lattice z reaches 400 nm, where one FP32 ulp is 3.05e-5
             np.testing.assert_allclose(x[:, :6], ref[0][:, :6], rtol=2.5e-7, atol=2e-5)
         e.close()
+
+
+def test_graph_kernel_launch_count(engine_mod):
+    """Every replay of a list-period graph adds that graph's kernel nodes:
+    at least one fused step per MD step plus the list rebuild."""
+    b = small_system(seed=46)
+    e = make_engine(engine_mod, b)
+    period = int(b.params.ljpairsupdatefreq)
+    e.step(0, period)                      # captures the graph and replays it once
+    n1 = e.graph_kernel_launches(reset=True)
+    e.step(period, 2 * period)             # two more replays
+    n2 = e.graph_kernel_launches(reset=True)
+    assert n1 >= period + 1, n1
+    assert n2 == 2 * n1, (n1, n2)
+    assert e.graph_kernel_launches() == 0
+    e.step(3 * period, 3)                  # shorter than a period: no graph
+    assert e.graph_kernel_launches() == 0
+    e.close()
