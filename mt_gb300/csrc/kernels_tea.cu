@@ -8,10 +8,13 @@
 // FP32x2 pairs; `tea_slices` threads share each bead i and take interleaved
 // j of every tile, so small batches still fill the GPU, and the partial sums
 // meet in shared memory.  The tile holds every value of bead j twice (both
-// lanes of a packed operand), so one broadcast 8-byte load feeds a packed
-// pair of beads i.  Away from the CTA's own beads the far-field formula runs
-// for every pair; the few overlapping pairs (r <= 2a) are found through the
-// running minimum of r^2 and corrected afterwards.  In the tile that holds
+// lanes of a packed operand, two operands per 16-byte word), so broadcast
+// loads feed the packed pairs of beads i directly.  Away from the CTA's own
+// beads the far-field formula runs for every pair; the few overlapping pairs
+// (r <= 2a) are found through running minima of r^2, one per quarter of a
+// thread's j values, and only a quarter that holds one is rescanned with the
+// near-field formula.  With tea_jparts > 1 the work items of the last waves
+// are split over parts of their j range (see tea_item).  In the tile that holds
 // the CTA's own beads the self pairs get r^2 = 1e30: their terms are then
 // far below the rounding of the sums, and the correction skips them.
 // Sums are kept in units of 0.75 a (T' = T / (0.75 a)).  The kernels are
