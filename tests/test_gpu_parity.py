@@ -375,3 +375,40 @@ def test_graph_kernel_launch_count(engine_mod):
     e.step(3 * period, 3)                  # shorter than a period: no graph
     assert e.graph_kernel_launches() == 0
     e.close()
+
+
+def test_tea_ragged_batch_matches_oracle(engine_mod, oracle_lib):
+    """TEA on an uneven batch (trajectories of 52 to ~480 beads, several
+    128-bead chunks each): epsilon, beta, C_i and one step against the
+    oracle, with whole and with split j ranges."""
+    from helpers import cutoff_margin
+    from mt_gb300 import synth
+    for seed in range(70, 120):
+        p = synth.default_params(seed=seed, hdi_on=1, tea_epsilon_freq=1)
+        b = synth.ragged_batch(p, 5, seed=seed, pf_range=(4, 14), free_range=(0, 300), cube=50.0, radius=8.12,
+                               psi_mode="make_mt", thermal=0.05)
+        if cutoff_margin(b, b.coords) > 2e-4:
+            break
+    sizes = np.diff(b.offsets)
+    assert sizes.max() > 128 and len(set(sizes.tolist())) > 1, sizes
+    o32 = oracle_lib.Oracle("orc", "f32")
+    e = make_engine(engine_mod, b)
+    eps, beta, ci, rc = e.tea_update()
+    assert rc == 0
+    ci_o, eps_o = o32.tea_epsilon(b, b.coords)
+    eps_t, beta_o, st = o32.tea_beta(b, eps_o)
+    assert rel_norm(ci[:, :3], ci_o[:, :3]) < 1e-5
+    np.testing.assert_allclose(eps, eps_t, rtol=1e-5)
+    np.testing.assert_allclose(beta, beta_o, rtol=1e-5)
+    e.close()
+    seeds = o32.generate_seeds(b.params.rseed, 2 * b.nbeads)
+    xo, _, so, _, st, _, _ = o32.run(b, b.coords, seeds, 0, 1)
+    assert st == 0
+    for jp in (1, 3):
+        e2 = make_engine(engine_mod, b)
+        t = e2.tuning()
+        e2.set_tuning(t["list_method"], t["step_block"], t["tea_slices"], jp)
+        e2.step(0, 1)
+        assert np.array_equal(e2.download_rng(), so)
+        np.testing.assert_allclose(e2.download_state()[:, :6], xo[:, :6], rtol=0, atol=1e-4)
+        e2.close()
