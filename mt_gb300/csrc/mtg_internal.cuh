@@ -107,20 +107,23 @@ __device__ __forceinline__ float uint_to_unit(uint32_t u) {
     const float f = __uint_as_float(0x3f800000u | (0x007fffffu & u)) - 1.0f;
     return f == 0.0f ? 1.0e-8f : f;
 }
-// rforce (src/HybridTaus.cu:85-98): four N(0,1) deviates by Box-Muller.
+// rforce (src/HybridTaus.cu:84-98): four N(0,1) deviates by Box-Muller.  The
+// sine and cosine are the hardware approximations the reference calls
+// (__sinf/__cosf), and the logarithm is the one its -use_fast_math build
+// (CMakeLists.txt:62) turns logf into.
 __device__ __forceinline__ float4 gauss4(uint4 &s) {
     float4 g;
     float u1 = uint_to_unit(hybrid_taus(s));
     float u2 = uint_to_unit(hybrid_taus(s));
-    float r = sqrtf(-2.0f * logf(u1));
+    float r = sqrtf(-2.0f * __logf(u1));
     float sn, cs;
-    sincosf(6.28318548f * u2, &sn, &cs);
+    __sincosf(6.28318548f * u2, &sn, &cs);
     g.x = r * sn;
     g.y = r * cs;
     u1 = uint_to_unit(hybrid_taus(s));
     u2 = uint_to_unit(hybrid_taus(s));
-    r = sqrtf(-2.0f * logf(u1));
-    sincosf(6.28318548f * u2, &sn, &cs);
+    r = sqrtf(-2.0f * __logf(u1));
+    __sincosf(6.28318548f * u2, &sn, &cs);
     g.z = r * sn;
     g.w = r * cs;
     return g;
