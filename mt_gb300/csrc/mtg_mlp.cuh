@@ -1,5 +1,6 @@
 // mtg_mlp.cuh - shapes, parameter layout and launchers of the TEA surrogate
-// network (kernels_mlp.cu).
+// network: Adam and the BF16 copies (kernels_mlp.cu), the tensor-core forward
+// pass (kernels_mlp_tc.cu) and backward pass (kernels_mlp_train_tc.cu).
 //
 // Parameter vector (FP32 masters, Adam moments and gradients share it):
 //   w1 [kHid][kIn] | w2 [kHid][kHid] | w3 [kHid][kHid] | w4 [kOut][kHid] |
