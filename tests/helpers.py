@@ -100,3 +100,16 @@ def golden_batch(d):
     if len(set(sizes.tolist())) == 1:
         b.uniform_ntot = int(sizes[0])
     return b
+
+
+def with_lone_monomers(b, local=(160, 161)):
+    """Turns the free dimer at the given local indices of every trajectory into
+    two monomers without a harmonic partner: count 0 and entry -1, as
+    read_PDB leaves such a bead (src/preparator.cpp:340); pairs_kernel then
+    takes R_MON = -r_mon and skips j = 1 for it (src/compute_cuda.cu:548,565,599)."""
+    for t in range(b.ntraj):
+        for i in local:
+            g = int(b.offsets[t]) + i
+            b.harmonic_count[g] = 0
+            b.harmonic[g * b.max_h:(g + 1) * b.max_h] = -1
+    return b

@@ -9,7 +9,7 @@ component) in FP32; multi-step states within the FP32 drift stated per test.
 import numpy as np
 import pytest
 
-from helpers import rel_norm, small_system, system_with_margin
+from helpers import rel_norm, small_system, system_with_margin, with_lone_monomers
 
 pytestmark = pytest.mark.gpu
 
@@ -59,12 +59,14 @@ def test_lists_golden(engine_mod):
     e.close()
 
 
-@pytest.mark.parametrize("case", ["default", "walls_barrier_seam", "gdp_ontubule", "static_lists"])
+@pytest.mark.parametrize("case", ["default", "walls_barrier_seam", "gdp_ontubule", "static_lists", "lone_monomers"])
 def test_forces_and_energies(engine_mod, oracle_lib, case):
     over = {}
     if case == "walls_barrier_seam":
         over = dict(is_wall=1, rep_r=9.0, barrier=1, seam_coeff=1.7)
     b = system_with_margin(seed=8, **over)
+    if case == "lone_monomers":
+        b = with_lone_monomers(b)
     if case == "gdp_ontubule":
         rng = np.random.default_rng(4)
         b.gtp[:] = rng.integers(0, 2, b.nbeads)
@@ -79,6 +81,8 @@ def test_forces_and_energies(engine_mod, oracle_lib, case):
     else:
         e = make_engine(engine_mod, b)
         e.rebuild_pairs()
+        for k in ("lj", "long", "lat"):
+            assert e.list_of_lists(k) == L.as_lists(k), k
     f = e.compute_forces()
     fo, f64 = o32.forces(b, b.coords, L), o64.forces(b, b.coords, L)
     for c in range(6):

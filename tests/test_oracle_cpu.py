@@ -4,7 +4,7 @@ present, against those kernels directly on further seeded cases."""
 import numpy as np
 import pytest
 
-from helpers import golden_batch, rel_norm, small_system, system_with_margin
+from helpers import with_lone_monomers, golden_batch, rel_norm, small_system, system_with_margin
 
 GOLD = __import__("os").path.join(__import__("os").path.dirname(__file__), "golden")
 
@@ -83,12 +83,14 @@ ref_only = pytest.mark.skipif(not __import__("oracle.oracle", fromlist=["x"]).re
 
 
 @ref_only
-@pytest.mark.parametrize("case", ["default", "walls_barrier_seam", "gdp_ontubule", "odd_pf"])
+@pytest.mark.parametrize("case", ["default", "walls_barrier_seam", "gdp_ontubule", "odd_pf", "lone_monomers"])
 def test_oracle_matches_reference_kernels(oracle_lib, case):
     over = {}
     if case == "walls_barrier_seam":
         over = dict(is_wall=1, rep_r=9.0, barrier=1, seam_coeff=1.7)
     b = system_with_margin(seed=7, **over) if case != "odd_pf" else small_system(seed=9, n_mon=11)
+    if case == "lone_monomers":
+        b = with_lone_monomers(b)
     if case == "gdp_ontubule":
         rng = np.random.default_rng(4)
         b.gtp[:] = rng.integers(0, 2, b.nbeads)
