@@ -173,17 +173,20 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
     int lo_buf[kCellMaxLong], la_buf[kCellMaxLat];
     int nlj = 0, nlo = 0, nla = 0;
     bool overflow = false;
-    // the 27 buckets (in shared memory for the rolled cell loop), a mask of
-    // the cells whose bucket an earlier cell already has, and each cell's
-    // range fetched while the previous cell runs
-    __shared__ int s_bk[27][kTile];
+    // the ranges of the 27 cells' buckets, all requested at once and kept in
+    // shared memory for the rolled cell loop, and a mask of the cells whose
+    // bucket an earlier cell already has
+    __shared__ int s_st[27][kTile], s_ct[27][kTile];
     uint32_t dup = 0;
     {
         int bk[27];
 #pragma unroll
-        for (int c = 0; c < 27; c++) {
+        for (int c = 0; c < 27; c++)
             bk[c] = tb + (int)(cell_hash(cx + c % 3 - 1, cy + (c / 3) % 3 - 1, cz + c / 9 - 1) & mask);
-            s_bk[c][threadIdx.x] = bk[c];
+#pragma unroll
+        for (int c = 0; c < 27; c++) {
+            s_st[c][threadIdx.x] = start[bk[c]];
+            s_ct[c][threadIdx.x] = cnt[bk[c]];
         }
 #pragma unroll
         for (int c = 1; c < 27; c++) {
@@ -193,14 +196,8 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
             dup |= (seen ? 1u : 0u) << c;
         }
     }
-    int st_next = start[s_bk[0][threadIdx.x]], ct_next = cnt[s_bk[0][threadIdx.x]];
     for (int c = 0; c < 27; c++) {
-        const int st_c = st_next, ct_c = ct_next;
-        if (c + 1 < 27) {
-            const int b = s_bk[c + 1][threadIdx.x];
-            st_next = start[b];
-            ct_next = cnt[b];
-        }
+        const int st_c = s_st[c][threadIdx.x], ct_c = s_ct[c][threadIdx.x];
         if (((dup >> c) & 1u) || ct_c == 0) continue;
         const int s0 = base + st_c, s1 = s0 + ct_c;
         for (int s4 = s0; s4 < s1; s4 += 4) {
