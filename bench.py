@@ -46,8 +46,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = json.load(open(os.path.join(ROOT, "BASELINE.json")))["metric"] if os.path.exists(
-    os.path.join(ROOT, "BASELINE.json")) else "monomer-steps/s"
+METRIC = "monomer-steps/s on 1 GB300: exact TEA vs learned TEA at \u22641% mobility error"
 UNIT = "monomer-steps/s"
 FALLBACK_HBM_GBS = 6800.0
 
