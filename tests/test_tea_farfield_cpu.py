@@ -2,7 +2,7 @@
 the RPY coupling decays as 1/r while the number of beads at distance r
 grows as r^2, so the far field carries much of the correlated displacement.
 Truncating sum_j T_ij g_j (src/bdhitea_kernel.cu:104-213) at a cutoff, on a
-seeded trajectory of the C4 kind, leaves an RMS mobility error above 1% even
+seeded lattice + free-tubulin trajectory, leaves an RMS mobility error above 1% even
 at 30 nm (FP64, CPU only; the full-size study is quoted in the design notes)."""
 import numpy as np
 
