@@ -2,7 +2,8 @@
  * mt_oracle.c - CPU oracle for the MADDY Brownian/Langevin hot path.
  *
  * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py as the checker.  Built with
+ * CPU-baseline legs of bench.py, as the reference to compare against, never
+ * as the product path.  Built with
  * -ffp-contract=off so that the FP32 results are identical on x86-64 and
  * aarch64 hosts.
  */
