@@ -39,6 +39,8 @@ def cutoff_margin(batch, coords):
     worst = np.inf
     for t in range(batch.ntraj):
         b0, b1 = int(batch.offsets[t]), int(batch.offsets[t + 1])
+        if b1 - b0 < 2:
+            continue
         x = coords[b0:b1, :3].astype(np.float64)
         R = rotations(coords[b0:b1])
         uz = R[:, :, 2]

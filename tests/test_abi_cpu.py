@@ -5,6 +5,7 @@ import re
 import subprocess
 
 import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -48,18 +49,29 @@ def test_derive_params_matches_reference_formula(engine_mod):
 
 
 def test_invalid_params_rejected_without_gpu(engine_mod):
-    """Argument checks run before any CUDA call and return MTG_E_CONFIG."""
+    """Argument checks run before any CUDA call and return MTG_E_CONFIG with
+    the reason."""
     import ctypes as C
     from mt_gb300 import _abi, synth
-    b = synth.uniform_batch(synth.default_params(), 1, 4, 0, seed=1)
     lib = engine_mod.load()
-    p = synth.default_params(ljpairsupdatefreq=0)
     h = C.c_void_p()
-    t = _abi.MtgTopology()
-    t.Ntot, t.Ntr = b.uniform_ntot, 1
-    rc = lib.mtg_create(C.byref(p), C.byref(t), C.byref(h))
-    assert rc == _abi.MTG_E_CONFIG
-    p = synth.default_params(hdi_on=1, tea_epsilon_freq=0)   # the reference would divide by zero
-    rc = lib.mtg_create(C.byref(p), C.byref(t), C.byref(h))
-    assert rc == _abi.MTG_E_CONFIG
-    assert b"tea_epsilon_freq" in lib.mtg_last_error_string() or True
+    t = _abi.MtgTopology()                       # no topology arrays
+    rc = lib.mtg_create(C.byref(synth.default_params()), C.byref(t), C.byref(h))
+    assert rc == _abi.MTG_E_CONFIG and b"required" in lib.mtg_last_error_string()
+    for over, word in ((dict(ljpairsupdatefreq=0), "ljpairsupdatefreq"),
+                       (dict(hdi_on=1, tea_epsilon_freq=0), "tea_epsilon_freq")):   # the reference would divide by zero
+        b = synth.uniform_batch(synth.default_params(**over), 1, 4, 2, seed=1)
+        with pytest.raises(engine_mod.MtgError, match=word):
+            engine_mod.Engine(b)
+
+
+def test_empty_trajectory_rejected(engine_mod):
+    """An empty trajectory is a configuration error (MTG_E_CONFIG), reported
+    before any device work: the reference never has one."""
+    from mt_gb300 import synth
+    p = synth.default_params(seed=5)
+    trajs = [synth.make_trajectory(6, 20, seed=5, radius=8.12, psi_mode="make_mt", cube=40.0),
+             synth.make_trajectory(0, 0, seed=6, radius=8.12, psi_mode="make_mt", cube=40.0)]
+    b = synth.batch_from_trajectories(p, trajs)
+    with pytest.raises(engine_mod.MtgError, match="MTG_E_CONFIG"):
+        engine_mod.Engine(b)

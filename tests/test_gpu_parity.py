@@ -416,3 +416,43 @@ def test_tea_ragged_batch_matches_oracle(engine_mod, oracle_lib):
         assert np.array_equal(e2.download_rng(), so)
         np.testing.assert_allclose(e2.download_state()[:, :6], xo[:, :6], rtol=0, atol=1e-4)
         e2.close()
+
+
+@pytest.mark.parametrize("method", [1, 2])
+def test_two_bead_trajectory(engine_mod, oracle_lib, method):
+    """A ragged batch with a trajectory of a single free dimer beside two
+    ordinary ones: lists, forces, energies and one step against the oracle,
+    for both rebuild methods."""
+    from mt_gb300 import synth
+    p = synth.default_params(seed=5)
+    trajs = [synth.make_trajectory(6, 20, seed=5, radius=8.12, psi_mode="make_mt", cube=40.0, thermal=0.05),
+             synth.make_trajectory(0, 2, seed=7, radius=8.12, psi_mode="make_mt", cube=40.0, thermal=0.05),
+             synth.make_trajectory(9, 40, seed=8, radius=8.12, psi_mode="make_mt", cube=40.0, thermal=0.05)]
+    b = synth.batch_from_trajectories(p, trajs)
+    assert list(np.diff(b.offsets)) == [98, 2, 157]
+    o = oracle_lib.Oracle("orc")
+    L = o.lists(b, b.coords)
+    e = make_engine(engine_mod, b)
+    e.set_list_method(method)
+    e.rebuild_pairs()
+    for k in ("lj", "long", "lat"):
+        assert e.list_of_lists(k) == L.as_lists(k), k
+    f = e.compute_forces()
+    fo = o.forces(b, b.coords, L)
+    for c in range(6):
+        assert rel_norm(f[:, c], fo[:, c]) < FORCE_RTOL, c
+    tot = e.energies()
+    eo = o.energies(b, b.coords, L)
+    for t in range(b.ntraj):
+        sl = slice(int(b.offsets[t]), int(b.offsets[t + 1]))
+        np.testing.assert_allclose(tot[t], eo[sl].sum(0), rtol=1e-5, atol=1e-3)
+    e.close()
+    seeds = o.generate_seeds(p.rseed, 2 * b.nbeads)
+    xo, _, so, _, st, _, _ = o.run(b, b.coords, seeds, 0, 1)
+    assert st == 0
+    e2 = make_engine(engine_mod, b)
+    e2.set_list_method(method)
+    e2.step(0, 1)
+    assert np.array_equal(e2.download_rng(), so)
+    np.testing.assert_allclose(e2.download_state()[:, :6], xo[:, :6], rtol=0, atol=5e-5)
+    e2.close()
