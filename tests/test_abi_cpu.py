@@ -55,7 +55,10 @@ def test_invalid_params_rejected_without_gpu(engine_mod):
     from mt_gb300 import _abi, synth
     lib = engine_mod.load()
     h = C.c_void_p()
-    t = _abi.MtgTopology()                       # no topology arrays
+    t = _abi.MtgTopology()                       # no beads
+    rc = lib.mtg_create(C.byref(synth.default_params()), C.byref(t), C.byref(h))
+    assert rc == _abi.MTG_E_CONFIG and b"Ntot > 0" in lib.mtg_last_error_string()
+    t.Ntot, t.Ntr = 8, 1                         # beads but no topology arrays
     rc = lib.mtg_create(C.byref(synth.default_params()), C.byref(t), C.byref(h))
     assert rc == _abi.MTG_E_CONFIG and b"required" in lib.mtg_last_error_string()
     for over, word in ((dict(ljpairsupdatefreq=0), "ljpairsupdatefreq"),
