@@ -134,7 +134,20 @@ __device__ void isort_strided(int *a, int n, int stride) {
     }
 }
 
-constexpr int kLocalLJ = 64;   // LJ hits sorted in local memory; more are sorted in place
+constexpr int kLocalLJ = 16;   // LJ hits sorted in shared memory; more are sorted in place
+
+// Insertion sort of one thread's column of a [rows][kTile] shared array.
+__device__ __forceinline__ void isort_col(int (*a)[kTile], int n, int t) {
+    for (int i = 1; i < n; i++) {
+        const int v = a[i][t];
+        int j = i - 1;
+        while (j >= 0 && a[j][t] > v) {
+            a[j + 1][t] = a[j][t];
+            j--;
+        }
+        a[j + 1][t] = v;
+    }
+}
 
 // Thread per bead: candidates are read from the bucket-ordered position copy
 // (one contiguous 16 B load each); the rare assembly candidates (< 6.6 nm)
@@ -169,7 +182,9 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
     const int tb = tbase[traj];
     const uint32_t mask = (uint32_t)tmask[traj];
 
-    int lj_buf[kLocalLJ];
+    // this thread's LJ hits: a column of shared memory (its own bank), so the
+    // buffer and its sort never leave the SM
+    __shared__ int s_lj[kLocalLJ][kTile];
     int lo_buf[kCellMaxLong], la_buf[kCellMaxLat];
     int nlj = 0, nlo = 0, nla = 0;
     bool overflow = false;
@@ -215,10 +230,10 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
                     if (nlj >= P.maxLJ) {
                         overflow = true;
                     } else if (nlj < kLocalLJ) {
-                        lj_buf[nlj] = jl;
+                        s_lj[nlj][threadIdx.x] = jl;
                     } else {
                         if (nlj == kLocalLJ)  // spill the local part first
-                            for (int k = 0; k < kLocalLJ; k++) B.lj[k * nb + g] = lj_buf[k];
+                            for (int k = 0; k < kLocalLJ; k++) B.lj[k * nb + g] = s_lj[k][threadIdx.x];
                         B.lj[nlj * nb + g] = jl;
                     }
                     nlj++;
@@ -264,8 +279,8 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
     if (P.lj_on) {
         const int n = min(nlj, P.maxLJ);
         if (n <= kLocalLJ) {
-            isort(lj_buf, n);
-            for (int k = 0; k < n; k++) B.lj[k * nb + g] = lj_buf[k];
+            isort_col(s_lj, n, threadIdx.x);
+            for (int k = 0; k < n; k++) B.lj[k * nb + g] = s_lj[k][threadIdx.x];
         } else {
             isort_strided(B.lj + g, n, nb);
         }
