@@ -211,66 +211,82 @@ __global__ void __launch_bounds__(kTile, 6) k_cell_lists(KParams P, DevBuffers B
             dup |= (seen ? 1u : 0u) << c;
         }
     }
-    for (int c = 0; c < 27; c++) {
-        const int st_c = s_st[c][threadIdx.x], ct_c = s_ct[c][threadIdx.x];
-        if (((dup >> c) & 1u) || ct_c == 0) continue;
-        const int s0 = base + st_c, s1 = s0 + ct_c;
-        for (int s4 = s0; s4 < s1; s4 += 4) {
-            float4 qq[4];   // four candidates in flight
+    // drop the buckets an earlier cell already has, then walk the remaining
+    // candidates in cell order four at a time across cell boundaries, so a
+    // sparse neighbourhood still has four loads in flight
+    for (int c = 0; c < 27; c++)
+        if ((dup >> c) & 1u) s_ct[c][threadIdx.x] = 0;
+    int c = 0, off = 0;
+    while (c < 27 && s_ct[c][threadIdx.x] == 0) c++;
+    while (c < 27) {
+        int sl[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) qq[u] = s4 + u < s1 ? cell_pos[s4 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                if (s4 + u >= s1) break;
-                const float4 q = qq[u];
-                const int jg = __float_as_int(q.w) & kCellIndexMask;
-                const int jl = jg - base;
-                const float cd = centre_dist(pi, q);
-                if (do_lj && jl != il && cd < P.ljcut) {
-                    if (nlj >= P.maxLJ) {
-                        overflow = true;
-                    } else if (nlj < kLocalLJ) {
-                        s_lj[nlj][threadIdx.x] = jl;
-                    } else {
-                        if (nlj == kLocalLJ)  // spill the local part first
-                            for (int k = 0; k < kLocalLJ; k++) B.lj[k * nb + g] = s_lj[k][threadIdx.x];
-                        B.lj[nlj * nb + g] = jl;
-                    }
-                    nlj++;
+        for (int u = 0; u < 4; u++) {
+            sl[u] = -1;
+            if (c < 27) {
+                sl[u] = base + s_st[c][threadIdx.x] + off;
+                if (++off == s_ct[c][threadIdx.x]) {
+                    off = 0;
+                    do {
+                        c++;
+                    } while (c < 27 && s_ct[c][threadIdx.x] == 0);
                 }
-                if (do_pairs && cd < kPairReach && jl != hpart) {
-                    const float4 pj = fr[jg];   // the exact state (q carries the index in w)
-                    const float rmon = h0 < 0 ? -2.0f : 2.0f;
-                    const int fj = B.flags[jg];
-                    if (((flags ^ fj) & kFlagBeta) != 0) {
-                        const float4 ui = fr[nb + g], uj = fr[nb + jg];
-                        const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
-                        if (norm3_rn(site_delta(pi, pj, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) <
-                            2.5f) {
-                            if (nlo < P.maxLong)
-                                lo_buf[nlo] = jl;
-                            else
-                                overflow = true;
-                            nlo++;
-                        }
+            }
+        }
+        float4 qq[4];   // four candidates in flight
+#pragma unroll
+        for (int u = 0; u < 4; u++) qq[u] = sl[u] >= 0 ? cell_pos[sl[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (sl[u] < 0) break;
+            const float4 q = qq[u];
+            const int jg = __float_as_int(q.w) & kCellIndexMask;
+            const int jl = jg - base;
+            const float cd = centre_dist(pi, q);
+            if (do_lj && jl != il && cd < P.ljcut) {
+                if (nlj >= P.maxLJ) {
+                    overflow = true;
+                } else if (nlj < kLocalLJ) {
+                    s_lj[nlj][threadIdx.x] = jl;
+                } else {
+                    if (nlj == kLocalLJ)  // spill the local part first
+                        for (int k = 0; k < kLocalLJ; k++) B.lj[k * nb + g] = s_lj[k][threadIdx.x];
+                    B.lj[nlj * nb + g] = jl;
+                }
+                nlj++;
+            }
+            if (do_pairs && cd < kPairReach && jl != hpart) {
+                const float4 pj = fr[jg];   // the exact state (q carries the index in w)
+                const float rmon = h0 < 0 ? -2.0f : 2.0f;
+                const int fj = B.flags[jg];
+                if (((flags ^ fj) & kFlagBeta) != 0) {
+                    const float4 ui = fr[nb + g], uj = fr[nb + jg];
+                    const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
+                    if (norm3_rn(site_delta(pi, pj, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon))) <
+                        2.5f) {
+                        if (nlo < P.maxLong)
+                            lo_buf[nlo] = jl;
+                        else
+                            overflow = true;
+                        nlo++;
                     }
-                    if (jl != il) {
-                        const float4 li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
-                        const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
-                        if (norm3_rn(site_delta(pi, pj, f3(li1), f3(l2))) < 2.5f) {
-                            if (nla < P.maxLat)
-                                la_buf[nla] = 2 * jl;       // orientation 0 -> -j
-                            else
-                                overflow = true;
-                            nla++;
-                        }
-                        if (norm3_rn(site_delta(pi, pj, f3(li2), f3(l1))) < 2.5f) {
-                            if (nla < P.maxLat)
-                                la_buf[nla] = 2 * jl + 1;   // orientation 1 -> +j
-                            else
-                                overflow = true;
-                            nla++;
-                        }
+                }
+                if (jl != il) {
+                    const float4 li1 = fr[2 * nb + g], li2 = fr[3 * nb + g];
+                    const float4 l1 = fr[2 * nb + jg], l2 = fr[3 * nb + jg];
+                    if (norm3_rn(site_delta(pi, pj, f3(li1), f3(l2))) < 2.5f) {
+                        if (nla < P.maxLat)
+                            la_buf[nla] = 2 * jl;       // orientation 0 -> -j
+                        else
+                            overflow = true;
+                        nla++;
+                    }
+                    if (norm3_rn(site_delta(pi, pj, f3(li2), f3(l1))) < 2.5f) {
+                        if (nla < P.maxLat)
+                            la_buf[nla] = 2 * jl + 1;   // orientation 1 -> +j
+                        else
+                            overflow = true;
+                        nla++;
                     }
                 }
             }
