@@ -1,0 +1,46 @@
+"""bench.py's reference arm (the CPU oracle port on the host cores) prints
+one JSON line with the keys of the bench contract, alone and as rank 0 of a
+two-rank torchrun whose other rank exits without work."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ARGS = ["--impl", "reference", "--workload", "plain_16x1520", "--steps", "1", "--warmup", "0"]
+
+
+def _json_lines(out: str):
+    return [json.loads(l) for l in out.splitlines() if l.startswith("{")]
+
+
+def _check(d, n_gpus):
+    assert d["impl"] == "reference" and d["n_gpus"] == n_gpus
+    for k in ("metric", "unit", "ms_per_step", "higher_is_better", "scaling", "dtype", "data", "config"):
+        assert k in d, k
+    assert d["value"] > 0 and d["vs_baseline"] is None and d["config"]["workload"] == "plain_16x1520"
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_json_line():
+    r = subprocess.run([sys.executable, "bench.py"] + ARGS, cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _json_lines(r.stdout)
+    assert len(lines) == 1
+    _check(lines[0], 1)
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", str(port), "bench.py", "--gpus", "2"] + ARGS
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _json_lines(r.stdout)
+    assert len(lines) == 1        # rank 0 alone prints
+    _check(lines[0], 2)
