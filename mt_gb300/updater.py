@@ -10,7 +10,6 @@ library's rand() reproduces the reference's choices.
 """
 from __future__ import annotations
 
-import math
 
 import numpy as np
 
