@@ -10,7 +10,6 @@ library's rand() reproduces the reference's choices.
 """
 from __future__ import annotations
 
-
 import numpy as np
 
 R_MON = 2.0
