@@ -33,13 +33,14 @@ def test_reference_arm_json_line():
     _check(lines[0], 1)
 
 
-def test_reference_arm_under_torchrun_two_ranks():
+def test_reference_arm_under_torchrun_two_ranks(tmp_path):
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
         port = s.getsockname()[1]
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(port), "bench.py", "--gpus", "2"] + ARGS
-    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
+    env = dict(os.environ, TMPDIR=str(tmp_path))   # torchrun's scratch stays in the test's folder
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)
     assert len(lines) == 1        # rank 0 alone prints
