@@ -456,3 +456,27 @@ def test_two_bead_trajectory(engine_mod, oracle_lib, method):
     assert np.array_equal(e2.download_rng(), so)
     np.testing.assert_allclose(e2.download_state()[:, :6], xo[:, :6], rtol=0, atol=5e-5)
     e2.close()
+
+
+@pytest.mark.parametrize("over", [dict(lj_on=0), dict(ljpairscutoff=5.0)], ids=["lj_off", "lj_cut_5nm"])
+@pytest.mark.parametrize("method", [1, 2])
+def test_assembly_lists_without_lj_prefilter(engine_mod, oracle_lib, over, method):
+    """Assembly lists when the LJ list cannot serve as their prefilter (LJ off,
+    or an LJ cutoff below the 6.6 nm reach of the site tests): the rebuild
+    runs the site tests itself.  Lists bit-exact, forces within 1e-5."""
+    b = system_with_margin(seed=21, **over)
+    e = make_engine(engine_mod, b)
+    e.set_list_method(method)
+    e.rebuild_pairs()
+    o = oracle_lib.Oracle("orc")
+    L = o.lists(b, b.coords)
+    # with LJ off the reference builds no LJ list at all (src/compute_cuda.cu:1141-1144)
+    for k in (("lj", "long", "lat") if b.params.lj_on else ("long", "lat")):
+        assert e.list_of_lists(k) == L.as_lists(k), k
+    if not b.params.lj_on:
+        assert all(len(x) == 0 for x in e.list_of_lists("lj"))
+    f = e.compute_forces()
+    fo = o.forces(b, b.coords, L)
+    for c in range(6):
+        assert rel_norm(f[:, c], fo[:, c]) < FORCE_RTOL, c
+    e.close()
