@@ -83,11 +83,16 @@ ref_only = pytest.mark.skipif(not __import__("oracle.oracle", fromlist=["x"]).re
 
 
 @ref_only
-@pytest.mark.parametrize("case", ["default", "walls_barrier_seam", "gdp_ontubule", "odd_pf", "lone_monomers"])
+@pytest.mark.parametrize("case", ["default", "walls_barrier_seam", "gdp_ontubule", "odd_pf", "lone_monomers",
+                                  "lj_off", "lj_cut_5nm"])
 def test_oracle_matches_reference_kernels(oracle_lib, case):
     over = {}
     if case == "walls_barrier_seam":
         over = dict(is_wall=1, rep_r=9.0, barrier=1, seam_coeff=1.7)
+    if case == "lj_off":
+        over = dict(lj_on=0)
+    if case == "lj_cut_5nm":
+        over = dict(ljpairscutoff=5.0)
     b = system_with_margin(seed=7, **over) if case != "odd_pf" else small_system(seed=9, n_mon=11)
     if case == "lone_monomers":
         b = with_lone_monomers(b)
