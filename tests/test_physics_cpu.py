@@ -67,3 +67,27 @@ def test_free_diffusion_temperature(oracle_lib):
     msd = np.concatenate(d2).mean()
     temp = p.gammaR * msd / (2 * synth.KB * p.dt)
     assert abs(temp / p.Temp - 1) < 0.02, temp
+
+
+def test_angular_forces_are_minus_the_energy_gradient(oracle_lib):
+    """With all bending equilibria at zero the generalised forces of the
+    three Euler angles (bending + site torques projected on the Euler axes)
+    are minus the angle derivatives of the energy.  With a non-zero theta0
+    they are not: the reference's bending energy and force use differently
+    ordered angle differences (src/compute_cuda.cu:158-164 against :751-756)."""
+    b = system_with_margin(seed=31, theta0_gtp=0.0, theta0_gdp=0.0, psi_0=0.0, fi_0=0.0)
+    o = oracle_lib.Oracle("orc", "f64")
+    x0 = b.coords.astype(np.float64)
+    L = o.lists(b, x0)
+    f = o.forces(b, x0, L)
+    beads = np.random.default_rng(0).choice(np.nonzero(b.extra == 0)[0], 12, replace=False)
+    h = 1e-5
+    for col in (3, 4, 5):                   # fi, theta, psi
+        fd = []
+        for i in beads:
+            xp, xm = x0.copy(), x0.copy()
+            xp[i, col] += h
+            xm[i, col] -= h
+            fd.append(-(o.energies(b, xp, L).sum() - o.energies(b, xm, L).sum()) / (2 * h))
+        an = f[beads, col]
+        assert np.linalg.norm(np.array(fd) - an) / np.linalg.norm(an) < 1e-7, col
