@@ -235,17 +235,27 @@ def ncu_traffic(kernel: str, workload: str):
 
 
 # ------------------------------------------------------------ CPU baseline
-def cpu_sample(spec: dict, seed: int, max_seconds: float = 20.0):
+def _omp_threads(n: int) -> bool:
+    """Sets the OpenMP thread count of this process (the oracle's libgomp)."""
+    import ctypes
+    try:
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(n))
+        return True
+    except (OSError, AttributeError):
+        return False
+
+
+def cpu_sample(spec: dict, seed: int, max_seconds: float = 20.0, single_core: bool = False):
     """Times the CPU oracle (all host threads) on a bounded sample: the first
     trajectories of the workload for one pair-list period (10 MD steps),
-    doubling the sample until it takes a few seconds."""
+    doubling the sample until it takes a few seconds.  With single_core, one
+    trajectory is also timed on one thread."""
     from mt_gb300 import synth
     from oracle import oracle
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
     o = oracle.Oracle("orc", "f32")
-    ntr = 1
-    best = None
-    while True:
+
+    def period_rate(ntr):
         b = make_batch(spec, seed, ntr)
         p = b.params
         seeds = o.generate_seeds(p.rseed, 2 * b.nbeads)
@@ -253,15 +263,26 @@ def cpu_sample(spec: dict, seed: int, max_seconds: float = 20.0):
         t0 = time.perf_counter()
         o.run(b, b.coords, seeds, 0, period)
         dt = time.perf_counter() - t0
-        best = (b.active_beads() * period / dt, ntr, dt, b.nbeads)
+        return b.active_beads() * period / dt, dt, b.nbeads
+
+    ntr = 1
+    while True:
+        rate, dt, nb = period_rate(ntr)
         if dt > 2.0 or ntr >= spec["ntraj"] or dt * 2 > max_seconds:
             break
         ntr *= 2
-    cores = os.cpu_count() or 1
-    rate, ntr, dt, nb = best
-    return {"value": rate, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", cores)), "kind": "port",
-            "sample": f"{ntr} of {spec['ntraj']} trajectories ({nb} beads) x {10} MD steps (one list period), "
-                      f"{dt:.2f} s"}
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    out = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{ntr} of {spec['ntraj']} trajectories ({nb} beads) x {10} MD steps (one list period), "
+                     f"{dt:.2f} s"}
+    if single_core and _omp_threads(1):
+        try:
+            r1, dt1, nb1 = period_rate(1)
+        finally:
+            _omp_threads(cores)
+        out["single_core"] = {"value": r1, "cores": 1,
+                              "sample": f"1 trajectory ({nb1} beads) x 10 MD steps, {dt1:.2f} s"}
+    return out
 
 
 def run_reference(args, spec, dist):
@@ -400,7 +421,7 @@ def run_gpu(args, spec, dist):
 
     out = None
     if dist.rank == 0:
-        cpu = cpu_sample(spec, seed) if dist.ws == 1 and not args.no_cpu_baseline else None
+        cpu = cpu_sample(spec, seed, single_core=True) if dist.ws == 1 and not args.no_cpu_baseline else None
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -545,7 +566,7 @@ def run_tea_compare(args, spec, dist):
     learned_ok = not results["learned"]["status"]["fell_back"]
     out = None
     if dist.rank == 0:
-        cpu = cpu_sample(dict(spec, kind="tea"), seed) if dist.ws == 1 and not args.no_cpu_baseline else None
+        cpu = cpu_sample(dict(spec, kind="tea"), seed, single_core=True) if dist.ws == 1 and not args.no_cpu_baseline else None
         L, X = results["learned"], results["exact"]
         out = {
             "metric": METRIC, "value": L["value"] if learned_ok else X["value"], "unit": UNIT, "n_gpus": dist.ws,
