@@ -314,12 +314,16 @@ int mtg_tea_update(mtg_engine *e, double *eps_out, float *beta_out, float *ci_ou
  * device array of 16384 x 7 doubles (917,504 bytes, held by every GPU that
  * loads the library until the process exits), so a batch may span at most
  * 16384 chunks of 128 beads (each trajectory is chunked separately; up to
- * 2,097,152 beads); larger batches get MTG_E_CONFIG.  The first call on a
- * device looks up that array's device address (make it before any stream
+ * 2,097,152 beads); larger batches get MTG_E_CONFIG.  The first call on
+ * each engine looks up that array's device address in the engine's context
+ * and keeps it in the engine (make that first call before any stream
  * capture).  Every call on a device shares the array: calls whose work
  * overlaps on the GPU (engines on different streams of the same device)
  * race and must be serialised by the caller.  Work is enqueued on the
- * engine's stream; mtg_sync() waits for it and reports a non-finite total. */
+ * engine's stream; mtg_sync() waits for it and reports a non-finite total.
+ * The caller's current device is restored before the call returns; a CUDA
+ * error already pending on the calling thread is reported as MTG_E_CUDA and
+ * left in place, and nothing is launched. */
 int mtg_energies_noalloc(mtg_engine *e, double *d_per_traj);
 
 /* ---- learned TEA ------------------------------------------------------- */
@@ -418,6 +422,12 @@ int mtg_graph_kernel_launches(mtg_engine *e, long long *launches, int reset);
  * per SM (5 runs each), the denominator of the roofline of the
  * FP32-pipe-bound TEA kernels. */
 int mtg_measure_fp32_tflops(int device, double *tflops);
+
+/* Architecture of the device code the library runs on `device`:
+ * binary_version = 10 * major + minor of its SASS (103 for sm_103a),
+ * ptx_version (may be NULL) of its PTX, from cudaFuncGetAttributes.  No
+ * reference counterpart (a build check: the library carries sm_103a code). */
+int mtg_device_code_version(int device, int *binary_version, int *ptx_version);
 
 /* Page-locked host buffers for fast state transfers (cudaHostAlloc). */
 int mtg_host_alloc(void **ptr, size_t bytes);

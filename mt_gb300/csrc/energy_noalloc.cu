@@ -9,8 +9,6 @@
 // reserved up front by a pool allocator, where a fresh cudaMalloc can fail.
 // Its scratch (the block partials) lives in a fixed, file-scope device array
 // instead, so the call itself allocates nothing.
-#include <mutex>
-
 #include "mtg_engine.cuh"
 
 namespace {
@@ -21,26 +19,34 @@ namespace {
 constexpr int kMaxChunks = 16384;
 static __device__ __align__(256) double g_energy_scratch[kMaxChunks * MTG_ENERGY_TERMS];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double *g_scratch_addr[kMaxDevices] = {nullptr};
-
-// Device address of g_energy_scratch on `device` (which must be current).
-// The host-side symbol is only a stand-in; a kernel needs this address.
-int scratch_address(int device, double **out) {
-    if (device < 0 || device >= kMaxDevices)
-        return mtg_internal_fail(MTG_E_CONFIG, "mtg_energies_noalloc: device index out of range");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[device]) {
+// Device address of g_energy_scratch in the current context.  The host-side
+// symbol is only a stand-in; a kernel needs this address.  It is looked up
+// once per engine (the engine's first call, with its device current) and kept
+// in the engine: an engine's buffers and this address belong to the same
+// context, so an engine created after the context was torn down and rebuilt
+// (cudaDeviceReset) looks the address up again instead of reusing a stale one.
+int scratch_address(mtg_engine *e, double **out) {
+    if (!e->noalloc_scratch) {
         void *p = nullptr;
         const cudaError_t err = cudaGetSymbolAddress(&p, g_energy_scratch);
         if (err != cudaSuccess)
             return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: cudaGetSymbolAddress of the scratch failed");
-        g_scratch_addr[device] = static_cast<double *>(p);
+        e->noalloc_scratch = static_cast<double *>(p);
     }
-    *out = g_scratch_addr[device];
+    *out = e->noalloc_scratch;
     return MTG_OK;
 }
+
+// Puts the caller's current device back on every return path.
+struct DeviceGuard {
+    int prev = -1;
+    DeviceGuard() {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 
 }  // namespace
 
@@ -51,16 +57,26 @@ extern "C" int mtg_energies_noalloc(mtg_engine *e, double *d_per_traj) {
         return mtg_internal_fail(MTG_E_CONFIG,
                                  "mtg_energies_noalloc: the batch needs more than 16384 chunks of 128 beads "
                                  "(trajectories are chunked separately); use mtg_energies");
+    DeviceGuard guard;
+    // an error left by earlier work of this thread is reported as such and
+    // left in place (peek, not get), so it is neither cleared nor blamed on
+    // this call's launches
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+        return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: a CUDA error was pending before the call "
+                                             "(left unreported by this call's launches)");
     if (cudaSetDevice(e->device) != cudaSuccess)
         return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: cudaSetDevice failed");
     double *scratch = nullptr;
-    const int rc = scratch_address(e->device, &scratch);
+    const int rc = scratch_address(e, &scratch);
     if (rc != MTG_OK) return rc;
     // every chunk's partials are overwritten by the energy kernel before the
     // totals kernel reads them, so nothing needs clearing between calls
     mtg::launch_energy(e->kp, e->bufs(), nullptr, scratch, e->work, e->nwork, e->stream);
+    if (cudaGetLastError() != cudaSuccess)
+        return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: energy kernel launch failed");
     mtg::launch_energy_totals(e->kp, scratch, e->work_first, d_per_traj, e->err, e->stream);
     if (cudaGetLastError() != cudaSuccess)
-        return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: kernel launch failed");
+        return mtg_internal_fail(MTG_E_CUDA, "mtg_energies_noalloc: totals kernel launch failed");
     return MTG_OK;
 }

@@ -84,6 +84,9 @@ struct mtg_engine {
     int hydro_ncand = -1;
     // stride-step outputs (output.cu)
     struct mtg_output *output = nullptr;
+    // device address of the fixed scratch of mtg_energies_noalloc, looked up
+    // by this engine's first call (energy_noalloc.cu)
+    double *noalloc_scratch = nullptr;
 
     mtg::CellBuffers cells() const {
         mtg::CellBuffers c{};

@@ -73,3 +73,20 @@ extern "C" int mtg_measure_fp32_tflops(int device, double *tflops) {
     *tflops = best;
     return MTG_OK;
 }
+
+// Architecture of the device code the library loads on `device`
+// (cudaFuncGetAttributes of one of its kernels: binaryVersion = major * 10 +
+// minor of the SASS that runs, ptxVersion of its PTX; 103 for sm_103a).
+extern "C" int mtg_device_code_version(int device, int *binary_version, int *ptx_version) {
+    if (!binary_version) return MTG_E_CONFIG;
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (cudaSetDevice(device) != cudaSuccess) return MTG_E_CUDA;
+    cudaFuncAttributes fa{};
+    const cudaError_t err = cudaFuncGetAttributes(&fa, k_fma_chain);
+    if (prev >= 0) cudaSetDevice(prev);
+    if (err != cudaSuccess) return MTG_E_CUDA;
+    *binary_version = fa.binaryVersion;
+    if (ptx_version) *ptx_version = fa.ptxVersion;
+    return MTG_OK;
+}

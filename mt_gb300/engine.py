@@ -65,6 +65,7 @@ EXPORTS = {
     "mtg_host_free": (C.c_int, [C.c_void_p]),
     "mtg_energies_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mtg_measure_fp32_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "mtg_device_code_version": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "mtg_set_list_method": (C.c_int, [C.c_void_p, C.c_int]),
     "mtg_get_list_method": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "mtg_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(MtgTuning)]),

@@ -189,6 +189,8 @@ void compute(Coord *r, Coord *f, Parameters &par, Topology &top, Energies *energ
         check(mtg_step(e, step, (int)(next - step)), "mtg_step");
         step = next;
     }
-    check(mtg_download_state(e, reinterpret_cast<float *>(r), nullptr), "mtg_download_state");
+    // deleteIntegration (src/compute_cuda.cu:1100-1123) copies nothing back:
+    // on return r holds the state of the last stride step, which main() then
+    // writes out (src/main.cpp:81)
     check(mtg_destroy(e), "mtg_destroy");
 }

@@ -40,7 +40,12 @@ def params_dict(p):
 
 
 def main():
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so", "ref"], check=True)
+    from oracle.reftree import reference_tree
+    ref = reference_tree()
+    if not ref:
+        raise SystemExit("the reference tree is needed (MTG_REFERENCE_TREE or a checkout beside this repository)")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so", "ref", f"REF={ref}"],
+                   check=True)
     # the reference's ran2 keeps static state: one seeding per process
     code = ("import sys, numpy as np; sys.path.insert(0, %r); from oracle import oracle as o;"
             "r = o.Oracle('ref'); s = r.generate_seeds(1234567, 64); st = s[:4].copy();"

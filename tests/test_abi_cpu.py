@@ -27,12 +27,15 @@ def test_library_exports_header(engine_mod):
     missing = declared_symbols() - exported
     assert not missing, missing
     # the Python binding declares every header entry point
-    assert declared_symbols() <= set(engine_mod.EXPORTS) | {"mtg_noalloc_placeholder"}
+    assert declared_symbols() <= set(engine_mod.EXPORTS)
 
 
-def test_library_is_sm103a(engine_mod):
-    out = subprocess.run(["cuobjdump", "--list-elf", engine_mod.LIB_PATH], capture_output=True, text=True).stdout
-    assert "sm_103a" in out
+def test_library_built_for_sm103a_only():
+    """The build compiles every translation unit for sm_103a alone (no PTX
+    for other targets, no multi-architecture fat binary); the GPU test
+    test_device_code_is_sm103a checks the loaded code at run time."""
+    from mt_gb300 import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 def test_derive_params_matches_reference_formula(engine_mod):

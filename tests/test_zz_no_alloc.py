@@ -37,6 +37,31 @@ def test_noalloc_totals_match_mtg_energies(engine_mod):
     e.close()
 
 
+def test_noalloc_calls_allocate_nothing(engine_mod):
+    """After a first call (which looks up the scratch address), further calls
+    leave the device's free memory unchanged: the property the entry point
+    exists for."""
+    import torch
+
+    b = small_system(seed=22, ntr=2)
+    e = engine_mod.Engine(b)
+    e.upload_state(b.coords)
+    e.rebuild_pairs()
+    lib = engine_mod.load()
+    out = torch.empty(b.ntraj * 7, dtype=torch.float64, device="cuda:0")
+    assert lib.mtg_energies_noalloc(e.h, C.c_void_p(out.data_ptr())) == 0
+    engine_mod.check(lib.mtg_sync(e.h))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for _ in range(20):
+        assert lib.mtg_energies_noalloc(e.h, C.c_void_p(out.data_ptr())) == 0
+    engine_mod.check(lib.mtg_sync(e.h))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, (free0, free1)
+    e.close()
+
+
 def test_noalloc_rejects_oversized_batch(engine_mod):
     """More chunks than the fixed scratch holds -> MTG_E_CONFIG with a message."""
     from mt_gb300 import synth
