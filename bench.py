@@ -24,8 +24,17 @@ roofline  the dominant kernel's algorithmic bytes per launch / its average
 cpu_baseline  the CPU oracle (the reference's algorithm restated in C, all
           host threads) on a bounded sample of the same workload.
 
---impl reference times that CPU implementation alone (the reference's own
-code path is CUDA-only and does not compile on the GPU host).
+The default run also measures the other configurations and adds them to
+the headline line as sub-objects, each with its own value, e2e, roofline
+and cpu_baseline: c1 (one 156-bead microtubule, 1e5 MD steps in one call,
+CPU baseline over the whole run on all threads and on one), c2_batched_plain
+(256 x 1520 beads), c3_ragged (the uneven 1024-trajectory batch) and
+c4_tea_exact (16 x 3300 beads, exact TEA).  --no-suite skips them.
+
+--impl reference times that CPU implementation alone: a port of the
+reference's algorithm, not the reference program (its CUDA sources do not
+travel to the GPU host, and its CPU-compilable kernel bodies cannot be built
+there), labelled "kind": "port".
 
 Multi-GPU (torchrun): each rank runs an independent copy of the workload
 (trajectories are independent: replicas, no collective); value = all
@@ -55,6 +64,11 @@ WORKLOADS = {
     # tubulin monomers (500 dimers, GDP) in a 100 nm cube; Morse, 8 nm LJ list
     # rebuilt every 10 steps; no hydrodynamics.
     "batched_plain_256x1520": dict(kind="plain", ntraj=256, n_mon=40, n_free=1000, cube=100.0),
+    # one straight 13 PF x 12 monomer lattice (156 beads, alternating alpha /
+    # beta), no free tubulin, no hydrodynamics: 1e5 MD steps in one call,
+    # pair lists rebuilt every 10 steps
+    "single_156": dict(kind="long", ntraj=1, n_mon=12, n_free=0, cube=100.0, md_steps=100_000,
+                       warm_md_steps=2_000),
     # small case for quick checks
     "plain_16x1520": dict(kind="plain", ntraj=16, n_mon=40, n_free=1000, cube=100.0),
     # uneven batch: 1024 trajectories, protofilament length U{8..120}, free
@@ -83,6 +97,15 @@ WORKLOADS = {
                                   cube=150.0, n_mon=64, n_free=1000, stride=100),
 }
 DEFAULT_WORKLOAD = "tea_learned_vs_exact_64x5600"
+# the other configurations, measured in the same default run and reported as
+# sub-objects of the headline line
+SUITE = (("c1", "single_156"), ("c2_batched_plain", "batched_plain_256x1520"), ("c3_ragged", "ragged_1024"),
+         ("c4_tea_exact", "tea_exact_16x3300"))
+SUB_KEYS = ("workload", "value", "unit", "ms_per_step", "steps", "warmup", "config", "roofline", "kernel_ms",
+            "kernel_share", "dominant_kernel", "gpu_launches", "e2e", "clocks", "cpu_baseline")
+PORT_NOTE = ("the oracle port: the reference's algorithm restated in C (oracle/), all host threads; the "
+             "reference program itself is not timed (its CUDA sources do not travel to the GPU host and no "
+             "aarch64 build of its CPU-compilable kernel bodies can be made here)")
 
 
 # ---------------------------------------------------------------- helpers
@@ -274,7 +297,7 @@ def cpu_sample(spec: dict, seed: int, max_seconds: float = 20.0, single_core: bo
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     out = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
            "sample": f"{ntr} of {spec['ntraj']} trajectories ({nb} beads) x {10} MD steps (one list period), "
-                     f"{dt:.2f} s"}
+                     f"{dt:.2f} s", "note": PORT_NOTE}
     if single_core and _omp_threads(1):
         try:
             r1, dt1, nb1 = period_rate(1)
@@ -282,6 +305,35 @@ def cpu_sample(spec: dict, seed: int, max_seconds: float = 20.0, single_core: bo
             _omp_threads(cores)
         out["single_core"] = {"value": r1, "cores": 1,
                               "sample": f"1 trajectory ({nb1} beads) x 10 MD steps, {dt1:.2f} s"}
+    return out
+
+
+def cpu_full_run(spec: dict, seed: int):
+    """The oracle port over the whole run of the single-trajectory
+    configuration (all md_steps), on all host threads and on one thread."""
+    from oracle import oracle
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
+    o = oracle.Oracle("orc", "f32")
+    b = make_batch(spec, seed)
+    n = int(spec["md_steps"])
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+    def rate():
+        seeds = o.generate_seeds(b.params.rseed, 2 * b.nbeads)
+        t0 = time.perf_counter()
+        o.run(b, b.coords, seeds, 0, n)
+        dt = time.perf_counter() - t0
+        return b.active_beads() * n / dt, dt
+
+    r_all, dt_all = rate()
+    out = {"value": r_all, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"the whole run: {b.nbeads} beads x {n} MD steps, {dt_all:.2f} s", "note": PORT_NOTE}
+    if _omp_threads(1):
+        try:
+            r1, dt1 = rate()
+        finally:
+            _omp_threads(cores)
+        out["single_core"] = {"value": r1, "cores": 1, "sample": f"the whole run on one thread, {dt1:.2f} s"}
     return out
 
 
@@ -318,14 +370,14 @@ def run_reference(args, spec, dist):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": args.workload, "sample_trajectories": ntr, "md_steps_per_bench_step": period},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
-                            "kind": "port",
+                            "kind": "port", "note": PORT_NOTE,
                             "sample": f"{ntr} of {spec['ntraj']} trajectories x {period} MD steps per bench step"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
 
 # ------------------------------------------------------------------ main
-def run_gpu(args, spec, dist):
+def run_gpu(args, spec, dist, cpu_seconds: float = 20.0):
     import torch
 
     from mt_gb300 import build as mbuild
@@ -421,7 +473,8 @@ def run_gpu(args, spec, dist):
 
     out = None
     if dist.rank == 0:
-        cpu = cpu_sample(spec, seed, single_core=True) if dist.ws == 1 and not args.no_cpu_baseline else None
+        cpu = cpu_sample(spec, seed, max_seconds=cpu_seconds, single_core=True) \
+            if dist.ws == 1 and not args.no_cpu_baseline else None
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -442,6 +495,117 @@ def run_gpu(args, spec, dist):
         }
     e.close()
     return out
+
+
+def run_long(args, spec, dist):
+    """The single-microtubule configuration: one trajectory, all md_steps MD
+    steps in one timed mtg_step call (graph replays of one pair-list period
+    each), after warm_md_steps untimed steps; the per-kernel timing for the
+    roofline comes from a separate 1000-step pass."""
+    import torch
+
+    from mt_gb300 import build as mbuild
+    from mt_gb300 import engine
+
+    mbuild.build()
+    torch.cuda.set_device(dist.local)
+    seed = 1 + dist.rank
+    b = make_batch(spec, seed)
+    b.params.device = dist.local
+    e = engine.Engine(b)
+    e.upload_state(b.coords)
+    period = int(b.params.ljpairsupdatefreq)
+    active = b.active_beads()
+    n = int(spec["md_steps"])
+    tune = e.autotune(0, period, cache=TUNE_CACHE, key=tune_key(b, args.workload))
+    step = 0
+    e.step(step, int(spec["warm_md_steps"]))
+    step += int(spec["warm_md_steps"])
+    e.set_kernel_timing(True)
+    e.step(step, 1000)
+    step += 1000
+    e.kernel_times(reset=True)
+    e.step(step, 1000)
+    step += 1000
+    kt = e.kernel_times(reset=True)
+    e.set_kernel_timing(False)
+    e.step(step, 1000)            # captures the untimed graphs again
+    step += 1000
+    e.graph_kernel_launches(reset=True)
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    ms = e.step_timed(step, n)
+    step += n
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    launches_timed = e.graph_kernel_launches(reset=True)
+    t_max = dist.max(ms)
+    value = dist.sum(active * n) / (t_max / 1e3)
+    kt_ms = {k: v[0] for k, v in kt.items()}
+    nl = {k: v[1] for k, v in kt.items()}
+    L = e.lists()
+    n_i = (L["lj"][0].astype(np.int64) + L["long"][0] + L["lat"][0] + b.harmonic_count).astype(np.int64)
+    work = float(np.sum((48 + 64 + 16 + 4 * n_i)[b.extra == 0]))
+    avg_ms = kt_ms["step_plain"] / max(1, nl["step_plain"])
+    peak, peak_kind = measured_peaks()
+    achieved = work / (avg_ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_step_plain", "achieved": achieved, "peak": peak, "peak_source": peak_kind,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": work,
+            "avg_launch_ms": avg_ms,
+            "note": "156 beads: the working set (about 20 KB) stays on chip; each launch is bound by its "
+                    "latency, not by HBM"}
+    # end to end through the C ABI: upload from pinned memory, the whole run, download
+    import ctypes as C
+    pin = engine.PinnedArray((e.nb, 7), np.float32)
+    pin.array[:] = e.download_state()
+    lib = engine.load()
+    fptr = pin.array.ctypes.data_as(C.POINTER(C.c_float))
+    t0 = time.perf_counter()
+    engine.check(lib.mtg_upload_state(e.h, fptr))
+    engine.check(lib.mtg_step(e.h, C.c_longlong(step), C.c_int(n)))
+    engine.check(lib.mtg_download_state(e.h, fptr, C.cast(None, C.POINTER(C.c_float))))
+    e2e_s = dist.max(time.perf_counter() - t0)
+    pin.free()
+    out = None
+    if dist.rank == 0:
+        cpu = cpu_full_run(spec, seed) if dist.ws == 1 and not args.no_cpu_baseline else None
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": 1, "warmup": 1,
+               "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic",
+               "config": {"workload": args.workload, "trajectories_per_gpu": b.ntraj, "beads_per_gpu": b.nbeads,
+                          "active_beads_per_gpu": active, "md_steps_per_bench_step": n,
+                          "warmup_md_steps": int(spec["warm_md_steps"]),
+                          "l2": "not flushed: the 20 KB state is cache-resident by design",
+                          "parallelism": f"replicas x{dist.ws} (independent trajectories)", "tuning": tune},
+               "roofline": roof,
+               "kernel_ms": {k: (kt_ms[k] / nl[k] if nl[k] else None) for k in kt_ms},
+               "kernel_share": {k: kt_ms[k] / max(1e-12, sum(kt_ms.values())) for k in kt_ms},
+               "dominant_kernel": max(kt_ms, key=lambda k: kt_ms[k]),
+               "gpu_launches": int(launches_timed),
+               "e2e": {"value": dist.sum(active * n) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 28 * e.nb,
+                       "d2h_bytes_per_step": 28 * e.nb},
+               "clocks": clk, "cpu_baseline": cpu}
+    e.close()
+    return out
+
+
+def run_suite_member(args, key: str, workload: str, dist):
+    """One configuration of the default run's suite, as a sub-object."""
+    import copy
+    sub = copy.copy(args)
+    sub.workload = workload
+    spec = WORKLOADS[workload]
+    if spec["kind"] == "long":
+        r = run_long(sub, spec, dist)
+    else:
+        r = run_gpu(sub, spec, dist, cpu_seconds=6.0)
+    if r is None:
+        return None
+    r = dict(r, workload=workload)
+    return {k: r[k] for k in SUB_KEYS if k in r}
 
 
 def train_surrogate(spec: dict, device: int, seed: int):
@@ -702,15 +866,26 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="mtg", choices=["mtg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU-oracle sample (profiling runs)")
+    ap.add_argument("--no-suite", action="store_true",
+                    help="default workload only, without the other configurations' sub-objects")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
     dist = Dist()
     try:
         if args.impl == "reference":
             run_reference(args, dict(spec, kind="tea") if spec["kind"] == "tea_compare" else
-                          dict(spec, kind="plain") if spec["kind"] == "stride" else spec, dist)
+                          dict(spec, kind="plain") if spec["kind"] in ("stride", "long") else spec, dist)
         elif spec["kind"] == "tea_compare":
             out = run_tea_compare(args, spec, dist)
+            if args.workload == DEFAULT_WORKLOAD and not args.no_suite:
+                for key, wl in SUITE:
+                    r = run_suite_member(args, key, wl, dist)
+                    if out is not None:
+                        out[key] = r
+            if out is not None:
+                print(json.dumps(out))
+        elif spec["kind"] == "long":
+            out = run_long(args, spec, dist)
             if out is not None:
                 print(json.dumps(out))
         elif spec["kind"] == "stride":

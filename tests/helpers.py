@@ -115,3 +115,51 @@ def with_lone_monomers(b, local=(160, 161)):
             b.harmonic_count[g] = 0
             b.harmonic[g * b.max_h:(g + 1) * b.max_h] = -1
     return b
+
+
+def per_bead_rel(got, ref, active, floor_frac):
+    """Largest per-bead relative error of vector rows: |got_i - ref_i| /
+    max(|ref_i|, floor_frac * RMS_i |ref_i|) over the active beads (row norms;
+    the floor keeps beads whose value nearly cancels from dominating)."""
+    got = np.asarray(got, np.float64)[active]
+    ref = np.asarray(ref, np.float64)[active]
+    if got.ndim == 1:
+        got, ref = got[:, None], ref[:, None]
+    mag = np.linalg.norm(ref, axis=1)
+    rms = float(np.sqrt(np.mean(mag ** 2))) if len(mag) else 0.0
+    if rms == 0.0:
+        return float(np.max(np.linalg.norm(got - ref, axis=1), initial=0.0)), 0.0
+    d = np.linalg.norm(got - ref, axis=1)
+    return float(np.max(d / np.maximum(mag, floor_frac * rms))), rms
+
+
+def site_tie_distance(batch, coords, g):
+    """FP64 distance of the closest longitudinal or lateral site test of bead g
+    (global index) to the 2.5 nm cutoff, over the beads of its trajectory."""
+    t = int(np.searchsorted(batch.offsets, g, side="right") - 1)
+    b0, b1 = int(batch.offsets[t]), int(batch.offsets[t + 1])
+    x = coords[b0:b1, :3].astype(np.float64)
+    R = rotations(coords[b0:b1])
+    uz = R[:, :, 2]
+    i = g - b0
+    p1, p2 = lateral_sites()
+    h0 = batch.harmonic[batch.max_h * g]
+    rmon = -2.0 if h0 < 0 else 2.0
+    worst = np.inf
+    si = x[i] + rmon * uz[i]
+    sj = x - rmon * uz
+    d = np.linalg.norm(sj - si, axis=1)
+    d[i] = np.inf
+    worst = min(worst, float(np.min(np.abs(d - 2.5))))
+    l1 = x + np.einsum("nij,j->ni", R, p1)
+    l2 = x + np.einsum("nij,j->ni", R, p2)
+    for a, c in ((l1, l2), (l2, l1)):
+        d = np.linalg.norm(c - a[i], axis=1)
+        d[i] = np.inf
+        worst = min(worst, float(np.min(np.abs(d - 2.5))))
+    return worst
+
+
+def ulp32(x):
+    """Spacing of FP32 numbers at |x|."""
+    return np.spacing(np.abs(np.asarray(x, np.float32))).astype(np.float64)
