@@ -88,7 +88,7 @@ WORKLOADS = {
     "tea_learned_vs_exact_64x5600": dict(kind="tea_compare", ntraj=64, n_mon=200, n_free=3000, cube=150.0,
                                          train=dict(ntraj=16, n_mon=100, n_free=2000, cube=100.0),
                                          samples=1_000_000, epochs=20, batch=4096, lr=1e-3, recheck=100,
-                                         max_err=0.01),
+                                         max_err=0.01, theta=0.85, ff_refresh=1000),
     # stride-step work on the uneven batch: every 100 steps a DCD frame of
     # every trajectory, the energy totals, mt_length and hydrolysis; the
     # asynchronous pipeline and the device analytics against the reference's
@@ -608,43 +608,79 @@ def run_suite_member(args, key: str, workload: str, dist):
     return {k: r[k] for k in SUB_KEYS if k in r}
 
 
-def train_surrogate(spec: dict, device: int, seed: int):
-    """Exact-TEA runs of the training system -> (descriptor, C_i, beta) samples -> network."""
+def tea_samples(tr: dict, device: int, seed: int, n: int, md_steps: int = 10_000):
+    """(descriptor, C_i, beta) samples from an exact-TEA run of the system tr:
+    snapshots spread evenly over md_steps MD steps (the 1e4 steps of the
+    exact-TEA configuration) until n samples are collected."""
     from mt_gb300 import engine
-    tr = dict(spec["train"], kind="tea")
-    b = make_batch(tr, seed + 1000)
+    b = make_batch(tr, seed)
     b.params.device = device
     e = engine.Engine(b)
     e.upload_state(b.coords)
-    Xs, Ts, step, n = [], [], 0, 0
-    t0 = time.perf_counter()
-    while n < spec["samples"]:
-        e.step(step, 10)
-        step += 10
+    snaps = -(-n // b.nbeads)
+    every = max(10, md_steps // snaps // 10 * 10)
+    Xs, Ts, step, k = [], [], 0, 0
+    while k < n:
+        e.step(step, every)
+        step += every
         X, T = e.tea_training_data()
         Xs.append(X)
         Ts.append(T)
-        n += len(X)
+        k += len(X)
     e.close()
-    X = np.concatenate(Xs)[:spec["samples"]]
-    T = np.concatenate(Ts)[:spec["samples"]]
+    return np.concatenate(Xs)[:n], np.concatenate(Ts)[:n], step
+
+
+def train_surrogate(spec: dict, device: int, seed: int):
+    """Exact-TEA runs of the training system -> (descriptor, C_i, beta) samples
+    -> network; its error on held-out trajectories (another seed of the same
+    system) against the mean predictor."""
+    from mt_gb300 import engine
+    tr = dict(spec["train"], kind="tea")
+    t0 = time.perf_counter()
+    X, T, steps = tea_samples(tr, device, seed + 1000, spec["samples"])
     t_data = time.perf_counter() - t0
+    Xv, Tv, _ = tea_samples(tr, device, seed + 2000, 100_000, md_steps=2_000)
     s = engine.Surrogate(device=device, seed=seed)
     t0 = time.perf_counter()
     losses = s.train(X, T, epochs=spec["epochs"], batch=spec["batch"], lr=spec["lr"], seed=seed)
     t_train = time.perf_counter() - t0
-    # the gain over the method without the network: mean-target predictor on held-out samples
-    hold = slice(0, min(len(X), 50_000))
-    pred = s.predict(X[hold])
-    rms_net = np.sqrt(((pred - T[hold]) ** 2).mean(0)).tolist()
-    rms_mean = np.sqrt(((T.mean(0) - T[hold]) ** 2).mean(0)).tolist()
-    info = {"samples": int(len(X)), "md_steps_of_exact_tea": step, "data_s": t_data, "train_s": t_train,
+    pred = s.predict(Xv)
+    rms_net = np.sqrt(((pred - Tv) ** 2).mean(0)).tolist()
+    rms_mean = np.sqrt(((T.mean(0) - Tv) ** 2).mean(0)).tolist()
+    info = {"samples": int(len(X)), "md_steps_of_exact_tea": steps, "data_s": t_data, "train_s": t_train,
             "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1]),
+            "held_out": f"{len(Xv)} samples of other trajectories of the training system",
             "rms_err_net_(Cx,Cy,Cz,beta)": rms_net, "rms_err_mean_predictor": rms_mean}
     return s, info
 
 
+def tea_effective_error(e, recompute_exact: bool, farfield: bool):
+    """RMS over active beads of |f - f_ref| / RMS |f_ref| for the effective TEA
+    forces of the current state under one draw of F and R (the noise streams
+    are restored, so both evaluations see the same R): f with the engine's
+    current C_i and beta (and the far-field product when farfield), f_ref
+    with freshly computed exact C_i and beta and the all-pairs product.
+    Leaves the exact C_i and beta in the engine when recompute_exact."""
+    seeds = e.download_rng()
+    if farfield:
+        _, f, _ = e.tea_effective_forces(exact=False, farfield=True)
+    else:
+        f, _, _ = e.tea_effective_forces(exact=True, farfield=False)
+    e.upload_rng(seeds)
+    if recompute_exact:
+        e.tea_update()
+    fr, _, _ = e.tea_effective_forces(exact=True, farfield=False)
+    act = e.batch.extra == 0
+    d = f[act, :3].astype(np.float64) - fr[act, :3]
+    return float(np.sqrt((d ** 2).sum(1).mean() / (fr[act, :3].astype(np.float64) ** 2).sum(1).mean()))
+
+
 def run_tea_compare(args, spec, dist):
+    """Exact TEA, exact TEA with stale epsilon (recomputed once per re-check
+    period, the zero-cost alternative to the network), and learned TEA (the
+    network's C_i and beta, the far-field mobility product, the exact re-check
+    every period) on the same batch, timed back to back."""
     import torch
 
     from mt_gb300 import build as mbuild
@@ -661,14 +697,18 @@ def run_tea_compare(args, spec, dist):
     active = b.active_beads()
     results = {}
     tune = None
-    for mode in ("exact", "learned"):
+    eps_freq = int(b.params.tea_epsilon_freq)
+    for mode in ("exact", "exact_stale_eps", "learned"):
+        b.params.tea_epsilon_freq = period if mode == "exact_stale_eps" else eps_freq
         e = engine.Engine(b)
         e.upload_state(b.coords)
-        if mode == "exact":   # launch shapes from the autotuner (exact TEA), used by both paths
+        if mode == "exact":   # launch shapes from the autotuner (exact TEA), used by every path
             tune = e.autotune(0, 10, cache=TUNE_CACHE, key=tune_key(b, args.workload))
         else:
             e.set_tuning(**tune["tuning"])
+        if mode == "learned":
             e.set_surrogate(surr, recheck_every=period, max_err=spec["max_err"])
+            e.set_tea_farfield(True, spec["theta"], refresh_every=spec["ff_refresh"])
         step = 0
         for _ in range(args.warmup):
             e.step(step, period)
@@ -700,6 +740,7 @@ def run_tea_compare(args, spec, dist):
                "gpu_launches": int(graph_kernels), "kt": kt}
         if mode == "learned":
             res["status"] = e.surrogate_status()
+            res["farfield"] = e.tea_farfield_stats()
         # e2e through the C ABI with pinned host buffers (one re-check period per step)
         import ctypes as C
         pin = engine.PinnedArray((e.nb, 7), np.float32)
@@ -717,21 +758,39 @@ def run_tea_compare(args, spec, dist):
         res["e2e"] = {"value": dist.sum(active * period * len(tt)) / dist.max(sum(tt)), "unit": UNIT,
                       "h2d_bytes_per_step": 28 * e.nb, "d2h_bytes_per_step": 28 * e.nb}
         pin.free()
+        # errors of the effective TEA forces against fresh exact TEA, on these
+        # (held-out) trajectories, at the end of a re-check period
+        e.step(step, period - 1)
+        step += period - 1
+        if mode == "exact_stale_eps":     # C_i, beta from period - 1 steps ago
+            res["mobility_error_vs_fresh_exact"] = tea_effective_error(e, True, False)
+        if mode == "learned":             # the network's C_i, beta (all-pairs), then the far field alone
+            res["mobility_error_network_only"] = tea_effective_error(e, True, False)
+            res["mobility_error_farfield_only"] = tea_effective_error(e, False, True)
         e.close()
         results[mode] = res
-    # roofline of the dominant kernel (the all-pairs mobility product)
+    b.params.tea_epsilon_freq = eps_freq
     import ctypes as C
     tf = C.c_double()
     engine.check(engine.load().mtg_measure_fp32_tflops(dist.local, C.byref(tf)))
-    kt = results["learned"]["kt"]
-    avg = kt["tea_step"][0] / max(1, kt["tea_step"][1])
-    work = 45.0 * tea_pairs(b)
-    achieved = work / (avg / 1e3) / 1e12
-    learned_ok = not results["learned"]["status"]["fell_back"]
+
+    def fp32_roof(kt, kind, kernel, work, note):
+        avg = kt[kind][0] / max(1, kt[kind][1])
+        ach = work / (avg / 1e3) / 1e12
+        return {"bound": "fp32", "kernel": kernel, "achieved": ach, "peak": tf.value,
+                "peak_source": "measured FP32 FMA rate (mtg_measure_fp32_tflops)", "unit": "TFLOP/s",
+                "frac": ach / tf.value, "traffic": ncu_traffic(kernel, args.workload),
+                "algorithmic_flop_per_launch": work, "avg_launch_ms": avg, "work": note}
+
+    L, X, S = results["learned"], results["exact"], results["exact_stale_eps"]
+    learned_ok = not L["status"]["fell_back"]
+    ffs = L["farfield"]
+    roof_exact = fp32_roof(X["kt"], "tea_step", "k_tea_step", 45.0 * tea_pairs(b), "45 FLOP per ordered pair")
+    roof_ff = fp32_roof(L["kt"], "ff_step", "k_ff_step", 45.0 * ffs["near_pairs"],
+                        "45 FLOP per ordered near pair (the pair loop; interpolation and update not counted)")
     out = None
     if dist.rank == 0:
         cpu = cpu_sample(dict(spec, kind="tea"), seed, single_core=True) if dist.ws == 1 and not args.no_cpu_baseline else None
-        L, X = results["learned"], results["exact"]
         out = {
             "metric": METRIC, "value": L["value"] if learned_ok else X["value"], "unit": UNIT, "n_gpus": dist.ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": L["ms_per_step"],
@@ -739,21 +798,27 @@ def run_tea_compare(args, spec, dist):
             "data": "synthetic",
             "config": {"workload": args.workload, "trajectories_per_gpu": b.ntraj, "beads_per_gpu": b.nbeads,
                        "md_steps_per_bench_step": period, "recheck_every": period, "max_mobility_error": spec["max_err"],
+                       "farfield_theta": spec["theta"], "farfield_refresh_every": spec["ff_refresh"],
                        "tuning": tune,
                        "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{dist.ws} (independent trajectories)"},
             "learned_tea": {"value": L["value"], "fell_back": not learned_ok,
                             "mobility_error_last_recheck": L["status"]["last_error"],
-                            "rechecks": L["status"]["rechecks"], "kernel_ms": L["kernel_ms"],
+                            "mobility_error_network_only": L["mobility_error_network_only"],
+                            "mobility_error_farfield_only": L["mobility_error_farfield_only"],
+                            "rechecks": L["status"]["rechecks"], "farfield": ffs,
+                            "ordered_pairs_all": tea_pairs(b), "kernel_ms": L["kernel_ms"],
                             "kernel_share": L["kernel_share"]},
             "exact_tea": {"value": X["value"], "ms_per_step": X["ms_per_step"], "kernel_ms": X["kernel_ms"],
-                          "kernel_share": X["kernel_share"], "e2e": X["e2e"]},
+                          "kernel_share": X["kernel_share"], "e2e": X["e2e"], "roofline": roof_exact},
+            "exact_tea_stale_epsilon": {"value": S["value"], "ms_per_step": S["ms_per_step"],
+                                        "epsilon_every": period,
+                                        "mobility_error_vs_fresh_exact": S["mobility_error_vs_fresh_exact"],
+                                        "kernel_ms": S["kernel_ms"]},
             "learned_over_exact": L["value"] / X["value"],
+            "learned_over_exact_stale_epsilon": L["value"] / S["value"],
             "surrogate_training": train_info,
-            "roofline": {"bound": "fp32", "kernel": "k_tea_step", "achieved": achieved, "peak": tf.value,
-                         "peak_source": "measured FP32 FMA rate (mtg_measure_fp32_tflops)", "unit": "TFLOP/s",
-                         "frac": achieved / tf.value, "traffic": ncu_traffic("k_tea_step", args.workload),
-                         "algorithmic_flop_per_launch": work, "avg_launch_ms": avg},
+            "roofline": roof_ff,
             "gpu_launches": L["gpu_launches"],
             "e2e": L["e2e"] if learned_ok else X["e2e"],
             "clocks": L["clocks"],

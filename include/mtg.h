@@ -369,6 +369,41 @@ int mtg_set_surrogate(mtg_engine *e, mtg_surrogate *s, int recheck_every, float 
  * last re-check's RMS relative difference. */
 int mtg_surrogate_status(mtg_engine *e, int *fell_back, int *rechecks, double *last_error);
 
+/* Far field of the learned mode's mobility product.  No reference
+ * counterpart: the reference sums T_ij over all pairs of a trajectory at
+ * every step (src/bdhitea_kernel.cu:174-180) and declares, but does not
+ * build, a listed variant (src/mt.h:118).  With on != 0, while the surrogate
+ * is in charge (mtg_set_surrogate), each trajectory's non-extra beads are
+ * grouped into leaves of at most 64 beads (a k-d bisection of the current
+ * positions); pairs in leaves near each other are summed exactly as the
+ * exact product does, and a leaf far from another (centres farther apart
+ * than (r_I + r_J + 2 nm) / theta, r the leaves' radii) acts on it through 8
+ * interpolation points per leaf (trilinear Chebyshev proxies of its bounding
+ * box, recomputed every step), in place of its beads.  The exact re-check of
+ * the learned mode then compares this product (with the surrogate's C_i and
+ * beta) against the exact one, and the fall-back to exact TEA covers both.
+ * theta in (0, 1]: smaller is more accurate and slower.  refresh_every: the
+ * grouping is rebuilt on the host from the current positions every that many
+ * steps (0: only here), before the step that reaches it. */
+int mtg_set_tea_farfield(mtg_engine *e, int on, float theta, int refresh_every);
+/* The grouping's leaves, the bead pairs summed exactly per step, and the
+ * proxy pairs evaluated per step (zeros while off). */
+int mtg_tea_farfield_stats(mtg_engine *e, int *nleaves, long long *near_pairs, long long *proxy_pairs);
+/* The grouping: sizes[4] = leaves, beads in leaves, near entries, far
+ * entries; leaf_start [leaves+1] into leaf_bead (bead indices, leaf after
+ * leaf); near_start / far_start [leaves+1] into near / far (leaf indices).
+ * Call with NULL arrays for the sizes first. */
+int mtg_tea_farfield_layout(mtg_engine *e, int *sizes, int *leaf_start, int *leaf_bead, int *near_start,
+                            int *near, int *far_start, int *far);
+/* Effective TEA forces f_i = F_i + C_i o R_i + sum_j T_ij (F_j + beta C_i o R_j)
+ * (the x, y, z of [nbeads*4]) of the current state with the engine's current
+ * C_i and beta, from one force evaluation and one draw of random forces:
+ * feff_exact by the all-pairs product, feff_ff by the far-field one (needs
+ * the far field on); rforce [nbeads*4] receives the random forces.  Any
+ * pointer may be NULL.  The draw advances the noise streams g as a step's
+ * does.  No reference counterpart (for checks of the approximation). */
+int mtg_tea_effective_forces(mtg_engine *e, float *feff_exact, float *feff_ff, float *rforce);
+
 /* ---- tuning ------------------------------------------------------------ */
 /* Launch shapes of the engine's kernels.  list_method as
  * mtg_set_list_method (1 tiles, 2 cells); step_block: threads per CTA of the
@@ -407,8 +442,9 @@ int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *devic
  * is counted; the call count below says how many launches were timed.)
  * Kinds: 0 pair-list rebuild, 1 fused plain step, 2 forces (+ TEA random
  * forces), 3 TEA epsilon pass, 4 TEA beta reduction, 5 TEA mobility step,
- * 6 learned-TEA descriptors + network + C_i/beta, 7 learned-TEA re-check. */
-#define MTG_KERNEL_KINDS 8
+ * 6 learned-TEA descriptors + network + C_i/beta, 7 learned-TEA re-check,
+ * 8 far-field proxies (charges and far potentials), 9 far-field mobility step. */
+#define MTG_KERNEL_KINDS 10
 int mtg_set_kernel_timing(mtg_engine *e, int on);
 int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int reset);
 /* Kernel launches replayed from the engine's step graphs since the last

@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
-SOURCES = ["mtg_api.cu", "kernels_step.cu", "kernels_lists.cu", "kernels_cells.cu", "kernels_tea.cu", "energy_noalloc.cu", "peak_probe.cu", "kernels_mlp.cu", "kernels_mlp_tc.cu", "kernels_mlp_train_tc.cu", "surrogate.cu", "restart.cu", "kernels_updater.cu", "output.cu"]
+SOURCES = ["mtg_api.cu", "kernels_step.cu", "kernels_lists.cu", "kernels_cells.cu", "kernels_tea.cu", "tea_ff.cu", "energy_noalloc.cu", "peak_probe.cu", "kernels_mlp.cu", "kernels_mlp_tc.cu", "kernels_mlp_train_tc.cu", "surrogate.cu", "restart.cu", "kernels_updater.cu", "output.cu"]
 
 
 def nvcc() -> str:

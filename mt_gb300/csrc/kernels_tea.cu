@@ -511,6 +511,7 @@ template <int SLICES, bool FEFF, bool SPLIT>
 __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KParams P, DevBuffers B, const int2 *work,
                                                                  float4 *feff, const int *gate) {
     if (FEFF && gate && *gate != 0) return;
+    if (!FEFF && gate && *gate == 0) return;   // the gated update runs after a fall-back only
     int item, part, parts;
     tea_item<SPLIT>(P, item, part, parts);
     const int2 w = work[item];
@@ -644,6 +645,7 @@ __global__ void __launch_bounds__(kTeaLanes *SLICES, 20 / SLICES) k_tea_step(KPa
 template <bool FEFF>
 __global__ void k_tea_step_finish(KParams P, DevBuffers B, const int2 *work, float4 *feff, const int *gate) {
     if (FEFF && gate && *gate != 0) return;
+    if (!FEFF && gate && *gate == 0) return;
     const int g = tea_tail_bead(P, B, work);
     if (g < 0) return;
     float4 acc = B.tea_part[g];
@@ -733,9 +735,386 @@ static void tea_step_dispatch(const KParams &P, const DevBuffers &B, const int2 
 void launch_tea_step(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, cudaStream_t s) {
     tea_step_dispatch<false>(P, B, work, nwork, nullptr, nullptr, s);
 }
+void launch_tea_step_gated(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
+                           cudaStream_t s) {
+    tea_step_dispatch<false>(P, B, work, nwork, nullptr, gate, s);
+}
 void launch_tea_feff(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, float4 *feff,
                      const int *gate, cudaStream_t s) {
     tea_step_dispatch<true>(P, B, work, nwork, feff, gate, s);
+}
+
+// ---------------------------------------------- far field of learned TEA
+// The learned mode's approximation of sum_j T_ij (F_j + beta C_i o R_j):
+// pairs of beads in near leaves are summed exactly (the packed pair loop of
+// k_tea_step over one source leaf per tile), and every far leaf J acts on a
+// target leaf I through proxies: J's sources are spread onto the 8 corners
+// of a Chebyshev grid in its bounding box (P2M, trilinear Lagrange weights at
+// nodes +-h/sqrt(2)), the RPY far field of those 8 charges is evaluated at
+// the 8 grid points of I (M2L) and interpolated back to I's beads (L2P).
+// Because C_i weights R_j per component and per target, the proxies carry F
+// and R separately and the targets receive A = T Q_F and B_k = T e_k Q_R,k
+// (k = x, y, z); a bead adds A + sum_k beta C_ik B_k.  Far means the leaves'
+// centres are farther apart than (r_I + r_J + margin) / theta (tea_ff.cu).
+
+// Tile of one source leaf, in the layout of TeaTile.
+struct FFTile {
+    float4 xy[kFFLeaf];
+    float4 zf[kFFLeaf];
+    float4 fyz[kFFLeaf];
+    float4 rxy[kFFLeaf];
+    float2 rz[kFFLeaf];
+};
+
+__device__ __forceinline__ void ff_tile_load(FFTile &T, const DevBuffers &B, const FFBuffers &F, int leaf) {
+    const int s = F.leaf_start[leaf], n = F.leaf_start[leaf + 1] - s;
+    for (int k = threadIdx.x; k < kFFLeaf; k += blockDim.x) {
+        float4 p = make_float4(kFarAway, kFarAway, kFarAway, 0.f), Fv = make_float4(0.f, 0.f, 0.f, 0.f), R = Fv;
+        if (k < n) {
+            const int g = F.leaf_bead[s + k];
+            p = B.frame_in[g];
+            Fv = B.force[g];
+            R = B.tea_r[g];
+        }
+        T.xy[k] = make_float4(p.x, p.x, p.y, p.y);
+        T.zf[k] = make_float4(p.z, p.z, Fv.x, Fv.x);
+        T.fyz[k] = make_float4(Fv.y, Fv.y, Fv.z, Fv.z);
+        T.rxy[k] = make_float4(R.x, R.x, R.y, R.y);
+        T.rz[k] = f2(R.z);
+    }
+}
+
+// Trilinear Lagrange weights of the 8 proxies (bit 0: x, bit 1: y, bit 2: z;
+// a clear bit is the node at -h/sqrt(2), a set bit the one at +h/sqrt(2)) at
+// position x of a box (c, h).
+__device__ __forceinline__ void ff_weights(float3 x, float4 c, float4 h, float w[8]) {
+    const float tx = (x.x - c.x) / (h.x * kFFNode), ty = (x.y - c.y) / (h.y * kFFNode),
+                tz = (x.z - c.z) / (h.z * kFFNode);
+    const float lx[2] = {0.5f * (1.0f - tx), 0.5f * (1.0f + tx)};
+    const float ly[2] = {0.5f * (1.0f - ty), 0.5f * (1.0f + ty)};
+    const float lz[2] = {0.5f * (1.0f - tz), 0.5f * (1.0f + tz)};
+#pragma unroll
+    for (int m = 0; m < 8; m++) w[m] = lx[m & 1] * ly[(m >> 1) & 1] * lz[(m >> 2) & 1];
+}
+__device__ __forceinline__ float3 ff_proxy(float4 c, float4 h, int m) {
+    return make_float3(c.x + ((m & 1) ? kFFNode : -kFFNode) * h.x, c.y + ((m & 2) ? kFFNode : -kFFNode) * h.y,
+                       c.z + ((m & 4) ? kFFNode : -kFFNode) * h.z);
+}
+
+// P2M: one CTA of kFFLeaf threads per leaf, one bead per thread: the leaf's
+// bounding box, then the proxy charges Q_m = sum_j w_m(x_j) (F_j, R_j).
+__global__ void __launch_bounds__(kFFLeaf) k_ff_p2m(KParams P, DevBuffers B, FFBuffers F, const int *gate) {
+    if (gate && *gate != 0) return;
+    const int L = blockIdx.x, t = threadIdx.x;
+    const int s = F.leaf_start[L], n = F.leaf_start[L + 1] - s;
+    __shared__ float sw[kFFLeaf][9];
+    __shared__ float sv[kFFLeaf][7];
+    __shared__ float3 slo[kFFLeaf / 32], shi[kFFLeaf / 32];
+    float3 x = make_float3(0.f, 0.f, 0.f), lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f);
+    float3 hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+    float4 Fv = make_float4(0.f, 0.f, 0.f, 0.f), R = Fv;
+    if (t < n) {
+        const int g = F.leaf_bead[s + t];
+        x = f3(B.frame_in[g]);
+        Fv = B.force[g];
+        R = B.tea_r[g];
+        lo = hi = x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
+        lo.y = fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o));
+        lo.z = fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o));
+        hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
+        hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
+        hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
+    }
+    if ((t & 31) == 0) {
+        slo[t >> 5] = lo;
+        shi[t >> 5] = hi;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kFFLeaf / 32; k++) {
+        lo = make_float3(fminf(lo.x, slo[k].x), fminf(lo.y, slo[k].y), fminf(lo.z, slo[k].z));
+        hi = make_float3(fmaxf(hi.x, shi[k].x), fmaxf(hi.y, shi[k].y), fmaxf(hi.z, shi[k].z));
+    }
+    const float4 c = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.f);
+    const float4 h = make_float4(fmaxf(0.5f * (hi.x - lo.x), 1e-3f), fmaxf(0.5f * (hi.y - lo.y), 1e-3f),
+                                 fmaxf(0.5f * (hi.z - lo.z), 1e-3f), 0.f);
+    float w[8];
+    ff_weights(x, c, h, w);
+#pragma unroll
+    for (int m = 0; m < 8; m++) sw[t][m] = t < n ? w[m] : 0.f;
+    sv[t][0] = Fv.x;
+    sv[t][1] = Fv.y;
+    sv[t][2] = Fv.z;
+    sv[t][3] = R.x;
+    sv[t][4] = R.y;
+    sv[t][5] = R.z;
+    __syncthreads();
+    if (t < 48) {
+        const int m = t / 6, v = t % 6;
+        float acc = 0.f;
+        for (int j = 0; j < n; j++) acc = fmaf(sw[j][m], sv[j][v], acc);
+        // (QF.xyz, QR.x) at float4 16L + m, (QR.y, QR.z) at 16L + 8 + m
+        float *q = reinterpret_cast<float *>(F.q);
+        q[(size_t)4 * (16 * L + (v < 4 ? m : 8 + m)) + (v < 4 ? v : v - 4)] = acc;
+    }
+    if (t == 0) {
+        F.box[2 * L] = c;
+        F.box[2 * L + 1] = h;
+    }
+}
+
+// M2L: one CTA of 128 threads per target leaf; thread t serves target proxy
+// t % 8 over every 16th far leaf, the 16 slices meet in shared memory.
+__global__ void __launch_bounds__(128) k_ff_m2l(KParams P, FFBuffers F, const int *gate) {
+    if (gate && *gate != 0) return;
+    const int L = blockIdx.x, t = threadIdx.x, n = t & 7, sl = t >> 3;
+    const TeaConst K = tea_const(P.tea_a);
+    const float3 xn = ff_proxy(F.box[2 * L], F.box[2 * L + 1], n);
+    float acc[12];
+#pragma unroll
+    for (int c = 0; c < 12; c++) acc[c] = 0.f;
+    for (int k = F.far_start[L] + sl; k < F.far_start[L + 1]; k += 16) {
+        const int J = F.far[k];
+        const float4 cJ = F.box[2 * J], hJ = F.box[2 * J + 1];
+#pragma unroll 2
+        for (int m = 0; m < 8; m++) {
+            const float3 y = ff_proxy(cJ, hJ, m);
+            const float dx = y.x - xn.x, dy = y.y - xn.y, dz = y.z - xn.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float rinv = rsqrt_hw(r2), q2 = rinv * rinv, tq = q2 * rinv;
+            const float cii = fmaf(K.kap, tq, rinv);
+            const float cr = tq * fmaf(-K.two_a2, q2, 1.0f);
+            const float4 qa = F.q[16 * J + m], qb = F.q[16 * J + 8 + m];
+            const float sF = cr * fmaf(dx, qa.x, fmaf(dy, qa.y, dz * qa.z));
+            acc[0] = fmaf(cii, qa.x, fmaf(sF, dx, acc[0]));
+            acc[1] = fmaf(cii, qa.y, fmaf(sF, dy, acc[1]));
+            acc[2] = fmaf(cii, qa.z, fmaf(sF, dz, acc[2]));
+            const float s0 = cr * dx * qa.w, s1 = cr * dy * qb.x, s2 = cr * dz * qb.y;
+            acc[3] = fmaf(cii, qa.w, fmaf(s0, dx, acc[3]));
+            acc[4] = fmaf(s0, dy, acc[4]);
+            acc[5] = fmaf(s0, dz, acc[5]);
+            acc[6] = fmaf(s1, dx, acc[6]);
+            acc[7] = fmaf(cii, qb.x, fmaf(s1, dy, acc[7]));
+            acc[8] = fmaf(s1, dz, acc[8]);
+            acc[9] = fmaf(s2, dx, acc[9]);
+            acc[10] = fmaf(s2, dy, acc[10]);
+            acc[11] = fmaf(cii, qb.y, fmaf(s2, dz, acc[11]));
+        }
+    }
+    __shared__ float red[128][13];
+#pragma unroll
+    for (int c = 0; c < 12; c++) red[t][c] = acc[c];
+    __syncthreads();
+    if (t < 96) {
+        const int pn = t / 12, c = t % 12;
+        float v = 0.f;
+#pragma unroll
+        for (int k = 0; k < 16; k++) v += red[k * 8 + pn][c];
+        reinterpret_cast<float *>(F.phi)[(size_t)96 * L + 12 * pn + c] = v;
+    }
+}
+
+// The packed pass of one source leaf for one packed pair of target beads
+// (self pairs pushed to r^2 = 1e30 when SELF), running minimum of r^2.
+template <int SLICES, bool SELF>
+__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_t, float2 nx, float2 ny, float2 nz,
+                                             float2 cbx, float2 cby, float2 cbz, float2 vkap, float2 vn2a2,
+                                             float2 one, float2 &ax, float2 &ay, float2 &az,
+                                             float (&rmin)[kTeaSeg]) {
+    constexpr int kLen = kFFLeaf / SLICES / kTeaSeg;
+#pragma unroll
+    for (int sg = 0; sg < kTeaSeg; sg++) {
+#pragma unroll
+        for (int k = 0; k < kLen; k++) {
+            const int t = sl + (sg * kLen + k) * SLICES;
+            const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
+            const float2 dx = __fadd2_rn(lo2(a), nx), dy = __fadd2_rn(hi2(a), ny), dz = __fadd2_rn(lo2(b), nz);
+            const float2 gx = __ffma2_rn(lo2(d), cbx, hi2(b)), gy = __ffma2_rn(hi2(d), cby, lo2(c)),
+                         gz = __ffma2_rn(T.rz[t], cbz, hi2(c));
+            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            if (SELF) {
+                if (t == self_t) r2.x = 1e30f;
+                if (t == self_t + kTeaLanes) r2.y = 1e30f;
+            }
+            rmin[sg] = fmin3(rmin[sg], r2.x, r2.y);
+            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+            const float2 q = __fmul2_rn(rinv, rinv);
+            const float2 tq = __fmul2_rn(q, rinv);
+            const float2 cii = __ffma2_rn(vkap, tq, rinv);
+            const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
+            const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
+            ax = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax));
+            ay = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay));
+            az = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az));
+        }
+    }
+}
+
+// Near pairs, far field and update: one CTA of 32 x SLICES threads per
+// target leaf; lane il serves the leaf's beads il and il + 32 as one packed
+// pair, the SLICES threads of a lane take interleaved beads of every source
+// leaf of the near list.  Overlapping pairs (r <= 2a) are corrected as in
+// k_tea_step.  Then the far field is interpolated from the leaf's proxies and
+// the bead moves (FEFF: its effective force goes to feff instead).
+template <int SLICES, bool FEFF>
+__global__ void __launch_bounds__(kTeaLanes *SLICES) k_ff_step(KParams P, DevBuffers B, FFBuffers F, float4 *feff,
+                                                               const int *gate) {
+    if (gate && *gate != 0) return;
+    const int L = blockIdx.x;
+    const int il = threadIdx.x % kTeaLanes, sl = threadIdx.x / kTeaLanes;
+    const int s0 = F.leaf_start[L], n = F.leaf_start[L + 1] - s0;
+    const int traj = F.leaf_traj[L];
+    __shared__ FFTile T;
+    __shared__ float4 s_red[2 * kTeaLanes * SLICES];
+    __shared__ float4 s_phi[24];
+    const float beta = B.tea_beta[traj], b2 = beta * beta;
+    int gi[2];
+    float4 pi[2], cb[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int k = il + h * kTeaLanes;
+        gi[h] = k < n ? F.leaf_bead[s0 + k] : -1;
+        pi[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+        cb[h] = pi[h];
+        if (gi[h] >= 0) {
+            pi[h] = B.frame_in[gi[h]];
+            const float4 ci = B.tea_ci[gi[h]];
+            cb[h] = make_float4(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
+                                beta / sqrtf(1.0f + b2 * ci.z), 0.f);
+        }
+    }
+    const float2 nx = make_float2(-pi[0].x, -pi[1].x), ny = make_float2(-pi[0].y, -pi[1].y),
+                 nz = make_float2(-pi[0].z, -pi[1].z);
+    const float2 cbx = make_float2(cb[0].x, cb[1].x), cby = make_float2(cb[0].y, cb[1].y),
+                 cbz = make_float2(cb[0].z, cb[1].z);
+    float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f);
+    const TeaConst K = tea_const(P.tea_a);
+    const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
+    for (int e = F.near_start[L]; e < F.near_start[L + 1]; e++) {
+        const int J = F.near[e];
+        ff_tile_load(T, B, F, J);
+        __syncthreads();
+        float rmin[kTeaSeg];
+#pragma unroll
+        for (int sg = 0; sg < kTeaSeg; sg++) rmin[sg] = 3.4e38f;
+        const bool self = J == L;
+        if (self)
+            ff_step_tile<SLICES, true>(T, sl, il, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az, rmin);
+        else
+            ff_step_tile<SLICES, false>(T, sl, il, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az, rmin);
+        unsigned segs = 0;
+#pragma unroll
+        for (int sg = 0; sg < kTeaSeg; sg++) segs |= (rmin[sg] <= K.four_a2 ? 1u : 0u) << sg;
+        constexpr int kLen = kFFLeaf / SLICES / kTeaSeg;
+        while (segs) {  // the segments that hold an overlapping pair
+            const int sg = __ffs(segs) - 1;
+            segs &= segs - 1;
+            for (int k = 0; k < kLen; k++) {
+                const int t = sl + (sg * kLen + k) * SLICES;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    if (self && t == il + h * kTeaLanes) continue;
+                    const float dx = T.xy[t].x + (h ? nx.y : nx.x), dy = T.xy[t].z + (h ? ny.y : ny.x),
+                                dz = T.zf[t].x + (h ? nz.y : nz.x);
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    if (!(r2 <= K.four_a2)) continue;
+                    const float gx = fmaf(T.rxy[t].x, h ? cbx.y : cbx.x, T.zf[t].z),
+                                gy = fmaf(T.rxy[t].z, h ? cby.y : cby.x, T.fyz[t].x),
+                                gz = fmaf(T.rz[t].x, h ? cbz.y : cbz.x, T.fyz[t].z);
+                    const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+                    const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
+                    if (h) {
+                        ax.y += nr.x - fa.x;
+                        ay.y += nr.y - fa.y;
+                        az.y += nr.z - fa.z;
+                    } else {
+                        ax.x += nr.x - fa.x;
+                        ay.x += nr.y - fa.y;
+                        az.x += nr.z - fa.z;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    s_red[(sl * 2 + 0) * kTeaLanes + il] = make_float4(ax.x, ay.x, az.x, 0.f);
+    s_red[(sl * 2 + 1) * kTeaLanes + il] = make_float4(ax.y, ay.y, az.y, 0.f);
+    if (threadIdx.x < 24) s_phi[threadIdx.x] = F.phi[24 * L + threadIdx.x];
+    __syncthreads();
+    if (sl != 0) return;
+    const float4 c = F.box[2 * L], hb = F.box[2 * L + 1];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        if (gi[h] < 0) continue;
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        for (int k = 0; k < SLICES; k++) {
+            const float4 v = s_red[(k * 2 + h) * kTeaLanes + il];
+            sx += v.x;
+            sy += v.y;
+            sz += v.z;
+        }
+        // far field interpolated from the leaf's 8 proxies (L2P)
+        float w[8];
+        ff_weights(f3(pi[h]), c, hb, w);
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            const float4 p0 = s_phi[3 * m], p1 = s_phi[3 * m + 1], p2 = s_phi[3 * m + 2];
+            // A + beta C_x B_x + beta C_y B_y + beta C_z B_z
+            const float ux = p0.x + cb[h].x * p0.w + cb[h].y * p1.z + cb[h].z * p2.y;
+            const float uy = p0.y + cb[h].x * p1.x + cb[h].y * p1.w + cb[h].z * p2.z;
+            const float uz = p0.z + cb[h].x * p1.y + cb[h].y * p2.x + cb[h].z * p2.w;
+            sx = fmaf(w[m], ux, sx);
+            sy = fmaf(w[m], uy, sy);
+            sz = fmaf(w[m], uz, sz);
+        }
+        tea_bead_update<FEFF>(P, B, gi[h], sx, sy, sz, b2, K, feff);
+    }
+}
+
+// Beads in no leaf (extra beads): the update draws their angular noise and
+// keeps their frame, as the all-pairs update does.
+template <bool FEFF>
+__global__ void k_ff_rest(KParams P, DevBuffers B, FFBuffers F, float4 *feff, const int *gate) {
+    if (gate && *gate != 0) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= F.nrest) return;
+    const int g = F.rest[k];
+    const float beta = B.tea_beta[B.traj[g]];
+    tea_bead_update<FEFF>(P, B, g, 0.f, 0.f, 0.f, beta * beta, tea_const(P.tea_a), feff);
+}
+
+void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s) {
+    if (F.nleaf == 0) return;
+    k_ff_p2m<<<F.nleaf, kFFLeaf, 0, s>>>(P, B, F, gate);
+    k_ff_m2l<<<F.nleaf, 128, 0, s>>>(P, F, gate);
+}
+
+template <int SL, bool FEFF>
+static void ff_step_launch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff, const int *gate,
+                           cudaStream_t s) {
+    if (F.nleaf > 0) k_ff_step<SL, FEFF><<<F.nleaf, kTeaLanes * SL, 0, s>>>(P, B, F, feff, gate);
+    if (F.nrest > 0) k_ff_rest<FEFF><<<(F.nrest + 127) / 128, 128, 0, s>>>(P, B, F, feff, gate);
+}
+template <bool FEFF>
+static void ff_step_dispatch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff,
+                             const int *gate, cudaStream_t s) {
+    switch (P.tea_slices) {
+        case 1:
+        case 2: ff_step_launch<2, FEFF>(P, B, F, feff, gate, s); break;
+        case 4: ff_step_launch<4, FEFF>(P, B, F, feff, gate, s); break;
+        default: ff_step_launch<8, FEFF>(P, B, F, feff, gate, s); break;
+    }
+}
+void launch_ff_step(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,
+                    const int *gate, cudaStream_t s) {
+    if (feff_only)
+        ff_step_dispatch<true>(P, B, F, feff, gate, s);
+    else
+        ff_step_dispatch<false>(P, B, F, feff, gate, s);
 }
 
 }  // namespace mtg

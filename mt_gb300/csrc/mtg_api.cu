@@ -284,6 +284,9 @@ void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
     }
     if (p.hdi_on) {
         timed_launch(e, 2, [&] { launch_forces(e->kp, e->bufs(), true, e->stream); });
+        // learned TEA with the far field: proxies of this step's F and R
+        const bool ff = e->surr && e->ff_on;
+        if (ff) timed_launch(e, 8, [&] { launch_ff_proxies(e->kp, e->bufs(), e->ffb, e->surr_gate, e->stream); });
         if (e->surr) {
             // learned TEA: the network replaces the epsilon pass; the exact
             // re-check decides whether it stays in charge
@@ -294,7 +297,18 @@ void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
             timed_launch(e, 3, [&] { launch_tea_eps(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
             timed_launch(e, 4, [&] { launch_tea_beta(e->kp, e->bufs(), p.tea_capricious, p.tea_epsmax, e->stream); });
         }
-        timed_launch(e, 5, [&] { launch_tea_step(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
+        if (ff) {
+            // the far-field product while the surrogate is in charge, the exact
+            // one after a fall-back (each gated on the fall-back flag)
+            timed_launch(e, 9, [&] {
+                launch_ff_step(e->kp, e->bufs(), e->ffb, false, nullptr, e->surr_gate, e->stream);
+            });
+            timed_launch(e, 5, [&] {
+                launch_tea_step_gated(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->surr_gate, e->stream);
+            });
+        } else {
+            timed_launch(e, 5, [&] { launch_tea_step(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
+        }
     } else {
         timed_launch(e, 1, [&] { launch_step_plain(e->kp, e->bufs(), e->keep_forces, e->stream); });
     }
@@ -634,6 +648,7 @@ int mtg_destroy(mtg_engine *e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     mtg_internal_close_output(e);
     destroy_graphs(e);
+    mtg_internal_ff_free(e);
     void *ptrs[] = {e->off, e->traj, e->flags, e->harm, e->zs, e->frame[0], e->frame[1], e->force, e->seeds,
                     e->ljc, e->lj, e->lonc, e->lon, e->latc, e->lat, e->err, e->work, e->work_first,
                     e->en_partials, e->en_traj, e->en_bead, e->tea_r, e->tea_ci, e->tea_eps, e->tea_beta,
@@ -821,7 +836,9 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
         destroy_graphs(e);
         e->graph_period = (int)period;
     }
-    const int max_launch_per_step = 6;
+    const int max_launch_per_step = 8;
+    int rc = mtg_internal_ff_refresh(e);   // a due far-field partition is rebuilt before any capture
+    if (rc) return rc;
     e->direct_next = e->direct_base;
     e->used_slots.clear();
     long long s = first_step;
@@ -882,6 +899,7 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
         }
     }
     CK(cudaGetLastError());
+    e->ff_steps += nsteps;
     return MTG_OK;
 }
 

@@ -84,6 +84,19 @@ struct mtg_engine {
     int hydro_ncand = -1;
     // stride-step outputs (output.cu)
     struct mtg_output *output = nullptr;
+    // far field of learned TEA (tea_ff.cu): partition, lists, proxy data
+    bool ff_on = false;
+    float ff_theta = 0.85f;
+    int ff_refresh = 0;
+    long long ff_steps = 0;          // steps since the partition was built
+    int *ff_ints = nullptr;          // every int array of the partition, one allocation
+    size_t ff_ints_cap = 0;
+    float4 *ff_f4 = nullptr;         // boxes, proxy charges, proxy potentials
+    size_t ff_f4_cap = 0;
+    mtg::FFBuffers ffb{};
+    long long ff_near_pairs = 0, ff_proxy_pairs = 0;
+    std::vector<int> ff_host;        // the partition as built (for mtg_tea_farfield_layout)
+    int ff_sizes[4] = {0, 0, 0, 0};  // leaves, leaf beads, near entries, far entries
     // device address of the fixed scratch of mtg_energies_noalloc, looked up
     // by this engine's first call (energy_noalloc.cu)
     double *noalloc_scratch = nullptr;
@@ -143,3 +156,6 @@ void enqueue_surrogate_eps(mtg_engine *e);
 void enqueue_surrogate_recheck(mtg_engine *e);
 // drops the captured step graphs (after a mode change)
 void mtg_internal_reset_graphs(mtg_engine *e);
+// far field of learned TEA (tea_ff.cu): rebuilds the partition when due
+int mtg_internal_ff_refresh(mtg_engine *e);
+void mtg_internal_ff_free(mtg_engine *e);

@@ -278,4 +278,36 @@ void launch_set_flags(int nb, const uint8_t *extra, const int *gtp, const int *o
 
 constexpr int kTile = 128;   // beads per CTA tile of the O(N^2) kernels
 
+// ---------------------------------------------- far field of learned TEA
+// Leaves of at most kFFLeaf beads (a k-d partition of each trajectory,
+// tea_ff.cu), their near / far source leaves, and the per-step proxy data:
+// the 8 points c + h (+-kFFNode, +-kFFNode, +-kFFNode) of a leaf's bounding
+// box (centre c, half extent h; tensor-product Chebyshev nodes of degree 2)
+// carry the leaf's sources (F, R) as interpolation charges and receive the
+// far field of the leaves far from it, interpolated back to its beads.
+constexpr int kFFLeaf = 64;
+constexpr float kFFNode = 0.70710678f;
+struct FFBuffers {
+    int nleaf, nrest;
+    const int *leaf_start;   // [nleaf+1] into leaf_bead
+    const int *leaf_bead;    // beads of every leaf, leaf after leaf
+    const int *leaf_traj;    // [nleaf]
+    const int *near_start;   // [nleaf+1] into near: source leaves summed pair by pair
+    const int *near;
+    const int *far_start;    // [nleaf+1] into far: source leaves taken through their proxies
+    const int *far;
+    const int *rest;         // [nrest] beads in no leaf (extra beads)
+    float4 *box;             // [2*nleaf] centre, half extent (w unused)
+    float4 *q;               // [16*nleaf] proxy m: (QF.xyz, QR.x) at 16L+m, (QR.y, QR.z, 0, 0) at 16L+8+m
+    float4 *phi;             // [24*nleaf] target proxy n: (A.xyz, B0.x), (B0.yz, B1.xy), (B1.z, B2.xyz) at 24L+3n
+};
+// proxies (P2M) and far-field potentials at target proxies (M2L), while *gate == 0
+void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s);
+// near pairs + interpolated far field + update (FEFF: effective forces into feff, no update), while *gate == 0
+void launch_ff_step(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,
+                    const int *gate, cudaStream_t s);
+// the exact mobility product + update, only while *gate == 1 (after a fall-back to exact TEA)
+void launch_tea_step_gated(const KParams &P, const DevBuffers &B, const int2 *work, int nwork, const int *gate,
+                           cudaStream_t s);
+
 }  // namespace mtg

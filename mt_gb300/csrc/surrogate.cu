@@ -702,7 +702,10 @@ void enqueue_surrogate_recheck(mtg_engine *e) {
     launch_tea_eps_gated(e->kp, Be, e->tea_work, e->tea_nwork, gate, 0, e->stream);
     launch_tea_beta_gated(e->kp, Be, e->p.tea_capricious, e->p.tea_epsmax, gate, 0, e->stream);
     launch_tea_feff(e->kp, Be, e->tea_work, e->tea_nwork, e->feff_a, gate, e->stream);
-    launch_tea_feff(e->kp, Bs, e->tea_work, e->tea_nwork, e->feff_b, gate, e->stream);
+    if (e->ff_on)   // the learned mode's product is the far-field one
+        launch_ff_step(e->kp, Bs, e->ffb, true, e->feff_b, gate, e->stream);
+    else
+        launch_tea_feff(e->kp, Bs, e->tea_work, e->tea_nwork, e->feff_b, gate, e->stream);
     k_mob_partial<<<kMobBlocks, 256, 0, e->stream>>>(e->nb, e->flags, e->feff_b, e->feff_a, e->surr_part, gate);
     k_mob_final<<<1, 1, 0, e->stream>>>(e->surr_part, kMobBlocks, e->surr_max_err, e->surr_err, e->surr_gate,
                                         e->surr_gate + 1);

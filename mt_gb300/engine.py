@@ -83,13 +83,20 @@ EXPORTS = {
     "mtg_tea_training_data": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "mtg_set_surrogate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_float]),
     "mtg_surrogate_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "mtg_set_tea_farfield": (C.c_int, [C.c_void_p, C.c_int, C.c_float, C.c_int]),
+    "mtg_tea_farfield_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_longlong)]),
+    "mtg_tea_farfield_layout": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 7),
+    "mtg_tea_effective_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                           C.POINTER(C.c_float)]),
 }
 
 SURROGATE_FEATURES = 32
 SURROGATE_OUTPUTS = 4
 SURROGATE_PARAMS = 37764
 
-KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step", "surrogate", "recheck")
+KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step", "surrogate", "recheck",
+                "ff_proxies", "ff_step")
 
 _lib = None
 
@@ -443,6 +450,33 @@ class Engine:
         fb, nr, err = C.c_int(), C.c_int(), C.c_double()
         check(self.lib.mtg_surrogate_status(self.h, C.byref(fb), C.byref(nr), C.byref(err)))
         return {"fell_back": bool(fb.value), "rechecks": nr.value, "last_error": err.value}
+
+    def set_tea_farfield(self, on: bool = True, theta: float = 0.85, refresh_every: int = 0):
+        check(self.lib.mtg_set_tea_farfield(self.h, int(on), theta, refresh_every))
+
+    def tea_farfield_stats(self):
+        nl, npairs, ppairs = C.c_int(), C.c_longlong(), C.c_longlong()
+        check(self.lib.mtg_tea_farfield_stats(self.h, C.byref(nl), C.byref(npairs), C.byref(ppairs)))
+        return {"leaves": nl.value, "near_pairs": npairs.value, "proxy_pairs": ppairs.value}
+
+    def tea_farfield_layout(self):
+        """(leaf_start, leaf_bead, near_start, near, far_start, far) of the grouping."""
+        sz = np.zeros(4, np.int32)
+        nul = C.cast(None, C.POINTER(C.c_int))
+        check(self.lib.mtg_tea_farfield_layout(self.h, ptr(sz, C.c_int), nul, nul, nul, nul, nul, nul))
+        nl = int(sz[0])
+        a = [np.zeros(nl + 1, np.int32), np.zeros(int(sz[1]), np.int32), np.zeros(nl + 1, np.int32),
+             np.zeros(max(int(sz[2]), 1), np.int32), np.zeros(nl + 1, np.int32), np.zeros(max(int(sz[3]), 1), np.int32)]
+        check(self.lib.mtg_tea_farfield_layout(self.h, ptr(sz, C.c_int), *[ptr(x, C.c_int) for x in a]))
+        return a[0], a[1], a[2], a[3][:int(sz[2])], a[4], a[5][:int(sz[3])]
+
+    def tea_effective_forces(self, exact: bool = True, farfield: bool = True):
+        """(feff_exact, feff_ff, rforce) [nb, 4] of the current state from one draw of random forces."""
+        fe = np.zeros((self.nb, 4), np.float32) if exact else None
+        ff = np.zeros((self.nb, 4), np.float32) if farfield else None
+        rf = np.zeros((self.nb, 4), np.float32)
+        check(self.lib.mtg_tea_effective_forces(self.h, ptr(fe, C.c_float), ptr(ff, C.c_float), ptr(rf, C.c_float)))
+        return fe, ff, rf
 
     def energies(self, per_bead: bool = False):
         pt = np.zeros((self.nt, 7), np.float64)
