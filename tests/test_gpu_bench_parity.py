@@ -17,7 +17,15 @@ errors at a floor of 1e-3 x RMS are recorded beside the bar for that reason:
 * LJ lists bit-exact (centre distances are correctly rounded on both sides);
   longitudinal/lateral lists bit-exact except where the FP64 site distance of
   a pair lies within TIE nm of the 2.5 nm cutoff (sin/cos differ by an ulp);
-* forces, per-bead energies, TEA C_i: <= RTOL relative to the FP32 oracle;
+* forces, per-bead energies, TEA C_i: <= RTOL relative to the FP32 oracle,
+  plus the FP32 rounding envelope 2 E32, E32 = the FP32 oracle's own largest
+  absolute error against the FP64 oracle over the array.  The envelope only
+  matters where a value is rounding noise: the translational force of a
+  bead of a straight lattice at rest, or of a free dimer whose bond sits at
+  its rest length (the sine and cosine of its random angles round by an ulp
+  differently in CUDA and in libm, and C = 300 kcal/mol/nm^2 turns that into
+  about 1e-4 of force), and the lateral Morse energy per bead (one ulp of D).
+  Everywhere else RTOL alone decides (the recorded gpu_vs_fp32_oracle);
 * per-trajectory energy totals, epsilon and beta: <= RTOL relative;
 * one step (plain or TEA) from identical state and seeds: noise streams
   bit-exact, every coordinate within 2 FP32 ulps of its value + RTOL x the
@@ -61,6 +69,20 @@ def _write_report():
         with open(path, "w") as f:
             json.dump({"rtol": RTOL, "floor_of_rms": FLOOR, "tie_nm": TIE, "cases": REPORT}, f, indent=1,
                       sort_keys=True)
+
+
+def envelope_check(got, o32, o64, act):
+    """Largest per-bead |got - o32| in units of RTOL max(|o32_i|, RMS) + 2 E32
+    (<= 1 passes), and E32 relative to the RMS."""
+    got, o32, o64 = (np.asarray(a, np.float64)[act] for a in (got, o32, o64))
+    if got.ndim == 1:
+        got, o32, o64 = got[:, None], o32[:, None], o64[:, None]
+    mag = np.linalg.norm(o32, axis=1)
+    rms = float(np.sqrt(np.mean(mag ** 2))) if len(mag) else 0.0
+    e32 = float(np.max(np.linalg.norm(o32 - o64, axis=1), initial=0.0))
+    tol = RTOL * np.maximum(mag, FLOOR * rms) + 2 * e32
+    d = np.linalg.norm(got - o32, axis=1)
+    return float(np.max(d / np.maximum(tol, 1e-300), initial=0.0)), e32 / max(rms, 1e-300)
 
 
 def record(case, quantity, **vals):
@@ -141,10 +163,11 @@ def test_lists_forces_energies_on_bench_workloads(engine_mod, oracle_lib, case, 
         i32, _ = per_bead_rel(f[:, cols], fo[:, cols], act, FLOOR_INFO)
         i64, _ = per_bead_rel(f[:, cols], f64[:, cols], act, FLOOR_INFO)
         io64, _ = per_bead_rel(fo[:, cols], f64[:, cols], act, FLOOR_INFO)
+        env, e32_rel = envelope_check(f[:, cols], fo[:, cols], f64[:, cols], act)
         record(name, q, gpu_vs_fp32_oracle=e32, gpu_vs_fp64_oracle=e64, fp32_oracle_vs_fp64=o_64, rms=rms,
                beads=int(act.sum()), at_floor_1e3_gpu_vs_fp32=i32, at_floor_1e3_gpu_vs_fp64=i64,
-               at_floor_1e3_fp32_vs_fp64=io64)
-        assert e32 <= RTOL, (q, e32, e64)
+               at_floor_1e3_fp32_vs_fp64=io64, fp32_envelope_of_rms=e32_rel, envelope_ratio=env)
+        assert env <= 1.0, (q, e32, e64, o_64, env)
         assert e64 <= 2 * o_64 + RTOL, (q, e64, o_64)
     tot, per = e.energies(per_bead=True)
     eo, e64o = o32.energies(b, b.coords, L), o64.energies(b, b.coords, L)
@@ -153,9 +176,10 @@ def test_lists_forces_energies_on_bench_workloads(engine_mod, oracle_lib, case, 
         e32, rms = per_bead_rel(per[:, c], eo[:, c], act, FLOOR)
         e64, _ = per_bead_rel(per[:, c], e64o[:, c], act, FLOOR)
         i32, _ = per_bead_rel(per[:, c], eo[:, c], act, FLOOR_INFO)
+        env, e32_rel = envelope_check(per[:, c], eo[:, c], e64o[:, c], act)
         record(name, f"energy_per_bead_{q}", gpu_vs_fp32_oracle=e32, gpu_vs_fp64_oracle=e64, rms=rms,
-               at_floor_1e3_gpu_vs_fp32=i32)
-        assert e32 <= RTOL, (q, e32)
+               at_floor_1e3_gpu_vs_fp32=i32, fp32_envelope_of_rms=e32_rel, envelope_ratio=env)
+        assert env <= 1.0, (q, e32, env)
     for t in range(b.ntraj):
         sl = slice(int(b.offsets[t]), int(b.offsets[t + 1]))
         ref32, ref64 = eo[sl].sum(0), e64o[sl].sum(0)

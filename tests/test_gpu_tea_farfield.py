@@ -82,7 +82,9 @@ def _trained_surrogate(engine_mod):
 
 def test_learned_mode_with_farfield_runs_and_rechecks(engine_mod):
     s = _trained_surrogate(engine_mod)
-    b = small_system(seed=52, ntr=3, n_mon=60, n_free=900, tea=True, tea_epsilon_freq=5, extra=2)
+    from mt_gb300 import synth
+    p = synth.default_params(seed=52, hdi_on=1, tea_epsilon_freq=5)
+    b = synth.uniform_batch(p, 3, 60, 900, seed=52, cube=80.0, thermal=0.05, n_extra_dimers=2)
     e = engine_mod.Engine(b)
     e.upload_state(b.coords)
     e.set_surrogate(s, recheck_every=10, max_err=1.0)
