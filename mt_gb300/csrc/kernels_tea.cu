@@ -867,64 +867,83 @@ __global__ void __launch_bounds__(kFFLeaf) k_ff_p2m(KParams P, DevBuffers B, FFB
     }
 }
 
-// M2L: one CTA of 128 threads per target leaf; thread t serves target proxy
-// t % 8 over every 16th far leaf, the 16 slices meet in shared memory.
+// M2L: one CTA of 128 threads per target leaf; thread t serves the target
+// proxies t % 4 and t % 4 + 4 (the same x and y, opposite z) as one packed
+// pair over every 32nd far leaf, and the 32 slices meet in shared memory.
 __global__ void __launch_bounds__(128) k_ff_m2l(KParams P, FFBuffers F, const int *gate) {
     if (gate && *gate != 0) return;
-    const int L = blockIdx.x, t = threadIdx.x, n = t & 7, sl = t >> 3;
+    const int L = blockIdx.x, t = threadIdx.x, np = t & 3, sl = t >> 2;
     const TeaConst K = tea_const(P.tea_a);
-    const float3 xn = ff_proxy(F.box[2 * L], F.box[2 * L + 1], n);
-    float acc[12];
+    const float4 cL = F.box[2 * L], hL = F.box[2 * L + 1];
+    const float3 x0 = ff_proxy(cL, hL, np), x1 = ff_proxy(cL, hL, np + 4);
+    const float2 nxx = f2(-x0.x), nxy = f2(-x0.y), nxz = make_float2(-x0.z, -x1.z);
+    const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
+    float2 acc[12];
 #pragma unroll
-    for (int c = 0; c < 12; c++) acc[c] = 0.f;
-    for (int k = F.far_start[L] + sl; k < F.far_start[L + 1]; k += 16) {
+    for (int c = 0; c < 12; c++) acc[c] = f2(0.f);
+    for (int k = F.far_start[L] + sl; k < F.far_start[L + 1]; k += 32) {
         const int J = F.far[k];
         const float4 cJ = F.box[2 * J], hJ = F.box[2 * J + 1];
 #pragma unroll 2
         for (int m = 0; m < 8; m++) {
             const float3 y = ff_proxy(cJ, hJ, m);
-            const float dx = y.x - xn.x, dy = y.y - xn.y, dz = y.z - xn.z;
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float rinv = rsqrt_hw(r2), q2 = rinv * rinv, tq = q2 * rinv;
-            const float cii = fmaf(K.kap, tq, rinv);
-            const float cr = tq * fmaf(-K.two_a2, q2, 1.0f);
+            const float2 dx = __fadd2_rn(f2(y.x), nxx), dy = __fadd2_rn(f2(y.y), nxy), dz = __fadd2_rn(f2(y.z), nxz);
+            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+            const float2 q2 = __fmul2_rn(rinv, rinv), tq = __fmul2_rn(q2, rinv);
+            const float2 cii = __ffma2_rn(vkap, tq, rinv);
+            const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q2, one));
             const float4 qa = F.q[16 * J + m], qb = F.q[16 * J + 8 + m];
-            const float sF = cr * fmaf(dx, qa.x, fmaf(dy, qa.y, dz * qa.z));
-            acc[0] = fmaf(cii, qa.x, fmaf(sF, dx, acc[0]));
-            acc[1] = fmaf(cii, qa.y, fmaf(sF, dy, acc[1]));
-            acc[2] = fmaf(cii, qa.z, fmaf(sF, dz, acc[2]));
-            const float s0 = cr * dx * qa.w, s1 = cr * dy * qb.x, s2 = cr * dz * qb.y;
-            acc[3] = fmaf(cii, qa.w, fmaf(s0, dx, acc[3]));
-            acc[4] = fmaf(s0, dy, acc[4]);
-            acc[5] = fmaf(s0, dz, acc[5]);
-            acc[6] = fmaf(s1, dx, acc[6]);
-            acc[7] = fmaf(cii, qb.x, fmaf(s1, dy, acc[7]));
-            acc[8] = fmaf(s1, dz, acc[8]);
-            acc[9] = fmaf(s2, dx, acc[9]);
-            acc[10] = fmaf(s2, dy, acc[10]);
-            acc[11] = fmaf(cii, qb.y, fmaf(s2, dz, acc[11]));
+            const float2 qfx = f2(qa.x), qfy = f2(qa.y), qfz = f2(qa.z);
+            const float2 sF = __fmul2_rn(cr, __ffma2_rn(dx, qfx, __ffma2_rn(dy, qfy, __fmul2_rn(dz, qfz))));
+            acc[0] = __ffma2_rn(cii, qfx, __ffma2_rn(sF, dx, acc[0]));
+            acc[1] = __ffma2_rn(cii, qfy, __ffma2_rn(sF, dy, acc[1]));
+            acc[2] = __ffma2_rn(cii, qfz, __ffma2_rn(sF, dz, acc[2]));
+            const float2 rx = f2(qa.w), ry = f2(qb.x), rz = f2(qb.y);
+            const float2 s0 = __fmul2_rn(__fmul2_rn(cr, dx), rx), s1 = __fmul2_rn(__fmul2_rn(cr, dy), ry),
+                         s2 = __fmul2_rn(__fmul2_rn(cr, dz), rz);
+            acc[3] = __ffma2_rn(cii, rx, __ffma2_rn(s0, dx, acc[3]));
+            acc[4] = __ffma2_rn(s0, dy, acc[4]);
+            acc[5] = __ffma2_rn(s0, dz, acc[5]);
+            acc[6] = __ffma2_rn(s1, dx, acc[6]);
+            acc[7] = __ffma2_rn(cii, ry, __ffma2_rn(s1, dy, acc[7]));
+            acc[8] = __ffma2_rn(s1, dz, acc[8]);
+            acc[9] = __ffma2_rn(s2, dx, acc[9]);
+            acc[10] = __ffma2_rn(s2, dy, acc[10]);
+            acc[11] = __ffma2_rn(cii, rz, __ffma2_rn(s2, dz, acc[11]));
         }
     }
-    __shared__ float red[128][13];
+    // red[slice][proxy][component]
+    __shared__ float red[32][8][13];
 #pragma unroll
-    for (int c = 0; c < 12; c++) red[t][c] = acc[c];
+    for (int c = 0; c < 12; c++) {
+        red[sl][np][c] = acc[c].x;
+        red[sl][np + 4][c] = acc[c].y;
+    }
     __syncthreads();
     if (t < 96) {
         const int pn = t / 12, c = t % 12;
         float v = 0.f;
-#pragma unroll
-        for (int k = 0; k < 16; k++) v += red[k * 8 + pn][c];
+#pragma unroll 8
+        for (int k = 0; k < 32; k++) v += red[k][pn][c];
         reinterpret_cast<float *>(F.phi)[(size_t)96 * L + 12 * pn + c] = v;
     }
 }
 
-// The packed pass of one source leaf for one packed pair of target beads
-// (self pairs pushed to r^2 = 1e30 when SELF), running minimum of r^2.
+// Beads i per thread in the far-field step: two packed pairs, the lanes of a
+// slice spread over the leaf (lane il serves il, il + 16, il + 32, il + 48).
+constexpr int kFFPairs = 2;
+constexpr int kFFLanes = kFFLeaf / (2 * kFFPairs);
+
+// The packed pass of one source leaf (self pairs pushed to r^2 = 1e30 when
+// SELF), running minimum of r^2 per packed pair and segment.
 template <int SLICES, bool SELF>
-__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_t, float2 nx, float2 ny, float2 nz,
-                                             float2 cbx, float2 cby, float2 cbz, float2 vkap, float2 vn2a2,
-                                             float2 one, float2 &ax, float2 &ay, float2 &az,
-                                             float (&rmin)[kTeaSeg]) {
+__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_t, const float2 (&nx)[kFFPairs],
+                                             const float2 (&ny)[kFFPairs], const float2 (&nz)[kFFPairs],
+                                             const float2 (&cbx)[kFFPairs], const float2 (&cby)[kFFPairs],
+                                             const float2 (&cbz)[kFFPairs], float2 vkap, float2 vn2a2,
+                                             float2 one, float2 (&ax)[kFFPairs], float2 (&ay)[kFFPairs],
+                                             float2 (&az)[kFFPairs], float (&rmin)[kFFPairs][kTeaSeg]) {
     constexpr int kLen = kFFLeaf / SLICES / kTeaSeg;
 #pragma unroll
     for (int sg = 0; sg < kTeaSeg; sg++) {
@@ -932,146 +951,177 @@ __device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_t
         for (int k = 0; k < kLen; k++) {
             const int t = sl + (sg * kLen + k) * SLICES;
             const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
-            const float2 dx = __fadd2_rn(lo2(a), nx), dy = __fadd2_rn(hi2(a), ny), dz = __fadd2_rn(lo2(b), nz);
-            const float2 gx = __ffma2_rn(lo2(d), cbx, hi2(b)), gy = __ffma2_rn(hi2(d), cby, lo2(c)),
-                         gz = __ffma2_rn(T.rz[t], cbz, hi2(c));
-            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-            if (SELF) {
-                if (t == self_t) r2.x = 1e30f;
-                if (t == self_t + kTeaLanes) r2.y = 1e30f;
+            const float2 xj = lo2(a), yj = hi2(a), zj = lo2(b);
+            const float2 fxj = hi2(b), fyj = lo2(c), fzj = hi2(c);
+            const float2 rxj = lo2(d), ryj = hi2(d), rzj = T.rz[t];
+#pragma unroll
+            for (int p = 0; p < kFFPairs; p++) {
+                const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
+                const float2 gx = __ffma2_rn(rxj, cbx[p], fxj), gy = __ffma2_rn(ryj, cby[p], fyj),
+                             gz = __ffma2_rn(rzj, cbz[p], fzj);
+                float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                if (SELF) {
+                    if (t == self_t + kFFLanes * 2 * p) r2.x = 1e30f;
+                    if (t == self_t + kFFLanes * (2 * p + 1)) r2.y = 1e30f;
+                }
+                rmin[p][sg] = fmin3(rmin[p][sg], r2.x, r2.y);
+                const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+                const float2 q = __fmul2_rn(rinv, rinv);
+                const float2 tq = __fmul2_rn(q, rinv);
+                const float2 cii = __ffma2_rn(vkap, tq, rinv);
+                const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
+                const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
+                ax[p] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax[p]));
+                ay[p] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay[p]));
+                az[p] = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az[p]));
             }
-            rmin[sg] = fmin3(rmin[sg], r2.x, r2.y);
-            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-            const float2 q = __fmul2_rn(rinv, rinv);
-            const float2 tq = __fmul2_rn(q, rinv);
-            const float2 cii = __ffma2_rn(vkap, tq, rinv);
-            const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
-            const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
-            ax = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax));
-            ay = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay));
-            az = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az));
         }
     }
 }
 
-// Near pairs, far field and update: one CTA of 32 x SLICES threads per
-// target leaf; lane il serves the leaf's beads il and il + 32 as one packed
-// pair, the SLICES threads of a lane take interleaved beads of every source
-// leaf of the near list.  Overlapping pairs (r <= 2a) are corrected as in
-// k_tea_step.  Then the far field is interpolated from the leaf's proxies and
-// the bead moves (FEFF: its effective force goes to feff instead).
+// Near pairs, far field and update: one CTA of kFFLanes x SLICES threads per
+// target leaf; lane il serves the leaf's beads il + 16 h (h = 0..3) as two
+// packed pairs, the SLICES threads of a lane take interleaved beads of every
+// source leaf of the near list.  Overlapping pairs (r <= 2a) are corrected as
+// in k_tea_step.  Then the far field is interpolated from the leaf's proxies
+// and the bead moves (FEFF: its effective force goes to feff instead).
 template <int SLICES, bool FEFF>
-__global__ void __launch_bounds__(kTeaLanes *SLICES) k_ff_step(KParams P, DevBuffers B, FFBuffers F, float4 *feff,
-                                                               const int *gate) {
+__global__ void __launch_bounds__(kFFLanes *SLICES, 40 / SLICES) k_ff_step(KParams P, DevBuffers B, FFBuffers F, float4 *feff,
+                                                              const int *gate) {
     if (gate && *gate != 0) return;
+    constexpr int kNI = 2 * kFFPairs;
     const int L = blockIdx.x;
-    const int il = threadIdx.x % kTeaLanes, sl = threadIdx.x / kTeaLanes;
+    const int il = threadIdx.x % kFFLanes, sl = threadIdx.x / kFFLanes;
     const int s0 = F.leaf_start[L], n = F.leaf_start[L + 1] - s0;
     const int traj = F.leaf_traj[L];
     __shared__ FFTile T;
-    __shared__ float4 s_red[2 * kTeaLanes * SLICES];
+    __shared__ float4 s_red[kNI * kFFLanes * SLICES];
     __shared__ float4 s_phi[24];
     const float beta = B.tea_beta[traj], b2 = beta * beta;
-    int gi[2];
-    float4 pi[2], cb[2];
+    // per packed pair p of beads i (2p, 2p+1): -position, beta C_i, sums
+    float2 nx[kFFPairs], ny[kFFPairs], nz[kFFPairs], cbx[kFFPairs], cby[kFFPairs], cbz[kFFPairs];
+    float2 ax[kFFPairs], ay[kFFPairs], az[kFFPairs];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int k = il + h * kTeaLanes;
-        gi[h] = k < n ? F.leaf_bead[s0 + k] : -1;
-        pi[h] = make_float4(0.f, 0.f, 0.f, 0.f);
-        cb[h] = pi[h];
-        if (gi[h] >= 0) {
-            pi[h] = B.frame_in[gi[h]];
-            const float4 ci = B.tea_ci[gi[h]];
-            cb[h] = make_float4(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
-                                beta / sqrtf(1.0f + b2 * ci.z), 0.f);
+    for (int h = 0; h < kNI; h++) {
+        const int k = il + h * kFFLanes;
+        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), cb = pi;
+        if (k < n) {
+            const int g = F.leaf_bead[s0 + k];
+            pi = B.frame_in[g];
+            const float4 ci = B.tea_ci[g];
+            cb = make_float4(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
+                             beta / sqrtf(1.0f + b2 * ci.z), 0.f);
+        }
+        float2 *v[6] = {&nx[h >> 1], &ny[h >> 1], &nz[h >> 1], &cbx[h >> 1], &cby[h >> 1], &cbz[h >> 1]};
+        const float val[6] = {-pi.x, -pi.y, -pi.z, cb.x, cb.y, cb.z};
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            if (h & 1)
+                v[c]->y = val[c];
+            else
+                v[c]->x = val[c];
         }
     }
-    const float2 nx = make_float2(-pi[0].x, -pi[1].x), ny = make_float2(-pi[0].y, -pi[1].y),
-                 nz = make_float2(-pi[0].z, -pi[1].z);
-    const float2 cbx = make_float2(cb[0].x, cb[1].x), cby = make_float2(cb[0].y, cb[1].y),
-                 cbz = make_float2(cb[0].z, cb[1].z);
-    float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f);
+#pragma unroll
+    for (int p = 0; p < kFFPairs; p++) ax[p] = ay[p] = az[p] = f2(0.f);
     const TeaConst K = tea_const(P.tea_a);
     const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
     for (int e = F.near_start[L]; e < F.near_start[L + 1]; e++) {
         const int J = F.near[e];
         ff_tile_load(T, B, F, J);
         __syncthreads();
-        float rmin[kTeaSeg];
+        float rmin[kFFPairs][kTeaSeg];
 #pragma unroll
-        for (int sg = 0; sg < kTeaSeg; sg++) rmin[sg] = 3.4e38f;
+        for (int p = 0; p < kFFPairs; p++)
+#pragma unroll
+            for (int sg = 0; sg < kTeaSeg; sg++) rmin[p][sg] = 3.4e38f;
         const bool self = J == L;
         if (self)
             ff_step_tile<SLICES, true>(T, sl, il, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az, rmin);
         else
             ff_step_tile<SLICES, false>(T, sl, il, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az, rmin);
-        unsigned segs = 0;
-#pragma unroll
-        for (int sg = 0; sg < kTeaSeg; sg++) segs |= (rmin[sg] <= K.four_a2 ? 1u : 0u) << sg;
         constexpr int kLen = kFFLeaf / SLICES / kTeaSeg;
-        while (segs) {  // the segments that hold an overlapping pair
-            const int sg = __ffs(segs) - 1;
-            segs &= segs - 1;
-            for (int k = 0; k < kLen; k++) {
-                const int t = sl + (sg * kLen + k) * SLICES;
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    if (self && t == il + h * kTeaLanes) continue;
-                    const float dx = T.xy[t].x + (h ? nx.y : nx.x), dy = T.xy[t].z + (h ? ny.y : ny.x),
-                                dz = T.zf[t].x + (h ? nz.y : nz.x);
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    if (!(r2 <= K.four_a2)) continue;
-                    const float gx = fmaf(T.rxy[t].x, h ? cbx.y : cbx.x, T.zf[t].z),
-                                gy = fmaf(T.rxy[t].z, h ? cby.y : cby.x, T.fyz[t].x),
-                                gz = fmaf(T.rz[t].x, h ? cbz.y : cbz.x, T.fyz[t].z);
-                    const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
-                    const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
-                    if (h) {
-                        ax.y += nr.x - fa.x;
-                        ay.y += nr.y - fa.y;
-                        az.y += nr.z - fa.z;
-                    } else {
-                        ax.x += nr.x - fa.x;
-                        ay.x += nr.y - fa.y;
-                        az.x += nr.z - fa.z;
+        for (int p = 0; p < kFFPairs; p++) {
+            unsigned segs = 0;
+#pragma unroll
+            for (int sg = 0; sg < kTeaSeg; sg++) segs |= (rmin[p][sg] <= K.four_a2 ? 1u : 0u) << sg;
+            while (segs) {  // the segments that hold an overlapping pair
+                const int sg = __ffs(segs) - 1;
+                segs &= segs - 1;
+                for (int k = 0; k < kLen; k++) {
+                    const int t = sl + (sg * kLen + k) * SLICES;
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        if (self && t == il + kFFLanes * (2 * p + h)) continue;
+                        const float dx = T.xy[t].x + (h ? nx[p].y : nx[p].x), dy = T.xy[t].z + (h ? ny[p].y : ny[p].x),
+                                    dz = T.zf[t].x + (h ? nz[p].y : nz[p].x);
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        if (!(r2 <= K.four_a2)) continue;
+                        const float gx = fmaf(T.rxy[t].x, h ? cbx[p].y : cbx[p].x, T.zf[t].z),
+                                    gy = fmaf(T.rxy[t].z, h ? cby[p].y : cby[p].x, T.fyz[t].x),
+                                    gz = fmaf(T.rz[t].x, h ? cbz[p].y : cbz[p].x, T.fyz[t].z);
+                        const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+                        const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
+                        if (h) {
+                            ax[p].y += nr.x - fa.x;
+                            ay[p].y += nr.y - fa.y;
+                            az[p].y += nr.z - fa.z;
+                        } else {
+                            ax[p].x += nr.x - fa.x;
+                            ay[p].x += nr.y - fa.y;
+                            az[p].x += nr.z - fa.z;
+                        }
                     }
                 }
             }
         }
         __syncthreads();
     }
-    s_red[(sl * 2 + 0) * kTeaLanes + il] = make_float4(ax.x, ay.x, az.x, 0.f);
-    s_red[(sl * 2 + 1) * kTeaLanes + il] = make_float4(ax.y, ay.y, az.y, 0.f);
+#pragma unroll
+    for (int h = 0; h < kNI; h++) {
+        const int p = h >> 1;
+        const bool hi = h & 1;
+        s_red[(sl * kNI + h) * kFFLanes + il] =
+            make_float4(hi ? ax[p].y : ax[p].x, hi ? ay[p].y : ay[p].x, hi ? az[p].y : az[p].x, 0.f);
+    }
     if (threadIdx.x < 24) s_phi[threadIdx.x] = F.phi[24 * L + threadIdx.x];
     __syncthreads();
     if (sl != 0) return;
     const float4 c = F.box[2 * L], hb = F.box[2 * L + 1];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        if (gi[h] < 0) continue;
+    for (int h = 0; h < kNI; h++) {
+        const int k = il + h * kFFLanes;
+        if (k >= n) continue;
+        const int g = F.leaf_bead[s0 + k];
+        const int p = h >> 1;
+        const bool hi = h & 1;
+        const float3 xi = make_float3(-(hi ? nx[p].y : nx[p].x), -(hi ? ny[p].y : ny[p].x),
+                                      -(hi ? nz[p].y : nz[p].x));
+        const float3 cbi = make_float3(hi ? cbx[p].y : cbx[p].x, hi ? cby[p].y : cby[p].x,
+                                       hi ? cbz[p].y : cbz[p].x);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         for (int k = 0; k < SLICES; k++) {
-            const float4 v = s_red[(k * 2 + h) * kTeaLanes + il];
+            const float4 v = s_red[(k * kNI + h) * kFFLanes + il];
             sx += v.x;
             sy += v.y;
             sz += v.z;
         }
         // far field interpolated from the leaf's 8 proxies (L2P)
         float w[8];
-        ff_weights(f3(pi[h]), c, hb, w);
+        ff_weights(xi, c, hb, w);
 #pragma unroll
         for (int m = 0; m < 8; m++) {
             const float4 p0 = s_phi[3 * m], p1 = s_phi[3 * m + 1], p2 = s_phi[3 * m + 2];
             // A + beta C_x B_x + beta C_y B_y + beta C_z B_z
-            const float ux = p0.x + cb[h].x * p0.w + cb[h].y * p1.z + cb[h].z * p2.y;
-            const float uy = p0.y + cb[h].x * p1.x + cb[h].y * p1.w + cb[h].z * p2.z;
-            const float uz = p0.z + cb[h].x * p1.y + cb[h].y * p2.x + cb[h].z * p2.w;
+            const float ux = p0.x + cbi.x * p0.w + cbi.y * p1.z + cbi.z * p2.y;
+            const float uy = p0.y + cbi.x * p1.x + cbi.y * p1.w + cbi.z * p2.z;
+            const float uz = p0.z + cbi.x * p1.y + cbi.y * p2.x + cbi.z * p2.w;
             sx = fmaf(w[m], ux, sx);
             sy = fmaf(w[m], uy, sy);
             sz = fmaf(w[m], uz, sz);
         }
-        tea_bead_update<FEFF>(P, B, gi[h], sx, sy, sz, b2, K, feff);
+        tea_bead_update<FEFF>(P, B, g, sx, sy, sz, b2, K, feff);
     }
 }
 
@@ -1096,17 +1146,18 @@ void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F
 template <int SL, bool FEFF>
 static void ff_step_launch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff, const int *gate,
                            cudaStream_t s) {
-    if (F.nleaf > 0) k_ff_step<SL, FEFF><<<F.nleaf, kTeaLanes * SL, 0, s>>>(P, B, F, feff, gate);
+    if (F.nleaf > 0) k_ff_step<SL, FEFF><<<F.nleaf, kFFLanes * SL, 0, s>>>(P, B, F, feff, gate);
     if (F.nrest > 0) k_ff_rest<FEFF><<<(F.nrest + 127) / 128, 128, 0, s>>>(P, B, F, feff, gate);
 }
 template <bool FEFF>
 static void ff_step_dispatch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff,
                              const int *gate, cudaStream_t s) {
+    // threads per target bead: twice the exact kernel's (a leaf has half its beads i)
     switch (P.tea_slices) {
         case 1:
-        case 2: ff_step_launch<2, FEFF>(P, B, F, feff, gate, s); break;
-        case 4: ff_step_launch<4, FEFF>(P, B, F, feff, gate, s); break;
-        default: ff_step_launch<8, FEFF>(P, B, F, feff, gate, s); break;
+        case 2: ff_step_launch<4, FEFF>(P, B, F, feff, gate, s); break;
+        case 4: ff_step_launch<8, FEFF>(P, B, F, feff, gate, s); break;
+        default: ff_step_launch<16, FEFF>(P, B, F, feff, gate, s); break;
     }
 }
 void launch_ff_step(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,
