@@ -400,8 +400,9 @@ int mtg_tea_farfield_layout(mtg_engine *e, int *sizes, int *leaf_start, int *lea
  * C_i and beta, from one force evaluation and one draw of random forces:
  * feff_exact by the all-pairs product, feff_ff by the far-field one (needs
  * the far field on); rforce [nbeads*4] receives the random forces.  Any
- * pointer may be NULL.  The draw advances the noise streams g as a step's
- * does.  No reference counterpart (for checks of the approximation). */
+ * pointer may be NULL.  The pair lists are rebuilt from the current state
+ * first.  The draw advances the noise streams g as a step's does.  No
+ * reference counterpart (for checks of the approximation). */
 int mtg_tea_effective_forces(mtg_engine *e, float *feff_exact, float *feff_ff, float *rforce);
 
 /* ---- tuning ------------------------------------------------------------ */

@@ -757,30 +757,48 @@ void launch_tea_feff(const KParams &P, const DevBuffers &B, const int2 *work, in
 // (k = x, y, z); a bead adds A + sum_k beta C_ik B_k.  Far means the leaves'
 // centres are farther apart than (r_I + r_J + margin) / theta (tea_ff.cu).
 
-// Tile of one source leaf, in the layout of TeaTile.
+// Tile of kFFTileLeaves source leaves (kFFLeaf slots each), in the layout of
+// TeaTile; filled from FFBuffers::pack by asynchronous 16-byte copies.
+constexpr int kFFTileLeaves = 2;
+constexpr int kFFTile = kFFLeaf * kFFTileLeaves;
 struct FFTile {
-    float4 xy[kFFLeaf];
-    float4 zf[kFFLeaf];
-    float4 fyz[kFFLeaf];
-    float4 rxy[kFFLeaf];
-    float2 rz[kFFLeaf];
+    float4 xy[kFFTile];
+    float4 zf[kFFTile];
+    float4 fyz[kFFTile];
+    float4 rxy[kFFTile];
+    float2 rz[kFFTile];
 };
 
-__device__ __forceinline__ void ff_tile_load(FFTile &T, const DevBuffers &B, const FFBuffers &F, int leaf) {
-    const int s = F.leaf_start[leaf], n = F.leaf_start[leaf + 1] - s;
-    for (int k = threadIdx.x; k < kFFLeaf; k += blockDim.x) {
-        float4 p = make_float4(kFarAway, kFarAway, kFarAway, 0.f), Fv = make_float4(0.f, 0.f, 0.f, 0.f), R = Fv;
-        if (k < n) {
-            const int g = F.leaf_bead[s + k];
-            p = B.frame_in[g];
-            Fv = B.force[g];
-            R = B.tea_r[g];
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Near-list entries a step CTA keeps in shared memory (longer lists are read
+// from global memory).
+constexpr int kFFNearSmem = 256;
+
+// Issues the copies of near-list entries e0, e0 + 1 (or the padding leaf past
+// e1; entries relative to the list's start) into tile T: each leaf is
+// kFFPackF4 contiguous float4 of pack.
+__device__ __forceinline__ void ff_tile_issue(FFTile &T, const FFBuffers &F, const int *near, int e0, int e1) {
+    constexpr int kPer = kFFPackF4;
+    for (int c = threadIdx.x; c < kFFTileLeaves * kPer; c += blockDim.x) {
+        const int q = c / kPer, w = c % kPer;
+        const int e = e0 + q;
+        const int J = e < e1 ? near[e] : F.nleaf;
+        const float4 *src = F.pack + (size_t)J * kPer + w;
+        float4 *dst;
+        if (w < 4 * kFFLeaf) {
+            const int a = w / kFFLeaf, k = q * kFFLeaf + w % kFFLeaf;
+            dst = a == 0 ? &T.xy[k] : a == 1 ? &T.zf[k] : a == 2 ? &T.fyz[k] : &T.rxy[k];
+        } else {
+            dst = reinterpret_cast<float4 *>(&T.rz[q * kFFLeaf + 2 * (w - 4 * kFFLeaf)]);
         }
-        T.xy[k] = make_float4(p.x, p.x, p.y, p.y);
-        T.zf[k] = make_float4(p.z, p.z, Fv.x, Fv.x);
-        T.fyz[k] = make_float4(Fv.y, Fv.y, Fv.z, Fv.z);
-        T.rxy[k] = make_float4(R.x, R.x, R.y, R.y);
-        T.rz[k] = f2(R.z);
+        cp_async16(dst, src);
     }
 }
 
@@ -806,7 +824,7 @@ __device__ __forceinline__ float3 ff_proxy(float4 c, float4 h, int m) {
 __global__ void __launch_bounds__(kFFLeaf) k_ff_p2m(KParams P, DevBuffers B, FFBuffers F, const int *gate) {
     if (gate && *gate != 0) return;
     const int L = blockIdx.x, t = threadIdx.x;
-    const int s = F.leaf_start[L], n = F.leaf_start[L + 1] - s;
+    const int s = L < F.nleaf ? F.leaf_start[L] : 0, n = L < F.nleaf ? F.leaf_start[L + 1] - s : 0;
     __shared__ float sw[kFFLeaf][9];
     __shared__ float sv[kFFLeaf][7];
     __shared__ float3 slo[kFFLeaf / 32], shi[kFFLeaf / 32];
@@ -820,6 +838,16 @@ __global__ void __launch_bounds__(kFFLeaf) k_ff_p2m(KParams P, DevBuffers B, FFB
         R = B.tea_r[g];
         lo = hi = x;
     }
+    {   // the leaf's beads in the step kernel's tile layout (block nleaf: the padding leaf)
+        float4 *pk = F.pack + (size_t)L * kFFPackF4;
+        const float3 px = t < n ? x : make_float3(kFarAway, kFarAway, kFarAway);
+        pk[t] = make_float4(px.x, px.x, px.y, px.y);
+        pk[kFFLeaf + t] = make_float4(px.z, px.z, Fv.x, Fv.x);
+        pk[2 * kFFLeaf + t] = make_float4(Fv.y, Fv.y, Fv.z, Fv.z);
+        pk[3 * kFFLeaf + t] = make_float4(R.x, R.x, R.y, R.y);
+        reinterpret_cast<float2 *>(pk + 4 * kFFLeaf)[t] = f2(R.z);
+    }
+    if (L >= F.nleaf) return;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
@@ -930,24 +958,25 @@ __global__ void __launch_bounds__(128) k_ff_m2l(KParams P, FFBuffers F, const in
     }
 }
 
-// Beads i per thread in the far-field step: two packed pairs, the lanes of a
-// slice spread over the leaf (lane il serves il, il + 16, il + 32, il + 48).
-constexpr int kFFPairs = 2;
+// Beads i per thread in the far-field step: one packed pair, the 32 lanes of
+// a slice (one warp) spread over the leaf (lane il serves il and il + 32), so
+// that every tile load of a warp is one broadcast.
+constexpr int kFFPairs = 1;
 constexpr int kFFLanes = kFFLeaf / (2 * kFFPairs);
 
-// The packed pass of one source leaf (self pairs pushed to r^2 = 1e30 when
-// SELF), running minimum of r^2 per packed pair and segment.
-template <int SLICES, bool SELF>
+// The packed pass of one tile (self pairs pushed to r^2 = 1e30 when SELF),
+// with TRACK the running minimum of r^2 per packed pair and segment.
+template <int SLICES, bool SELF, bool TRACK>
 __device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_t, const float2 (&nx)[kFFPairs],
                                              const float2 (&ny)[kFFPairs], const float2 (&nz)[kFFPairs],
                                              const float2 (&cbx)[kFFPairs], const float2 (&cby)[kFFPairs],
                                              const float2 (&cbz)[kFFPairs], float2 vkap, float2 vn2a2,
                                              float2 one, float2 (&ax)[kFFPairs], float2 (&ay)[kFFPairs],
                                              float2 (&az)[kFFPairs], float (&rmin)[kFFPairs][kTeaSeg]) {
-    constexpr int kLen = kFFLeaf / SLICES / kTeaSeg;
+    constexpr int kLen = kFFTile / SLICES / kTeaSeg;
 #pragma unroll
     for (int sg = 0; sg < kTeaSeg; sg++) {
-#pragma unroll
+#pragma unroll(kLen <= 4 ? kLen : 2)
         for (int k = 0; k < kLen; k++) {
             const int t = sl + (sg * kLen + k) * SLICES;
             const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
@@ -964,7 +993,7 @@ __device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_t
                     if (t == self_t + kFFLanes * 2 * p) r2.x = 1e30f;
                     if (t == self_t + kFFLanes * (2 * p + 1)) r2.y = 1e30f;
                 }
-                rmin[p][sg] = fmin3(rmin[p][sg], r2.x, r2.y);
+                if (TRACK) rmin[p][sg] = fmin3(rmin[p][sg], r2.x, r2.y);
                 const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
                 const float2 q = __fmul2_rn(rinv, rinv);
                 const float2 tq = __fmul2_rn(q, rinv);
@@ -980,13 +1009,16 @@ __device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_t
 }
 
 // Near pairs, far field and update: one CTA of kFFLanes x SLICES threads per
-// target leaf; lane il serves the leaf's beads il + 16 h (h = 0..3) as two
-// packed pairs, the SLICES threads of a lane take interleaved beads of every
-// source leaf of the near list.  Overlapping pairs (r <= 2a) are corrected as
-// in k_tea_step.  Then the far field is interpolated from the leaf's proxies
-// and the bead moves (FEFF: its effective force goes to feff instead).
-template <int SLICES, bool FEFF>
-__global__ void __launch_bounds__(kFFLanes *SLICES, 40 / SLICES) k_ff_step(KParams P, DevBuffers B, FFBuffers F, float4 *feff,
+// target leaf; lane il serves the leaf's beads il + kFFLanes h as packed
+// pairs, the SLICES threads of a lane take interleaved beads of every tile of
+// near leaves (two leaves per tile, copied asynchronously one tile ahead).
+// Overlapping pairs (r <= 2a) get the near formula: with LISTCORR by walking
+// the bead's LJ list once, otherwise by rescanning the tile segments whose
+// running minimum of r^2 flags one, as in k_tea_step.  Then the far field is
+// interpolated from the leaf's proxies and the bead moves (FEFF: its
+// effective force goes to feff instead).
+template <int SLICES, bool FEFF, bool LISTCORR>
+__global__ void __launch_bounds__(kFFLanes *SLICES, 20 / SLICES) k_ff_step(KParams P, DevBuffers B, FFBuffers F, float4 *feff,
                                                               const int *gate) {
     if (gate && *gate != 0) return;
     constexpr int kNI = 2 * kFFPairs;
@@ -994,7 +1026,7 @@ __global__ void __launch_bounds__(kFFLanes *SLICES, 40 / SLICES) k_ff_step(KPara
     const int il = threadIdx.x % kFFLanes, sl = threadIdx.x / kFFLanes;
     const int s0 = F.leaf_start[L], n = F.leaf_start[L + 1] - s0;
     const int traj = F.leaf_traj[L];
-    __shared__ FFTile T;
+    __shared__ FFTile T2[2];
     __shared__ float4 s_red[kNI * kFFLanes * SLICES];
     __shared__ float4 s_phi[24];
     const float beta = B.tea_beta[traj], b2 = beta * beta;
@@ -1026,21 +1058,49 @@ __global__ void __launch_bounds__(kFFLanes *SLICES, 40 / SLICES) k_ff_step(KPara
     for (int p = 0; p < kFFPairs; p++) ax[p] = ay[p] = az[p] = f2(0.f);
     const TeaConst K = tea_const(P.tea_a);
     const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
-    for (int e = F.near_start[L]; e < F.near_start[L + 1]; e++) {
-        const int J = F.near[e];
-        ff_tile_load(T, B, F, J);
+    // near leaves in tiles of kFFTileLeaves, double-buffered: the copies of
+    // tile k + 1 are in flight while tile k is summed
+    const int e_beg = F.near_start[L], nnear = F.near_start[L + 1] - e_beg;
+    __shared__ int s_near[kFFNearSmem];
+    const int *near = F.near + e_beg;
+    if (nnear <= kFFNearSmem) {
+        for (int k = threadIdx.x; k < nnear; k += blockDim.x) s_near[k] = near[k];
+        near = s_near;
         __syncthreads();
+    }
+    const int ntiles = (nnear + kFFTileLeaves - 1) / kFFTileLeaves;
+    ff_tile_issue(T2[0], F, near, 0, nnear);
+    cp_async_commit();
+    for (int it = 0; it < ntiles; it++) {
+        if (it + 1 < ntiles) ff_tile_issue(T2[(it + 1) & 1], F, near, (it + 1) * kFFTileLeaves, nnear);
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncthreads();
+        const FFTile &T = T2[it & 1];
+        int self_q = -1;
+#pragma unroll
+        for (int q = 0; q < kFFTileLeaves; q++) {
+            const int e = it * kFFTileLeaves + q;
+            if (e < nnear && near[e] == L) self_q = q;
+        }
         float rmin[kFFPairs][kTeaSeg];
 #pragma unroll
         for (int p = 0; p < kFFPairs; p++)
 #pragma unroll
             for (int sg = 0; sg < kTeaSeg; sg++) rmin[p][sg] = 3.4e38f;
-        const bool self = J == L;
+        const bool self = self_q >= 0;
+        const int self_t = il + self_q * kFFLeaf;
         if (self)
-            ff_step_tile<SLICES, true>(T, sl, il, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az, rmin);
+            ff_step_tile<SLICES, true, !LISTCORR>(T, sl, self_t, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay,
+                                                  az, rmin);
         else
-            ff_step_tile<SLICES, false>(T, sl, il, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay, az, rmin);
-        constexpr int kLen = kFFLeaf / SLICES / kTeaSeg;
+            ff_step_tile<SLICES, false, !LISTCORR>(T, sl, self_t, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay,
+                                                   az, rmin);
+        if (LISTCORR) {   // overlapping pairs are corrected from the pair list below
+            __syncthreads();
+            continue;
+        }
+        constexpr int kLen = kFFTile / SLICES / kTeaSeg;
 #pragma unroll
         for (int p = 0; p < kFFPairs; p++) {
             unsigned segs = 0;
@@ -1053,7 +1113,7 @@ __global__ void __launch_bounds__(kFFLanes *SLICES, 40 / SLICES) k_ff_step(KPara
                     const int t = sl + (sg * kLen + k) * SLICES;
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
-                        if (self && t == il + kFFLanes * (2 * p + h)) continue;
+                        if (self && t == self_t + kFFLanes * (2 * p + h)) continue;
                         const float dx = T.xy[t].x + (h ? nx[p].y : nx[p].x), dy = T.xy[t].z + (h ? ny[p].y : ny[p].x),
                                     dz = T.zf[t].x + (h ? nz[p].y : nz[p].x);
                         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
@@ -1077,6 +1137,48 @@ __global__ void __launch_bounds__(kFFLanes *SLICES, 40 / SLICES) k_ff_step(KPara
             }
         }
         __syncthreads();
+    }
+    if (LISTCORR) {
+        // overlapping pairs (r <= 2a): every one is within the LJ list cutoff
+        // (checked by the launcher), so the far-field term of the tile pass is
+        // replaced by the near one while walking the bead's list; the SLICES
+        // threads of a bead take interleaved entries
+        const int base = B.off[traj], nb = P.nb;
+#pragma unroll
+        for (int h = 0; h < kNI; h++) {
+            const int k = il + h * kFFLanes;
+            if (k >= n) continue;
+            const int g = F.leaf_bead[s0 + k];
+            const int p = h >> 1;
+            const bool hi = h & 1;
+            const float mx = hi ? nx[p].y : nx[p].x, my = hi ? ny[p].y : ny[p].x, mz = hi ? nz[p].y : nz[p].x;
+            const float bx = hi ? cbx[p].y : cbx[p].x, by = hi ? cby[p].y : cby[p].x, bz = hi ? cbz[p].y : cbz[p].x;
+            float3 corr = make_float3(0.f, 0.f, 0.f);
+            const int cnt = B.ljc[g];
+            for (int q = sl; q < cnt; q += SLICES) {
+                const int pj = base + B.lj[q * nb + g];
+                const float4 xj = B.frame_in[pj];
+                const float dx = xj.x + mx, dy = xj.y + my, dz = xj.z + mz;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (!(r2 <= K.four_a2) || (B.flags[pj] & kFlagExtra)) continue;
+                const float4 Fj = B.force[pj], Rj = B.tea_r[pj];
+                const float gx = fmaf(Rj.x, bx, Fj.x), gy = fmaf(Rj.y, by, Fj.y), gz = fmaf(Rj.z, bz, Fj.z);
+                const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+                const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
+                corr.x += nr.x - fa.x;
+                corr.y += nr.y - fa.y;
+                corr.z += nr.z - fa.z;
+            }
+            if (hi) {
+                ax[p].y += corr.x;
+                ay[p].y += corr.y;
+                az[p].y += corr.z;
+            } else {
+                ax[p].x += corr.x;
+                ay[p].x += corr.y;
+                az[p].x += corr.z;
+            }
+        }
     }
 #pragma unroll
     for (int h = 0; h < kNI; h++) {
@@ -1139,25 +1241,33 @@ __global__ void k_ff_rest(KParams P, DevBuffers B, FFBuffers F, float4 *feff, co
 
 void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s) {
     if (F.nleaf == 0) return;
-    k_ff_p2m<<<F.nleaf, kFFLeaf, 0, s>>>(P, B, F, gate);
+    k_ff_p2m<<<F.nleaf + 1, kFFLeaf, 0, s>>>(P, B, F, gate);
     k_ff_m2l<<<F.nleaf, 128, 0, s>>>(P, F, gate);
 }
+
+// Overlapping pairs can be taken from the LJ list when it holds every pair
+// within 2a (plus 2 nm for the motion since its rebuild).
+static bool ff_list_corr(const KParams &P) { return P.lj_on && P.ljcut >= 2.0f * P.tea_a + 2.0f; }
 
 template <int SL, bool FEFF>
 static void ff_step_launch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff, const int *gate,
                            cudaStream_t s) {
-    if (F.nleaf > 0) k_ff_step<SL, FEFF><<<F.nleaf, kFFLanes * SL, 0, s>>>(P, B, F, feff, gate);
+    if (F.nleaf > 0) {
+        if (ff_list_corr(P))
+            k_ff_step<SL, FEFF, true><<<F.nleaf, kFFLanes * SL, 0, s>>>(P, B, F, feff, gate);
+        else
+            k_ff_step<SL, FEFF, false><<<F.nleaf, kFFLanes * SL, 0, s>>>(P, B, F, feff, gate);
+    }
     if (F.nrest > 0) k_ff_rest<FEFF><<<(F.nrest + 127) / 128, 128, 0, s>>>(P, B, F, feff, gate);
 }
 template <bool FEFF>
 static void ff_step_dispatch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff,
                              const int *gate, cudaStream_t s) {
-    // threads per target bead: twice the exact kernel's (a leaf has half its beads i)
     switch (P.tea_slices) {
         case 1:
-        case 2: ff_step_launch<4, FEFF>(P, B, F, feff, gate, s); break;
-        case 4: ff_step_launch<8, FEFF>(P, B, F, feff, gate, s); break;
-        default: ff_step_launch<16, FEFF>(P, B, F, feff, gate, s); break;
+        case 2: ff_step_launch<2, FEFF>(P, B, F, feff, gate, s); break;
+        case 4: ff_step_launch<4, FEFF>(P, B, F, feff, gate, s); break;
+        default: ff_step_launch<8, FEFF>(P, B, F, feff, gate, s); break;
     }
 }
 void launch_ff_step(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,

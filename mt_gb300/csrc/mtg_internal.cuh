@@ -300,7 +300,12 @@ struct FFBuffers {
     float4 *box;             // [2*nleaf] centre, half extent (w unused)
     float4 *q;               // [16*nleaf] proxy m: (QF.xyz, QR.x) at 16L+m, (QR.y, QR.z, 0, 0) at 16L+8+m
     float4 *phi;             // [24*nleaf] target proxy n: (A.xyz, B0.x), (B0.yz, B1.xy), (B1.z, B2.xyz) at 24L+3n
+    float4 *pack;            // [(nleaf+1)*kFFPackF4] each leaf's beads in the tile layout of the step kernel
+                             // (leaf nleaf: padding, far away with zero F and R), written every step by P2M
 };
+// float4 per leaf of FFBuffers::pack: x x y y | z z Fx Fx | Fy Fy Fz Fz | Rx Rx Ry Ry
+// (kFFLeaf each), then Rz Rz of two slots per float4 (kFFLeaf / 2)
+constexpr int kFFPackF4 = 4 * kFFLeaf + kFFLeaf / 2;
 // proxies (P2M) and far-field potentials at target proxies (M2L), while *gate == 0
 void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s);
 // near pairs + interpolated far field + update (FEFF: effective forces into feff, no update), while *gate == 0

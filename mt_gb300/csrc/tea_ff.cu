@@ -150,7 +150,7 @@ static int ff_build(mtg_engine *e) {
                                        &P.far_start, &P.far, &P.rest};
     size_t nints = 0;
     for (auto *v : parts) nints += v->size() + 1;
-    const size_t nf4 = (size_t)(2 + 16 + 24) * std::max(nleaf, 1);
+    const size_t nf4 = (size_t)(2 + 16 + 24) * std::max(nleaf, 1) + (size_t)kFFPackF4 * (nleaf + 1);
     if (nints > e->ff_ints_cap) {
         if (e->ff_ints) cudaFree(e->ff_ints);
         e->ff_ints = nullptr;
@@ -188,6 +188,7 @@ static int ff_build(mtg_engine *e) {
     F.box = e->ff_f4;
     F.q = e->ff_f4 + 2 * (size_t)nleaf;
     F.phi = e->ff_f4 + 18 * (size_t)nleaf;
+    F.pack = e->ff_f4 + 42 * (size_t)std::max(nleaf, 1);
     e->ff_near_pairs = P.near_pairs;
     e->ff_proxy_pairs = P.proxy_pairs;
     e->ff_sizes[0] = nleaf;
@@ -254,6 +255,12 @@ int mtg_tea_effective_forces(mtg_engine *e, float *feff_exact, float *feff_ff, f
     if (!e->have_state) return mtg_internal_fail(MTG_E_STATE, "no state uploaded");
     if (feff_ff && !e->ff_on) return mtg_internal_fail(MTG_E_STATE, "the far field is off");
     FCK(cudaSetDevice(e->device));
+    // the pair lists of the current state (the far-field step corrects
+    // overlapping pairs from the LJ list)
+    if (e->p.lj_on || e->p.is_assembly) {
+        const int rc = mtg_rebuild_pairs(e);
+        if (rc) return rc;
+    }
     const size_t nb = e->nb;
     float4 *buf = nullptr;
     FCK(cudaMalloc(&buf, sizeof(float4) * 2 * nb));
