@@ -931,10 +931,14 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="mtg", choices=["mtg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU-oracle sample (profiling runs)")
+    ap.add_argument("--ff-theta", type=float, default=None,
+                    help="admissibility of the learned mode's far field (default: the workload's)")
     ap.add_argument("--no-suite", action="store_true",
                     help="default workload only, without the other configurations' sub-objects")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
+    if args.ff_theta is not None:
+        spec = dict(spec, theta=args.ff_theta)
     dist = Dist()
     try:
         if args.impl == "reference":
