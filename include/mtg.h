@@ -413,14 +413,19 @@ int mtg_tea_effective_forces(mtg_engine *e, float *feff_exact, float *feff_ff, f
  * work item is split into (1, 2, 3, 4).  With more than one part, the items
  * of the last one to two waves of a launch (all items of a launch shorter
  * than two waves) run as that many shorter CTAs, so the last waves are
- * fuller; the parts' sums meet in a second kernel.  No reference
- * counterpart (the reference launches everything with 32-thread blocks,
- * src/mt.h:34). */
+ * fuller; the parts' sums meet in a second kernel.  plain_persistent: 1 runs
+ * the plain (no-HI) steps between two pair-list rebuilds as one launch with
+ * one CTA per trajectory and the trajectory's frames in shared memory (for
+ * batches whose largest trajectory has at most 2048 beads), 0 one launch
+ * per step; both give identical results.
+ * No reference counterpart (the reference launches everything with 32-thread
+ * blocks, src/mt.h:34). */
 typedef struct {
     int list_method;
     int step_block;
     int tea_slices;
     int tea_jparts;
+    int plain_persistent;
 } mtg_tuning;
 int mtg_get_tuning(mtg_engine *e, mtg_tuning *t);
 int mtg_set_tuning(mtg_engine *e, const mtg_tuning *t);
@@ -444,8 +449,10 @@ int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *devic
  * Kinds: 0 pair-list rebuild, 1 fused plain step, 2 forces (+ TEA random
  * forces), 3 TEA epsilon pass, 4 TEA beta reduction, 5 TEA mobility step,
  * 6 learned-TEA descriptors + network + C_i/beta, 7 learned-TEA re-check,
- * 8 far-field proxies (charges and far potentials), 9 far-field mobility step. */
-#define MTG_KERNEL_KINDS 10
+ * 8 far-field proxies (charges and far potentials), 9 far-field mobility step,
+ * 10 persistent run of plain steps (one launch covers the steps between two
+ * pair-list rebuilds). */
+#define MTG_KERNEL_KINDS 11
 int mtg_set_kernel_timing(mtg_engine *e, int on);
 int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int reset);
 /* Kernel launches replayed from the engine's step graphs since the last

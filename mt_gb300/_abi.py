@@ -104,4 +104,5 @@ def ptr(a, ctype):
 class MtgTuning(C.Structure):
     """mtg_tuning: launch shapes chosen by the autotuner."""
 
-    _fields_ = [("list_method", _i), ("step_block", _i), ("tea_slices", _i), ("tea_jparts", _i)]
+    _fields_ = [("list_method", _i), ("step_block", _i), ("tea_slices", _i), ("tea_jparts", _i),
+                ("plain_persistent", _i)]

@@ -40,14 +40,30 @@ __device__ __forceinline__ void acc_bend(const KParams &P, Acc &A, float rmon, f
     }
 }
 
+// Where a bead's neighbours' frames and flags are read: plane k of local bead
+// j at fr[k * stride + base + j], its flags at fl[base + j].  The per-step
+// kernels read the global frame buffer (stride nb, base = the trajectory's
+// first bead); the persistent kernel reads its trajectory's copy in shared
+// memory (stride = trajectory size, base 0).  Same arithmetic either way.
+struct NbrView {
+    const float4 *fr;
+    const int *fl;
+    int stride, base;
+};
+__device__ __forceinline__ NbrView global_view(const KParams &P, const DevBuffers &B, int traj) {
+    return {B.frame_in, B.flags, P.nb, B.off[traj]};
+}
+
 // Generalised force on bead g (compute_kernel, src/compute_cuda.cu:32-525):
 // harmonic + bending, Morse longitudinal + bending, Morse lateral with seam
 // coefficient, barriers, LJ inside 6 nm, walls.  out = (fx, fy, fz, ffi,
 // ftheta, fpsi).
-__device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &B, int g, int traj, int base,
+__device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &B, const NbrView &V, int g, int traj,
                                             int flags, const Frame &Fi, float out[6]) {
-    const int nb = P.nb;
-    const float4 *fr = B.frame_in;
+    const int nb = P.nb;          // list layout (k-major over all beads)
+    const int ps = V.stride;      // plane stride of the neighbour frames
+    const int base = V.base;
+    const float4 *fr = V.fr;
     Acc A = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const float3 uzi = f3(Fi.p1);
     const bool off_tub = (flags & kFlagOnTubule) == 0;
@@ -71,14 +87,14 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         const int e = k == 0 ? e_h0 : B.harm[g * P.maxH + k];
         const float rmon = e < 0 ? 2.0f : -2.0f;
         const int pj = base + (e < 0 ? -e : e);
-        const float4 rj = fr[pj], uj = fr[nb + pj];
+        const float4 rj = fr[pj], uj = fr[ps + pj];
         const float3 wi = make_float3(uzi.x * rmon, uzi.y * rmon, uzi.z * rmon);
         const float3 wj = make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon);
         const float3 d = site_delta(Fi.p0, rj, wi, wj);
         const float dr = norm3_rn(d);
         acc_pair(A, P.C, d, wi);
         if (dr < 1.0f) {
-            const float thj = fr[2 * nb + pj].w;
+            const float thj = fr[2 * ps + pj].w;
             acc_bend(P, A, rmon, uj.w - Fi.p1.w, rj.w - Fi.p0.w, thj - Fi.p2.w,
                      (flags & kFlagGtp) ? P.th0_gtp : P.th0_gdp);
         }
@@ -88,7 +104,7 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         const int e = k == 0 ? e_l0 : B.lon[k * nb + g];
         const float rmon = e < 0 ? 2.0f : -2.0f;
         const int pj = base + (e < 0 ? -e : e);
-        const float4 rj = fr[pj], uj = fr[nb + pj];
+        const float4 rj = fr[pj], uj = fr[ps + pj];
         const float3 wi = make_float3(uzi.x * rmon, uzi.y * rmon, uzi.z * rmon);
         const float3 wj = make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon);
         const float3 d = site_delta(Fi.p0, rj, wi, wj);
@@ -96,15 +112,15 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         float dUdr = dr == 0.0f ? 0.0f : dmorse(P.D_long, P.A_long, dr) / dr;
         int fj = -1;
         if (P.barrier) {
-            fj = B.flags[pj];
+            fj = V.fl[pj];
             if (off_tub && (fj & kFlagOnTubule) == 0 && dr != 0.0f) dUdr += dbarr(P.a_bl, P.r_bl, P.w_bl, dr) / dr;
         }
         acc_pair(A, dUdr, d, wi);
         if (dr < 1.0f) {
             // theta0 of the bead nearer the plus end (:282-283)
             int glast = flags;
-            if (!(Fi.p0.z > rj.z)) glast = fj >= 0 ? fj : B.flags[pj];
-            const float thj = fr[2 * nb + pj].w;
+            if (!(Fi.p0.z > rj.z)) glast = fj >= 0 ? fj : V.fl[pj];
+            const float thj = fr[2 * ps + pj].w;
             acc_bend(P, A, rmon, uj.w - Fi.p1.w, rj.w - Fi.p0.w, thj - Fi.p2.w,
                      (glast & kFlagGtp) ? P.th0_gtp : P.th0_gdp);
         }
@@ -117,11 +133,11 @@ __device__ __forceinline__ void bead_forces(const KParams &P, const DevBuffers &
         if (j == kZeroCode) j = 0;
         const int pj = base + j;
         const float4 rj = fr[pj];
-        const float4 sj = neg ? fr[3 * nb + pj] : fr[2 * nb + pj];
+        const float4 sj = neg ? fr[3 * ps + pj] : fr[2 * ps + pj];
         const float3 wi = neg ? f3(Fi.p2) : f3(Fi.p3);
         const float3 d = site_delta(Fi.p0, rj, wi, f3(sj));
         const float dr = norm3_rn(d);
-        const int fj = B.flags[pj];
+        const int fj = V.fl[pj];
         const float D = ((flags ^ fj) & kFlagBeta) ? P.D_lat_seam : P.D_lat;
         float dUdr = dr == 0.0f ? 0.0f : dmorse(D, P.A_lat, dr) / dr;
         if (P.barrier && off_tub && (fj & kFlagOnTubule) == 0 && dr != 0.0f)
@@ -193,8 +209,9 @@ __device__ __forceinline__ Frame load_frame(const float4 *planes, int nb, int g)
 }
 
 // Euler-Maruyama update of one moving bead (integrate_kernel,
-// src/compute_cuda.cu:955-963): xyz from normals gx, angles from ga.
-__device__ __forceinline__ Frame em_update(const KParams &P, const Frame &Fi, const float f[6], float4 gx,
+// src/compute_cuda.cu:955-963): xyz from normals gx, angles from ga.  Not
+// inlined, for the reason given at make_frame.
+__device__ __noinline__ Frame em_update(const KParams &P, const Frame &Fi, const float f[6], float4 gx,
                                            float4 ga) {
     const float x = Fi.p0.x + (P.kr * f[0] + P.varR * gx.x);
     const float y = Fi.p0.y + (P.kr * f[1] + P.varR * gx.y);
@@ -217,7 +234,7 @@ __global__ void __launch_bounds__(256) k_step_plain(KParams P, DevBuffers B) {
         const bool moving = !(flags & kFlagFixed);
         if (moving || KEEP_FORCES) {
             const int traj = B.traj[g];
-            bead_forces(P, B, g, traj, B.off[traj], flags, Fi, f);
+            bead_forces(P, B, global_view(P, B, traj), g, traj, flags, Fi, f);
         }
         if (moving) {
             uint4 s1 = B.seeds[g], s2 = B.seeds[nb + g];
@@ -234,6 +251,94 @@ __global__ void __launch_bounds__(256) k_step_plain(KParams P, DevBuffers B) {
     }
 }
 
+// ------------------------------------------------------- persistent period
+// A whole run of plain steps between two pair-list rebuilds in one launch:
+// one CTA per trajectory keeps the trajectory's frames (the four planes) and
+// flags in shared memory across the steps, so every neighbour gather of the
+// force loop is a shared-memory load; the pair lists and noise streams stay
+// in global memory (L2).  Each step is a force phase over the CTA's beads, a
+// barrier, the Euler-Maruyama update of every moving bead into shared
+// memory, and a barrier; trajectories never interact, so no grid-wide
+// synchronisation is needed.  The arithmetic is bead_forces / em_update, as in
+// k_step_plain: the result equals that of nsteps launches of k_step_plain bit
+// for bit.  At the end the frames go to the buffer the engine's step parity
+// expects (frame_out for an odd number of steps, frame_in otherwise).
+template <bool KEEP_FORCES>
+__global__ void __launch_bounds__(kPeriodThreads, 2) k_step_period(KParams P, DevBuffers B, int nsteps, int nmax) {
+    extern __shared__ float4 s_dyn[];
+    const int traj = blockIdx.x;
+    const int base = B.off[traj], n = B.off[traj + 1] - base;
+    const int nb = P.nb, nt = blockDim.x;
+    float4 *sf = s_dyn;                                       // plane k of bead j at sf[k * n + j]
+    int *sfl = reinterpret_cast<int *>(s_dyn + 4 * (size_t)nmax);
+    for (int j = threadIdx.x; j < n; j += nt) {
+        const int g = base + j;
+        sf[j] = B.frame_in[g];
+        sf[n + j] = B.frame_in[nb + g];
+        sf[2 * n + j] = B.frame_in[2 * nb + g];
+        sf[3 * n + j] = B.frame_in[3 * nb + g];
+        sfl[j] = B.flags[g];
+    }
+    __syncthreads();
+    const NbrView V = {sf, sfl, n, 0};
+    float f[kPeriodBeads][6];
+    for (int step = 0; step < nsteps; step++) {
+#pragma unroll
+        for (int q = 0; q < kPeriodBeads; q++) {
+            const int j = threadIdx.x + q * nt;
+#pragma unroll
+            for (int c = 0; c < 6; c++) f[q][c] = 0.f;
+            if (j < n) {
+                const int fl = sfl[j];
+                if (!(fl & kFlagExtra) && (KEEP_FORCES || !(fl & kFlagFixed))) {
+                    Frame Fi;
+                    Fi.p0 = sf[j];
+                    Fi.p1 = sf[n + j];
+                    Fi.p2 = sf[2 * n + j];
+                    Fi.p3 = sf[3 * n + j];
+                    bead_forces(P, B, V, base + j, traj, fl, Fi, f[q]);
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kPeriodBeads; q++) {
+            const int j = threadIdx.x + q * nt;
+            if (j >= n) continue;
+            const int fl = sfl[j], g = base + j;
+            if (!(fl & (kFlagExtra | kFlagFixed))) {
+                Frame Fi;
+                Fi.p0 = sf[j];
+                Fi.p1 = sf[n + j];
+                Fi.p2 = sf[2 * n + j];
+                Fi.p3 = sf[3 * n + j];
+                uint4 s1 = B.seeds[g], s2 = B.seeds[nb + g];
+                const float4 gx = gauss4(s1), ga = gauss4(s2);
+                B.seeds[g] = s1;
+                B.seeds[nb + g] = s2;
+                Fi = em_update(P, Fi, f[q], gx, ga);
+                sf[j] = Fi.p0;
+                sf[n + j] = Fi.p1;
+                sf[2 * n + j] = Fi.p2;
+                sf[3 * n + j] = Fi.p3;
+            }
+            if (KEEP_FORCES && step == nsteps - 1) {
+                B.force[g] = make_float4(f[q][0], f[q][1], f[q][2], 0.f);
+                B.force[nb + g] = make_float4(f[q][3], f[q][4], f[q][5], 0.f);
+            }
+        }
+        __syncthreads();
+    }
+    float4 *out = (nsteps & 1) ? B.frame_out : B.frame_in;
+    for (int j = threadIdx.x; j < n; j += nt) {
+        const int g = base + j;
+        out[g] = sf[j];
+        out[nb + g] = sf[n + j];
+        out[2 * nb + g] = sf[2 * n + j];
+        out[3 * nb + g] = sf[3 * n + j];
+    }
+}
+
 // Forces only (for output and the TEA path).  With TEA_PREPARE it also draws
 // the random force of every bead from stream g scaled by sqrt(2 kB T gammaR /
 // dt) (integrateTea_prepare, src/bdhitea_kernel.cu:16-36).
@@ -247,7 +352,7 @@ __global__ void __launch_bounds__(256) k_forces(KParams P, DevBuffers B) {
     if (!(flags & kFlagExtra)) {
         const Frame Fi = load_frame(B.frame_in, nb, g);
         const int traj = B.traj[g];
-        bead_forces(P, B, g, traj, B.off[traj], flags, Fi, f);
+        bead_forces(P, B, global_view(P, B, traj), g, traj, flags, Fi, f);
     }
     B.force[g] = make_float4(f[0], f[1], f[2], 0.f);
     B.force[nb + g] = make_float4(f[3], f[4], f[5], 0.f);
@@ -440,6 +545,29 @@ void launch_step_plain(const KParams &P, const DevBuffers &B, bool keep_forces, 
     else
         k_step_plain<false><<<blocks(P.nb, t), t, 0, s>>>(P, B);
 }
+size_t period_smem_bytes(int nmax) { return (size_t)nmax * (4 * sizeof(float4) + sizeof(int)); }
+bool period_fits(int nmax) {
+    return nmax > 0 && nmax <= kPeriodThreads * kPeriodBeads && period_smem_bytes(nmax) <= kPeriodMaxSmem;
+}
+int period_prepare(int nmax) {
+    const int bytes = (int)period_smem_bytes(nmax);
+    if (cudaFuncSetAttribute(k_step_period<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_step_period<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+        return -1;
+    return 0;
+}
+void launch_step_period(const KParams &P, const DevBuffers &B, bool keep_forces, int nsteps, int nmax,
+                        cudaStream_t s) {
+    int t = ((nmax + 31) / 32) * 32;
+    if (t > kPeriodThreads) t = kPeriodThreads;
+    const size_t bytes = period_smem_bytes(nmax);
+    if (keep_forces)
+        k_step_period<true><<<P.nt, t, bytes, s>>>(P, B, nsteps, nmax);
+    else
+        k_step_period<false><<<P.nt, t, bytes, s>>>(P, B, nsteps, nmax);
+}
+
 void launch_forces(const KParams &P, const DevBuffers &B, bool tea_prepare, cudaStream_t s) {
     if (tea_prepare)
         k_forces<true><<<blocks(P.nb, 128), 128, 0, s>>>(P, B);

@@ -315,6 +315,23 @@ void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
     e->cur ^= 1;
 }
 
+// The persistent plain path applies (see mtg_tuning::plain_persistent).
+bool period_active(const mtg_engine *e) { return e->persistent && !e->p.hdi_on && period_fits(e->max_traj_beads); }
+
+// Enqueues steps step .. step+run-1 of the plain loop as one persistent launch,
+// after the pair-list rebuild due at `step`; run never crosses a rebuild.
+void enqueue_period_run(mtg_engine *e, long long step, int run, bool allow_rebuild = true) {
+    const mtg_params &p = e->p;
+    if (allow_rebuild && step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
+        timed_launch(e, 0, [&] { launch_lists(e); });
+        e->lists_valid = true;
+    }
+    timed_launch(e, 10, [&] {
+        launch_step_period(e->kp, e->bufs(), e->keep_forces, run, e->max_traj_beads, e->stream);
+    });
+    if (run & 1) e->cur ^= 1;
+}
+
 // Creates event pairs up to slot `upto` (never called during a capture).
 void reserve_slots(mtg_engine *e, int upto) {
     while ((int)e->ev_a.size() < upto) {
@@ -846,7 +863,10 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
     if (e->lists_fresh && s < end && s % p.ljpairsupdatefreq == 0) {
         // the caller rebuilt the lists for this step already (reference order:
         // rebuild, host hooks, forces; src/compute_cuda.cu:1140-1228)
-        enqueue_step(e, s, false);
+        if (period_active(e))
+            enqueue_period_run(e, s, 1, false);
+        else
+            enqueue_step(e, s, false);
         s++;
     }
     if (nsteps > 0) e->lists_fresh = false;
@@ -870,7 +890,17 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
                 e->capturing = true;
                 cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
                 if (ce == cudaSuccess) {
-                    for (long long k = 0; k < period; k++) enqueue_step(e, k);
+                    if (period_active(e)) {
+                        const long long freq = p.ljpairsupdatefreq;
+                        for (long long k = 0; k < period;) {
+                            long long run = freq - k % freq;
+                            if (k + run > period) run = period - k;
+                            enqueue_period_run(e, k, (int)run);
+                            k += run;
+                        }
+                    } else {
+                        for (long long k = 0; k < period; k++) enqueue_step(e, k);
+                    }
                     ce = cudaStreamEndCapture(e->stream, &g);
                 }
                 e->capturing = false;
@@ -893,6 +923,13 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
             if (period & 1) e->cur ^= 1;
             if (p.lj_on || p.is_assembly) e->lists_valid = true;
             s += period;
+        } else if (period_active(e)) {
+            // outside a graph the persistent path runs up to the next rebuild
+            const long long freq = p.ljpairsupdatefreq;
+            long long run = freq - s % freq;
+            if (s + run > end) run = end - s;
+            enqueue_period_run(e, s, (int)run);
+            s += run;
         } else {
             enqueue_step(e, s);
             s++;
@@ -953,6 +990,7 @@ int mtg_get_tuning(mtg_engine *e, mtg_tuning *t) {
     t->step_block = e->kp.step_block;
     t->tea_slices = e->kp.tea_slices;
     t->tea_jparts = e->kp.tea_jparts;
+    t->plain_persistent = e->persistent ? 1 : 0;
     return MTG_OK;
 }
 
@@ -963,8 +1001,18 @@ int mtg_set_tuning(mtg_engine *e, const mtg_tuning *t) {
     if (t->tea_slices != 1 && t->tea_slices != 2 && t->tea_slices != 4 && t->tea_slices != 8)
         return fail(MTG_E_CONFIG, "tea_slices must be 1, 2, 4 or 8");
     if (t->tea_jparts < 1 || t->tea_jparts > kTeaMaxParts) return fail(MTG_E_CONFIG, "tea_jparts must be 1..4");
+    if (t->plain_persistent != 0 && t->plain_persistent != 1) return fail(MTG_E_CONFIG, "plain_persistent must be 0 or 1");
+    if (t->plain_persistent && !period_fits(e->max_traj_beads))
+        return fail(MTG_E_CONFIG, "plain_persistent needs trajectories of at most %d beads",
+                    kPeriodThreads * kPeriodBeads);
     int rc = mtg_set_list_method(e, t->list_method);
     if (rc) return rc;
+    if (t->plain_persistent) {
+        cudaSetDevice(e->device);
+        if (period_prepare(e->max_traj_beads) != 0)
+            return fail(MTG_E_CUDA, "the persistent step kernel could not reserve its shared memory");
+    }
+    e->persistent = t->plain_persistent != 0;
     e->kp.step_block = t->step_block;
     e->kp.tea_slices = t->tea_slices;
     e->kp.tea_jparts = t->tea_jparts;
@@ -994,9 +1042,10 @@ int mtg_autotune(mtg_engine *e, long long first_step, int trial_steps, mtg_tunin
         if (lm == 1 && !lists && !cands.empty()) continue;
         if (e->p.hdi_on) {
             for (int sl : {1, 2, 4, 8})
-                for (int jp = 1; jp <= kTeaMaxParts; jp++) cands.push_back({lm, orig.step_block, sl, jp});
+                for (int jp = 1; jp <= kTeaMaxParts; jp++) cands.push_back({lm, orig.step_block, sl, jp, 0});
         } else {
-            for (int bs : {64, 128, 256}) cands.push_back({lm, bs, orig.tea_slices, orig.tea_jparts});
+            for (int bs : {64, 128, 256}) cands.push_back({lm, bs, orig.tea_slices, orig.tea_jparts, 0});
+            if (period_fits(e->max_traj_beads)) cands.push_back({lm, orig.step_block, orig.tea_slices, orig.tea_jparts, 1});
         }
     }
     float best_t = 3.4e38f;

@@ -59,6 +59,8 @@ struct mtg_engine {
     double kt_total[MTG_KERNEL_KINDS] = {0};
     long long kt_count[MTG_KERNEL_KINDS] = {0};
     cudaEvent_t call_a = nullptr, call_b = nullptr;
+    // plain steps between rebuilds as one persistent launch (k_step_period)
+    bool persistent = false;
     // list rebuild method: 0 auto, 1 brute-force tiles, 2 cell list
     int list_method = 0;
     bool use_cells = false;

@@ -136,8 +136,11 @@ struct Frame {
 
 __device__ __forceinline__ float3 f3(const float4 &v) { return make_float3(v.x, v.y, v.z); }
 
-// Builds the four planes of a bead from its state.
-__device__ __forceinline__ Frame make_frame(const KParams &P, float x, float y, float z, float fi,
+// Builds the four planes of a bead from its state.  Not inlined: every
+// kernel of a translation unit then runs the same compiled arithmetic (the
+// per-step and the persistent plain step must agree bit for bit, and an
+// inlined copy could contract multiply-adds differently in each).
+static __device__ __noinline__ Frame make_frame(const KParams &P, float x, float y, float z, float fi,
                                             float theta, float psi) {
     float sf, cf, st, ct, sp, cp;
     sincosf(fi, &sf, &cf);
@@ -255,6 +258,16 @@ float bin_beads(const KParams &P, const DevBuffers &B, const CellBuffers &C, flo
                 cudaStream_t s);
 void launch_step_plain(const KParams &P, const DevBuffers &B, bool keep_forces, cudaStream_t s);
 void launch_forces(const KParams &P, const DevBuffers &B, bool tea_prepare, cudaStream_t s);
+// Persistent run of nsteps plain steps (no rebuild inside), one CTA per
+// trajectory with its frames in shared memory; nmax = the largest trajectory.
+constexpr int kPeriodThreads = 256;
+constexpr int kPeriodBeads = 8;                   // beads per thread: trajectories up to 2048 beads
+constexpr size_t kPeriodMaxSmem = 227 * 1024;     // bytes of dynamic shared memory a CTA may hold
+size_t period_smem_bytes(int nmax);
+bool period_fits(int nmax);
+int period_prepare(int nmax);                     // opts the kernel into its shared memory (outside captures)
+void launch_step_period(const KParams &P, const DevBuffers &B, bool keep_forces, int nsteps, int nmax,
+                        cudaStream_t s);
 void launch_energy(const KParams &P, const DevBuffers &B, double *per_bead, double *partials,
                    const int2 *work, int nwork, cudaStream_t s);
 void launch_energy_totals(const KParams &P, const double *partials, const int *work_first, double *per_traj,

@@ -96,7 +96,7 @@ SURROGATE_OUTPUTS = 4
 SURROGATE_PARAMS = 37764
 
 KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step", "surrogate", "recheck",
-                "ff_proxies", "ff_step")
+                "ff_proxies", "ff_step", "step_period")
 
 _lib = None
 
@@ -401,10 +401,11 @@ class Engine:
         t = MtgTuning()
         check(self.lib.mtg_get_tuning(self.h, C.byref(t)))
         return {"list_method": t.list_method, "step_block": t.step_block, "tea_slices": t.tea_slices,
-                "tea_jparts": t.tea_jparts}
+                "tea_jparts": t.tea_jparts, "plain_persistent": t.plain_persistent}
 
-    def set_tuning(self, list_method: int, step_block: int, tea_slices: int, tea_jparts: int = 1):
-        t = MtgTuning(list_method, step_block, tea_slices, tea_jparts)
+    def set_tuning(self, list_method: int, step_block: int, tea_slices: int, tea_jparts: int = 1,
+                   plain_persistent: int = 0):
+        t = MtgTuning(list_method, step_block, tea_slices, tea_jparts, plain_persistent)
         check(self.lib.mtg_set_tuning(self.h, C.byref(t)))
 
     def autotune(self, first_step: int, trial_steps: int, cache: str | None = None, key: str | None = None):
@@ -423,7 +424,7 @@ class Engine:
         ms = C.c_float()
         check(self.lib.mtg_autotune(self.h, C.c_longlong(first_step), trial_steps, C.byref(t), C.byref(ms)))
         entry = {"tuning": {"list_method": t.list_method, "step_block": t.step_block, "tea_slices": t.tea_slices,
-                            "tea_jparts": t.tea_jparts},
+                            "tea_jparts": t.tea_jparts, "plain_persistent": t.plain_persistent},
                  "trial_ms": ms.value, "cached": False}
         if cache and key:
             try:

@@ -480,3 +480,48 @@ def test_assembly_lists_without_lj_prefilter(engine_mod, oracle_lib, over, metho
     for c in range(6):
         assert rel_norm(f[:, c], fo[:, c]) < FORCE_RTOL, c
     e.close()
+
+
+@pytest.mark.parametrize("keep", [False, True])
+def test_persistent_period_equals_per_step_kernels(engine_mod, keep):
+    """The persistent plain path (one launch per pair-list period, one CTA per
+    trajectory with its frames in shared memory) gives the per-step kernels'
+    result bit for bit, on an uneven batch with extra and fixed beads, with
+    and without stored forces."""
+    from mt_gb300 import synth
+    p = synth.default_params(seed=61)
+    trajs = [synth.make_trajectory(14, 120, seed=61, radius=8.12, psi_mode="make_mt", cube=50.0, thermal=0.05,
+                                   n_extra_dimers=2),
+             synth.make_trajectory(4, 0, seed=62, radius=8.12, psi_mode="make_mt", cube=50.0, thermal=0.05),
+             synth.make_trajectory(30, 400, seed=63, radius=8.12, psi_mode="make_mt", cube=60.0, thermal=0.05)]
+    b = synth.batch_from_trajectories(p, trajs)
+    runs = []
+    for persistent in (0, 1):
+        e = make_engine(engine_mod, b)
+        e.set_keep_forces(keep)
+        t = e.tuning()
+        e.set_tuning(t["list_method"], t["step_block"], t["tea_slices"], t["tea_jparts"], persistent)
+        e.set_kernel_timing(True)
+        e.step(0, 35)                      # three periods from graphs + a direct tail
+        kt = e.kernel_times()
+        assert (kt["step_period"][1] > 0) == bool(persistent)
+        runs.append((e.download_state(forces=True), e.download_rng(), e.lists()))
+        e.close()
+    (x0, f0), r0, l0 = runs[0]
+    (x1, f1), r1, l1 = runs[1]
+    assert np.array_equal(x0, x1) and np.array_equal(r0, r1)
+    if keep:
+        assert np.array_equal(f0, f1)
+    for k in ("lj", "long", "lat"):
+        assert np.array_equal(l0[k][0], l1[k][0]) and np.array_equal(l0[k][1], l1[k][1])
+
+
+def test_persistent_rejects_large_trajectories(engine_mod):
+    from mt_gb300 import synth
+    p = synth.default_params(seed=64)
+    b = synth.uniform_batch(p, 1, 120, 2000, seed=64, cube=150.0)     # 3560 beads
+    e = make_engine(engine_mod, b)
+    t = e.tuning()
+    with pytest.raises(engine_mod.MtgError, match="2048"):
+        e.set_tuning(t["list_method"], t["step_block"], t["tea_slices"], t["tea_jparts"], 1)
+    e.close()
