@@ -161,6 +161,11 @@ int mtg_num_beads(const mtg_engine *e, int *nbeads, int *ntraj);
 /* Re-seeds all 2*nbeads HybridTaus streams with the reference's ran2-based
  * generator (src/HybridTaus.cu:32-48, src/ran2.h:18-56). */
 int mtg_seed_rng(mtg_engine *e, int rseed);
+/* The HybridTaus states of nstreams streams (4*nstreams uint32) as
+ * generateSeeds makes them from rseed (src/HybridTaus.cu:32-48), on the host
+ * only: how a batch split over several engines gets the streams one engine
+ * of the whole batch would have (stream g and g + nbeads of each bead). */
+int mtg_generate_seeds(int rseed, long long nstreams, uint32_t *seeds);
 /* Reads / writes the raw HybridTaus states, 2*nbeads uint4 = 8*nbeads uint32
  * (stream p drives xyz noise of bead p, stream p+nbeads its angle noise). */
 int mtg_download_rng(mtg_engine *e, uint32_t *seeds);
@@ -365,6 +370,16 @@ int mtg_tea_training_data(mtg_engine *e, float *X, float *T);
  * are compared; when their RMS difference relative to the exact ones
  * exceeds max_err the engine falls back to exact TEA for good. */
 int mtg_set_surrogate(mtg_engine *e, mtg_surrogate *s, int recheck_every, float max_err);
+/* Polls of each bounded wait of the surrogate's tensor-core inference for
+ * the MMAs of a layer: polls < 0 restores the default (2^20); 0 makes every
+ * such wait give up at once (a test of the timeout path).  A wait that runs out ends the
+ * call with MTG_E_TIMEOUT (mtg_surrogate_predict, or the mtg_step whose
+ * learned-TEA work it was) instead of blocking: the kernel records the
+ * timeout, waits up to the default limit for the MMAs it already issued,
+ * frees its tensor memory and returns, and the next call runs normally.
+ * Takes effect for step graphs captured after the call.  The reference has
+ * no bounded wait: its CUDA errors end the program (src/Cuda.h:120-135). */
+int mtg_surrogate_set_wait_limit(mtg_surrogate *s, int polls);
 /* fell_back: 1 after a fall-back; rechecks: re-checks done; last_error: the
  * last re-check's RMS relative difference. */
 int mtg_surrogate_status(mtg_engine *e, int *fell_back, int *rechecks, double *last_error);

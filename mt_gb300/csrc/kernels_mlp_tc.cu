@@ -69,7 +69,8 @@ __device__ __forceinline__ bool group_and(int g, bool v) {
 // to Z [n][3][kHid] for the backward pass.
 template <bool TRAIN>
 __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd_tc(const Weights W, const float *X, const int *idx, int n,
-                                                               const float *norm, float *Y, float *Z, int *err) {
+                                                               const float *norm, float *Y, float *Z, int *err,
+                                                               uint32_t spin) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd_tc(const Weights W, 
                     issue_layer(tmem, ah, bw[layer], kHid, instr_desc(kTcRows, layer == 3 ? kOutPad : kHid));
                 mma_commit(mbar);
             }
-            ok = group_and(g, mbar_wait(mbar, phase));
+            ok = group_and(g, mbar_wait(mbar, phase, spin));   // the tile loop's wait: `spin` polls
             phase ^= 1u;
             if (!ok) break;
             fence_after_sync();
@@ -202,8 +203,9 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd_tc(const Weights W, 
             if (gtid == 0) {
                 atomicOr(err, kErrTimeout);
                 // the MMAs already issued may still run: give them a bounded
-                // time to finish before the TMEM goes back
-                mbar_wait(mbar, phase ^ 1u);
+                // time (the full default limit, whatever `spin` is) to finish
+                // before the TMEM goes back
+                mbar_wait(mbar, phase ^ 1u, kSpinLimit);
             }
             break;
         }
@@ -218,6 +220,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd_tc(const Weights W, 
 }
 
 size_t infer_tc_smem() { return sizeof(TcSmem) + 128; }
+
+uint32_t tc_default_spin() { return kSpinLimit; }
 
 cudaError_t prepare_tc() {
     cudaError_t e =
@@ -236,11 +240,11 @@ int sm_count() {
 }
 
 cudaError_t launch_infer_tc(const Weights &W, const float *X, int n, const float *norm, float *Y, int *err,
-                            cudaStream_t s) {
+                            cudaStream_t s, uint32_t spin) {
     const int tiles = (n + kTcRows - 1) / kTcRows;
     if (tiles == 0) return cudaSuccess;
     const int sms = sm_count(), grid = tiles < sms ? tiles : sms;
-    k_mlp_fwd_tc<false><<<grid, kFwdThreads, infer_tc_smem(), s>>>(W, X, nullptr, n, norm, Y, nullptr, err);
+    k_mlp_fwd_tc<false><<<grid, kFwdThreads, infer_tc_smem(), s>>>(W, X, nullptr, n, norm, Y, nullptr, err, spin);
     return cudaGetLastError();
 }
 
@@ -249,7 +253,7 @@ cudaError_t launch_forward_tc(const Weights &W, const float *X, const int *idx, 
     const int tiles = (n + kTcRows - 1) / kTcRows;
     if (tiles == 0) return cudaSuccess;
     const int sms = sm_count(), grid = tiles < sms ? tiles : sms;
-    k_mlp_fwd_tc<true><<<grid, kFwdThreads, infer_tc_smem(), s>>>(W, X, idx, n, norm, Y, Z, err);
+    k_mlp_fwd_tc<true><<<grid, kFwdThreads, infer_tc_smem(), s>>>(W, X, idx, n, norm, Y, Z, err, kSpinLimit);
     return cudaGetLastError();
 }
 

@@ -712,6 +712,14 @@ int mtg_seed_rng(mtg_engine *e, int rseed) {
     return mtg_upload_rng(e, s.data());
 }
 
+int mtg_generate_seeds(int rseed, long long nstreams, uint32_t *seeds) {
+    if (!seeds || nstreams < 0) return fail(MTG_E_CONFIG, "seeds is NULL or nstreams negative");
+    std::vector<uint32_t> s;
+    make_seeds(rseed, (size_t)nstreams, s);
+    std::memcpy(seeds, s.data(), sizeof(uint32_t) * s.size());
+    return MTG_OK;
+}
+
 int mtg_upload_rng(mtg_engine *e, const uint32_t *seeds) {
     if (!e || !seeds) return fail(MTG_E_CONFIG, "engine or seeds is NULL");
     cudaSetDevice(e->device);

@@ -54,9 +54,12 @@ cudaError_t launch_loss_sum(const float *part, int nparts, float *out, cudaStrea
 
 // Inference on the tcgen05 tensor cores (kernels_mlp_tc.cu): Y = network of
 // the normalised X, n rows; a wait that runs out sets kErrTimeout in *err.
+// spin: polls of each wait for a layer's MMAs (0: none, the wait gives up at
+// once); tc_default_spin() is the limit every other wait uses.
 cudaError_t prepare_tc();
+uint32_t tc_default_spin();
 cudaError_t launch_infer_tc(const Weights &W, const float *X, int n, const float *norm, float *Y, int *err,
-                            cudaStream_t s);
+                            cudaStream_t s, uint32_t spin = tc_default_spin());
 // Training on the tcgen05 tensor cores: the forward pass with the
 // pre-activations Z [n][3][kHid] (rows of X gathered through idx, may be
 // NULL), and the backward pass (kernels_mlp_train_tc.cu) writing per-CTA

@@ -70,9 +70,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t phase) {
     return ok != 0;
 }
 
-// Bounded wait for the given phase of the mbarrier; true when it completed.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
-    for (uint32_t i = 0; i < kSpinLimit; i++)
+// Bounded wait for the given phase of the mbarrier (at most `limit` polls);
+// true when it completed.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, uint32_t limit = kSpinLimit) {
+    for (uint32_t i = 0; i < limit; i++)
         if (mbar_try_wait(mbar, phase)) return true;
     return false;
 }

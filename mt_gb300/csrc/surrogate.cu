@@ -319,6 +319,7 @@ struct mtg_surrogate {
     __nv_bfloat16 *bf = nullptr;  // all BF16 copies
     int *err = nullptr;            // device error word of the tensor-core inference
     int adam_step = 0;
+    uint32_t spin = mlp::tc_default_spin();   // polls of the inference's waits for its MMAs
 };
 
 namespace {
@@ -447,7 +448,7 @@ int mtg_surrogate_predict(mtg_surrogate *s, const float *X, int n, float *Y) {
     SCK(cudaMalloc(&dX, sizeof(float) * (size_t)n * mlp::kIn + 16));
     SCK(cudaMalloc(&dY, sizeof(float) * (size_t)n * mlp::kOut + 16));
     SCK(cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * mlp::kIn, cudaMemcpyHostToDevice, s->stream));
-    SCK(mlp::launch_infer_tc(s->W, dX, n, s->norm, dY, s->err, s->stream));
+    SCK(mlp::launch_infer_tc(s->W, dX, n, s->norm, dY, s->err, s->stream, s->spin));
     int herr = 0;
     SCK(cudaMemcpyAsync(Y, dY, sizeof(float) * (size_t)n * mlp::kOut, cudaMemcpyDeviceToHost, s->stream));
     SCK(cudaMemcpyAsync(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
@@ -680,7 +681,8 @@ void enqueue_surrogate_eps(mtg_engine *e) {
     const float inv = bin_beads(e->kp, B, e->cells(), kDescCut, true, e->stream);
     k_descriptors<<<e->nwork, kTile, 0, e->stream>>>(e->kp, B, e->cells(), e->work, inv, e->surr_stats, e->surr_desc,
                                                      gate);
-    mlp::launch_infer_tc(e->surr->W, e->surr_desc, e->nb, e->surr->norm, e->surr_pred, e->err, e->stream);
+    mlp::launch_infer_tc(e->surr->W, e->surr_desc, e->nb, e->surr->norm, e->surr_pred, e->err, e->stream,
+                         e->surr->spin);
     k_surr_beta<<<e->nt, 256, 0, e->stream>>>(e->kp, B, e->surr_pred, e->surr->ynorm, gate);
     k_surr_ci<<<(e->nb + 255) / 256, 256, 0, e->stream>>>(e->kp, B, e->surr_pred, e->surr->ynorm, gate);
     // after a fallback the exact pass runs instead (gated on the flag)
@@ -732,6 +734,12 @@ int mtg_set_surrogate(mtg_engine *e, mtg_surrogate *s, int recheck_every, float 
     SCK(cudaMemsetAsync(e->surr_err, 0, sizeof(double), e->stream));
     SCK(cudaStreamSynchronize(e->stream));
     mtg_internal_reset_graphs(e);
+    return MTG_OK;
+}
+
+int mtg_surrogate_set_wait_limit(mtg_surrogate *s, int polls) {
+    if (!s) return sfail(MTG_E_CONFIG, "surrogate is NULL");
+    s->spin = polls < 0 ? mlp::tc_default_spin() : (uint32_t)polls;
     return MTG_OK;
 }
 

@@ -27,6 +27,7 @@ EXPORTS = {
     "mtg_seed_rng": (C.c_int, [C.c_void_p, C.c_int]),
     "mtg_download_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "mtg_upload_rng": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
+    "mtg_generate_seeds": (C.c_int, [C.c_int, C.c_longlong, C.POINTER(C.c_uint32)]),
     "mtg_write_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.c_longlong]),
     "mtg_output_open": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int, C.c_int,
                                   C.c_int, C.c_float, C.c_char_p, C.c_char_p]),
@@ -83,6 +84,7 @@ EXPORTS = {
     "mtg_tea_training_data": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "mtg_set_surrogate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_float]),
     "mtg_surrogate_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "mtg_surrogate_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int]),
     "mtg_set_tea_farfield": (C.c_int, [C.c_void_p, C.c_int, C.c_float, C.c_int]),
     "mtg_tea_farfield_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong),
                                          C.POINTER(C.c_longlong)]),
@@ -538,6 +540,17 @@ class Surrogate:
                                            lr, seed, ptr(losses, C.c_float)))
         return losses
 
+    def set_wait_limit(self, polls: int = -1):
+        """Polls of the inference's bounded waits for the tensor cores (< 0: default)."""
+        check(self.lib.mtg_surrogate_set_wait_limit(self.h, polls))
+
+    def predict_raw(self, X):
+        """mtg_surrogate_predict returning (status, Y) instead of raising."""
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((len(X), SURROGATE_OUTPUTS), np.float32)
+        rc = self.lib.mtg_surrogate_predict(self.h, ptr(X, C.c_float), len(X), ptr(Y, C.c_float))
+        return rc, Y
+
     def predict(self, X):
         X = np.ascontiguousarray(X, np.float32)
         Y = np.zeros((len(X), SURROGATE_OUTPUTS), np.float32)
@@ -552,3 +565,90 @@ class Surrogate:
         check(self.lib.mtg_surrogate_loss_grad(self.h, ptr(X, C.c_float), ptr(T, C.c_float), len(X), C.byref(loss),
                                                ptr(g, C.c_float)))
         return loss.value, g
+
+
+def generate_seeds(rseed: int, nstreams: int) -> np.ndarray:
+    """HybridTaus states of nstreams streams from rseed (mtg_generate_seeds)."""
+    out = np.zeros(4 * nstreams, np.uint32)
+    check(load().mtg_generate_seeds(rseed, nstreams, ptr(out, C.c_uint32)))
+    return out
+
+
+def split_by_beads(offsets, nparts: int):
+    """Contiguous groups of trajectories with about equal bead counts: part k
+    ends at the first trajectory boundary at or past k/nparts of the beads.
+    Returns [(t0, t1)] covering every trajectory once (parts may be empty
+    when there are fewer trajectories than parts)."""
+    offsets = np.asarray(offsets, np.int64)
+    nt, nb = len(offsets) - 1, int(offsets[-1])
+    if nparts < 1:
+        raise ValueError("nparts must be positive")
+    cuts = [0]
+    for k in range(1, nparts):
+        t = int(np.searchsorted(offsets, k * nb / nparts, side="left"))
+        cuts.append(min(max(t, cuts[-1]), nt))
+    cuts.append(nt)
+    return [(cuts[k], cuts[k + 1]) for k in range(nparts)]
+
+
+class ShardedEngine:
+    """One batch over several GPUs, the replacement of the reference's MPI
+    replicas (src/main.cpp:27-48): trajectories never interact, so the batch
+    is cut into contiguous groups of about equal bead counts
+    (split_by_beads), each group runs on its own engine, device and stream,
+    and calls fan out to the engines (concurrently, one host thread each) and
+    gather their results in batch order.  No collective and no peer access.
+    The noise streams are the ones an engine of the whole batch would draw
+    (mtg_generate_seeds of the whole batch, sliced per group), so the result
+    equals that engine's bit for bit."""
+
+    def __init__(self, batch, devices):
+        import concurrent.futures as cf
+
+        from . import synth
+        self.batch = batch
+        parts = split_by_beads(batch.offsets, len(devices))
+        self.parts = [(t0, t1, d) for (t0, t1), d in zip(parts, devices) if t1 > t0]
+        self.nb, self.nt = batch.nbeads, batch.ntraj
+        self.engines = []
+        for t0, t1, d in self.parts:
+            sub = synth.sub_batch(batch, t0, t1)
+            sub.params.device = d
+            self.engines.append(Engine(sub))
+        self.ranges = [(int(batch.offsets[t0]), int(batch.offsets[t1])) for t0, t1, _ in self.parts]
+        seeds = generate_seeds(int(batch.params.rseed), 2 * self.nb).reshape(2, self.nb, 4)
+        for e, (b0, b1) in zip(self.engines, self.ranges):
+            e.upload_rng(np.ascontiguousarray(seeds[:, b0:b1]).reshape(-1))
+        self._pool = cf.ThreadPoolExecutor(max_workers=len(self.engines))
+
+    def _each(self, fn):
+        return list(self._pool.map(fn, range(len(self.engines))))
+
+    def upload_state(self, coords):
+        c = np.ascontiguousarray(coords, np.float32)
+        self._each(lambda k: self.engines[k].upload_state(c[self.ranges[k][0]:self.ranges[k][1]]))
+
+    def download_state(self):
+        return np.concatenate(self._each(lambda k: self.engines[k].download_state()))
+
+    def download_rng(self):
+        parts = self._each(lambda k: self.engines[k].download_rng().reshape(2, -1, 4))
+        return np.concatenate(parts, axis=1).reshape(-1)
+
+    def step(self, first_step: int, nsteps: int):
+        self._each(lambda k: self.engines[k].step(first_step, nsteps))
+
+    def energies(self):
+        return np.concatenate(self._each(lambda k: self.engines[k].energies()))
+
+    def close(self):
+        for e in self.engines:
+            e.close()
+        self.engines = []
+        self._pool.shutdown()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

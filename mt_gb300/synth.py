@@ -339,6 +339,20 @@ def batch_from_trajectories(params: MtgParams, trajs, fix: int = 1, max_h: int =
     return b
 
 
+def sub_batch(b: Batch, t0: int, t1: int) -> Batch:
+    """Trajectories t0 .. t1-1 of a batch as a batch of their own (a copy of
+    the parameters, offsets from 0, per-bead arrays sliced)."""
+    import copy
+    b0, b1 = int(b.offsets[t0]), int(b.offsets[t1])
+    sub = Batch(params=copy.copy(b.params), offsets=(b.offsets[t0:t1 + 1] - b0).astype(np.int32),
+                coords=b.coords[b0:b1].copy(), mon_type=b.mon_type[b0:b1].copy(), fixed=b.fixed[b0:b1].copy(),
+                extra=b.extra[b0:b1].copy(), gtp=b.gtp[b0:b1].copy(), on_tubule=b.on_tubule[b0:b1].copy(),
+                harmonic_count=b.harmonic_count[b0:b1].copy(),
+                harmonic=b.harmonic[b.max_h * b0:b.max_h * b1].copy(), zs=b.zs[t0:t1].copy(), max_h=b.max_h,
+                max_long=b.max_long, max_lat=b.max_lat, max_lj=b.max_lj, uniform_ntot=b.uniform_ntot)
+    return sub
+
+
 def uniform_batch(params: MtgParams, ntr: int, n_mon: int, n_free: int, seed: int = 0, **kw) -> Batch:
     """Ntr trajectories sharing one template topology, each with its own seeded
     free-tubulin placement (the template bead order is identical)."""

@@ -525,3 +525,23 @@ def test_persistent_rejects_large_trajectories(engine_mod):
     with pytest.raises(engine_mod.MtgError, match="2048"):
         e.set_tuning(t["list_method"], t["step_block"], t["tea_slices"], t["tea_jparts"], 1)
     e.close()
+
+
+def test_sharded_engine_equals_one_engine(engine_mod):
+    """A batch split over engines (here two on the same GPU, independent
+    streams, nothing shared) gives the result of one engine of the whole
+    batch bit for bit: states, noise streams and energy totals."""
+    from mt_gb300 import synth
+    p = synth.default_params(seed=71)
+    b = synth.ragged_batch(p, 6, seed=71, pf_range=(6, 16), free_range=(0, 200), cube=60.0, radius=8.12,
+                           psi_mode="make_mt", thermal=0.05)
+    one = make_engine(engine_mod, b)
+    one.step(0, 25)
+    with engine_mod.ShardedEngine(b, devices=[0, 0]) as sh:
+        assert len(sh.engines) == 2
+        sh.upload_state(b.coords)
+        sh.step(0, 25)
+        assert np.array_equal(sh.download_state(), one.download_state())
+        assert np.array_equal(sh.download_rng(), one.download_rng())
+        np.testing.assert_array_equal(sh.energies(), one.energies())
+    one.close()
