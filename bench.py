@@ -932,6 +932,67 @@ def run_stride(args, spec, dist):
             "async_over_sync": res["async"]["value"] / res["sync"]["value"]}
 
 
+# Small cases of the hot kernels for one-kernel ncu captures (`--profile-case`):
+# each builds its system, runs a few warm-up launches and then `launches`
+# launches of the kernel named, and prints one JSON line.  The command that
+# captures one launch of, e.g., k_ff_step:
+#   ncu --set full --clock-control none -k regex:k_ff_step -s 4 -c 1 -o prof \
+#       python bench.py --profile-case ff_step
+# Sizes are those of the workloads (one list period of steps, trajectories
+# cut to keep a case at a few hundred MB on the device).
+PROFILE_CASES = {
+    # 16 of the 64 x 5600 learned-workload trajectories; untrained network
+    # (the kernels' work does not depend on the weights), far field at the
+    # workload's theta, no re-check
+    "ff_step": dict(workload="tea_learned_vs_exact_64x5600", ntraj=16, steps=10),
+    "tea_step": dict(workload="tea_exact_64x5600", ntraj=16, steps=10),
+    "step_plain": dict(workload="ragged_1024", ntraj=None, steps=10),
+    "step_period": dict(workload="single_156", ntraj=None, steps=100),
+    # inference over the 16 x 5600 learned-workload beads, and one training
+    # epoch (backward kernel) on their samples
+    "mlp_infer": dict(workload="tea_learned_vs_exact_64x5600", ntraj=16, steps=6),
+    "mlp_backward": dict(workload="tea_learned_vs_exact_64x5600", ntraj=16, steps=1),
+}
+
+
+def run_profile_case(name: str):
+    c = PROFILE_CASES[name]
+    spec = dict(WORKLOADS[c["workload"]])
+    from mt_gb300 import build as mbuild
+    from mt_gb300 import engine as eng
+
+    mbuild.build()
+    b = make_batch(spec, 1, c["ntraj"])
+    out = {"profile_case": name, "workload": c["workload"], "trajectories": b.ntraj, "beads": b.nbeads}
+    with eng.Engine(b) as e:
+        e.upload_state(b.coords)
+        if name in ("ff_step", "mlp_infer", "mlp_backward"):
+            X, T = e.tea_training_data()
+            s = eng.Surrogate(seed=1)
+            if name == "mlp_backward":
+                s.train(X, T, epochs=c["steps"], batch=spec["batch"], lr=spec["lr"], seed=1)
+            elif name == "mlp_infer":
+                for _ in range(c["steps"]):
+                    s.predict(X)
+            else:
+                e.set_surrogate(s, recheck_every=0, max_err=1e9)
+                e.set_tea_farfield(True, spec["theta"], refresh_every=spec["ff_refresh"])
+                e.step(0, c["steps"])
+                out["farfield"] = e.tea_farfield_stats()
+            s.close()
+        elif name == "step_period":
+            e.set_tuning(2, 128, 8, 1, plain_persistent=1)
+            e.step(0, c["steps"])
+        else:
+            if name == "step_plain":
+                e.set_tuning(2, 256, 1, 1, plain_persistent=0)
+            else:   # whole j ranges: k_tea_step alone, no split tail
+                e.set_tuning(2, 128, 4, 1, plain_persistent=0)
+            e.step(0, c["steps"])
+        out["status"] = "ok"
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -944,7 +1005,12 @@ def main():
                     help="admissibility of the learned mode's far field (default: the workload's)")
     ap.add_argument("--no-suite", action="store_true",
                     help="default workload only, without the other configurations' sub-objects")
+    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES), default=None,
+                    help="run one small case of a hot kernel for an ncu capture and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args.profile_case)
+        return
     spec = WORKLOADS[args.workload]
     if args.ff_theta is not None:
         spec = dict(spec, theta=args.ff_theta)

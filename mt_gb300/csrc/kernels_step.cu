@@ -209,16 +209,19 @@ __device__ __forceinline__ Frame load_frame(const float4 *planes, int nb, int g)
 }
 
 // Euler-Maruyama update of one moving bead (integrate_kernel,
-// src/compute_cuda.cu:955-963): xyz from normals gx, angles from ga.  Not
-// inlined, for the reason given at make_frame.
-__device__ __noinline__ Frame em_update(const KParams &P, const Frame &Fi, const float f[6], float4 gx,
+// src/compute_cuda.cu:955-963): xyz from normals gx, angles from ga.
+// Explicitly rounded, like make_frame, so that every kernel gets the same bits.
+__device__ __forceinline__ float em_rn(float x, float k, float f, float v, float g) {
+    return __fadd_rn(x, __fadd_rn(__fmul_rn(k, f), __fmul_rn(v, g)));
+}
+__device__ __forceinline__ Frame em_update(const KParams &P, const Frame &Fi, const float f[6], float4 gx,
                                            float4 ga) {
-    const float x = Fi.p0.x + (P.kr * f[0] + P.varR * gx.x);
-    const float y = Fi.p0.y + (P.kr * f[1] + P.varR * gx.y);
-    const float z = Fi.p0.z + (P.kr * f[2] + P.varR * gx.z);
-    const float fi = Fi.p0.w + (P.kfi * f[3] + P.nfi * ga.x);
-    const float psi = Fi.p1.w + (P.kfi * f[5] + P.nfi * ga.y);
-    const float th = Fi.p2.w + (P.kth * f[4] + P.varTheta * ga.z);
+    const float x = em_rn(Fi.p0.x, P.kr, f[0], P.varR, gx.x);
+    const float y = em_rn(Fi.p0.y, P.kr, f[1], P.varR, gx.y);
+    const float z = em_rn(Fi.p0.z, P.kr, f[2], P.varR, gx.z);
+    const float fi = em_rn(Fi.p0.w, P.kfi, f[3], P.nfi, ga.x);
+    const float psi = em_rn(Fi.p1.w, P.kfi, f[5], P.nfi, ga.y);
+    const float th = em_rn(Fi.p2.w, P.kth, f[4], P.varTheta, ga.z);
     return make_frame(P, x, y, z, fi, th, psi);
 }
 

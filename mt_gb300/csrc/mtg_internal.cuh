@@ -136,26 +136,32 @@ struct Frame {
 
 __device__ __forceinline__ float3 f3(const float4 &v) { return make_float3(v.x, v.y, v.z); }
 
-// Builds the four planes of a bead from its state.  Not inlined: every
-// kernel of a translation unit then runs the same compiled arithmetic (the
-// per-step and the persistent plain step must agree bit for bit, and an
-// inlined copy could contract multiply-adds differently in each).
-static __device__ __noinline__ Frame make_frame(const KParams &P, float x, float y, float z, float fi,
-                                            float theta, float psi) {
+// Builds the four planes of a bead from its state.  Every product and sum
+// is an explicitly rounded intrinsic, so no multiply-add is contracted: the
+// result does not depend on the kernel this is inlined into (the per-step and
+// the persistent plain step agree bit for bit).
+__device__ __forceinline__ float dot3_rn(float a0, float b0, float a1, float b1, float a2, float b2) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
+}
+__device__ __forceinline__ Frame make_frame(const KParams &P, float x, float y, float z, float fi, float theta,
+                                            float psi) {
     float sf, cf, st, ct, sp, cp;
     sincosf(fi, &sf, &cf);
     sincosf(theta, &st, &ct);
     sincosf(psi, &sp, &cp);
-    const float m00 = cp * ct, m01 = cp * st * sf - sp * cf, m02 = cp * st * cf + sp * sf;
-    const float m10 = sp * ct, m11 = sp * st * sf + cp * cf, m12 = sp * st * cf - cp * sf;
-    const float m20 = -st, m21 = ct * sf, m22 = ct * cf;
+    const float cpst = __fmul_rn(cp, st), spst = __fmul_rn(sp, st);
+    const float m00 = __fmul_rn(cp, ct), m01 = __fsub_rn(__fmul_rn(cpst, sf), __fmul_rn(sp, cf)),
+                m02 = __fadd_rn(__fmul_rn(cpst, cf), __fmul_rn(sp, sf));
+    const float m10 = __fmul_rn(sp, ct), m11 = __fadd_rn(__fmul_rn(spst, sf), __fmul_rn(cp, cf)),
+                m12 = __fsub_rn(__fmul_rn(spst, cf), __fmul_rn(cp, sf));
+    const float m20 = -st, m21 = __fmul_rn(ct, sf), m22 = __fmul_rn(ct, cf);
     Frame F;
     F.p0 = make_float4(x, y, z, fi);
     F.p1 = make_float4(m02, m12, m22, psi);
-    F.p2 = make_float4(m00 * P.p1x + m01 * P.p1y + m02 * P.p1z, m10 * P.p1x + m11 * P.p1y + m12 * P.p1z,
-                       m20 * P.p1x + m21 * P.p1y + m22 * P.p1z, theta);
-    F.p3 = make_float4(m00 * P.p2x + m01 * P.p2y + m02 * P.p2z, m10 * P.p2x + m11 * P.p2y + m12 * P.p2z,
-                       m20 * P.p2x + m21 * P.p2y + m22 * P.p2z, 0.0f);
+    F.p2 = make_float4(dot3_rn(m00, P.p1x, m01, P.p1y, m02, P.p1z), dot3_rn(m10, P.p1x, m11, P.p1y, m12, P.p1z),
+                       dot3_rn(m20, P.p1x, m21, P.p1y, m22, P.p1z), theta);
+    F.p3 = make_float4(dot3_rn(m00, P.p2x, m01, P.p2y, m02, P.p2z), dot3_rn(m10, P.p2x, m11, P.p2y, m12, P.p2z),
+                       dot3_rn(m20, P.p2x, m21, P.p2y, m22, P.p2z), 0.0f);
     return F;
 }
 
