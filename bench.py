@@ -975,6 +975,7 @@ def run_profile_case(name: str):
                 for _ in range(c["steps"]):
                     s.predict(X)
             else:
+                e.set_tuning(2, 128, 4, 1, plain_persistent=0)
                 e.set_surrogate(s, recheck_every=0, max_err=1e9)
                 e.set_tea_farfield(True, spec["theta"], refresh_every=spec["ff_refresh"])
                 e.step(0, c["steps"])

@@ -389,12 +389,14 @@ int mtg_surrogate_status(mtg_engine *e, int *fell_back, int *rechecks, double *l
  * every step (src/bdhitea_kernel.cu:174-180) and declares, but does not
  * build, a listed variant (src/mt.h:118).  With on != 0, while the surrogate
  * is in charge (mtg_set_surrogate), each trajectory's non-extra beads are
- * grouped into leaves of at most 64 beads (a k-d bisection of the current
- * positions); pairs in leaves near each other are summed exactly as the
- * exact product does, and a leaf far from another (centres farther apart
- * than (r_I + r_J + 2 nm) / theta, r the leaves' radii) acts on it through 8
- * interpolation points per leaf (trilinear Chebyshev proxies of its bounding
- * box, recomputed every step), in place of its beads.  The exact re-check of
+ * arranged in a k-d tree (bisection of the current positions) with leaves of
+ * at most 32 beads; pairs in leaves near each other are summed exactly as
+ * the exact product does, and a node well separated from another (centres
+ * farther apart than (r_N + r_J + 2 nm) / theta' and spheres more than
+ * 4a + 2 nm apart, r the nodes' radii, theta' = theta for two leaves and
+ * 0.7 theta otherwise), at the coarsest level where it is, acts on it through
+ * 8 interpolation points per node (trilinear Chebyshev proxies of its
+ * bounding box, recomputed every step), in place of its beads.  The exact re-check of
  * the learned mode then compares this product (with the surrogate's C_i and
  * beta) against the exact one, and the fall-back to exact TEA covers both.
  * theta in (0, 1]: smaller is more accurate and slower.  refresh_every: the
@@ -404,12 +406,14 @@ int mtg_set_tea_farfield(mtg_engine *e, int on, float theta, int refresh_every);
 /* The grouping's leaves, the bead pairs summed exactly per step, and the
  * proxy pairs evaluated per step (zeros while off). */
 int mtg_tea_farfield_stats(mtg_engine *e, int *nleaves, long long *near_pairs, long long *proxy_pairs);
-/* The grouping: sizes[4] = leaves, beads in leaves, near entries, far
+/* The tree: sizes[5] = leaves, beads in leaves, near entries, nodes, far
  * entries; leaf_start [leaves+1] into leaf_bead (bead indices, leaf after
- * leaf); near_start / far_start [leaves+1] into near / far (leaf indices).
- * Call with NULL arrays for the sizes first. */
+ * leaf); near_start [leaves+1] into near (leaf indices); node_range
+ * [2*nodes] the begin and end of each node in leaf_bead (nodes 0 .. leaves-1
+ * are the leaves); node_parent [nodes] (-1 for a root); far_start [nodes+1]
+ * into far (node indices).  Call with NULL arrays for the sizes first. */
 int mtg_tea_farfield_layout(mtg_engine *e, int *sizes, int *leaf_start, int *leaf_bead, int *near_start,
-                            int *near, int *far_start, int *far);
+                            int *near, int *node_range, int *node_parent, int *far_start, int *far);
 /* Effective TEA forces f_i = F_i + C_i o R_i + sum_j T_ij (F_j + beta C_i o R_j)
  * (the x, y, z of [nbeads*4]) of the current state with the engine's current
  * C_i and beta, from one force evaluation and one draw of random forces:

@@ -757,16 +757,17 @@ void launch_tea_feff(const KParams &P, const DevBuffers &B, const int2 *work, in
 // (k = x, y, z); a bead adds A + sum_k beta C_ik B_k.  Far means the leaves'
 // centres are farther apart than (r_I + r_J + margin) / theta (tea_ff.cu).
 
-// Tile of kFFTileLeaves source leaves (kFFLeaf slots each), in the layout of
-// TeaTile; filled from FFBuffers::pack by asynchronous 16-byte copies.
-constexpr int kFFTileLeaves = 2;
-constexpr int kFFTile = kFFLeaf * kFFTileLeaves;
+// Tile of kFFTileLeaves source leaves (kFFPairSlots bead pairs each), in the
+// layout of FFBuffers::pack: the two lanes of a packed pair are two source
+// beads.  Filled from pack by asynchronous 16-byte copies.
+constexpr int kFFTileLeaves = 4;
+constexpr int kFFTileSlots = kFFPairSlots * kFFTileLeaves;
 struct FFTile {
-    float4 xy[kFFTile];
-    float4 zf[kFFTile];
-    float4 fyz[kFFTile];
-    float4 rxy[kFFTile];
-    float2 rz[kFFTile];
+    float4 xy[kFFTileSlots];   // xa xb ya yb
+    float4 zf[kFFTileSlots];   // za zb Fxa Fxb
+    float4 fyz[kFFTileSlots];  // Fya Fyb Fza Fzb
+    float4 rxy[kFFTileSlots];  // Rxa Rxb Rya Ryb
+    float2 rz[kFFTileSlots];   // Rza Rzb
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -781,9 +782,9 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // from global memory).
 constexpr int kFFNearSmem = 256;
 
-// Issues the copies of near-list entries e0, e0 + 1 (or the padding leaf past
-// e1; entries relative to the list's start) into tile T: each leaf is
-// kFFPackF4 contiguous float4 of pack.
+// Issues the copies of near-list entries e0 .. e0 + kFFTileLeaves - 1 (the
+// padding leaf past e1; entries relative to the list's start) into tile T:
+// each leaf is kFFPackF4 contiguous float4 of pack.
 __device__ __forceinline__ void ff_tile_issue(FFTile &T, const FFBuffers &F, const int *near, int e0, int e1) {
     constexpr int kPer = kFFPackF4;
     for (int c = threadIdx.x; c < kFFTileLeaves * kPer; c += blockDim.x) {
@@ -792,11 +793,11 @@ __device__ __forceinline__ void ff_tile_issue(FFTile &T, const FFBuffers &F, con
         const int J = e < e1 ? near[e] : F.nleaf;
         const float4 *src = F.pack + (size_t)J * kPer + w;
         float4 *dst;
-        if (w < 4 * kFFLeaf) {
-            const int a = w / kFFLeaf, k = q * kFFLeaf + w % kFFLeaf;
+        if (w < 4 * kFFPairSlots) {
+            const int a = w / kFFPairSlots, k = q * kFFPairSlots + w % kFFPairSlots;
             dst = a == 0 ? &T.xy[k] : a == 1 ? &T.zf[k] : a == 2 ? &T.fyz[k] : &T.rxy[k];
         } else {
-            dst = reinterpret_cast<float4 *>(&T.rz[q * kFFLeaf + 2 * (w - 4 * kFFLeaf)]);
+            dst = reinterpret_cast<float4 *>(&T.rz[q * kFFPairSlots + 2 * (w - 4 * kFFPairSlots)]);
         }
         cp_async16(dst, src);
     }
@@ -819,88 +820,182 @@ __device__ __forceinline__ float3 ff_proxy(float4 c, float4 h, int m) {
                        c.z + ((m & 4) ? kFFNode : -kFFNode) * h.z);
 }
 
-// P2M: one CTA of kFFLeaf threads per leaf, one bead per thread: the leaf's
-// bounding box, then the proxy charges Q_m = sum_j w_m(x_j) (F_j, R_j).
-__global__ void __launch_bounds__(kFFLeaf) k_ff_p2m(KParams P, DevBuffers B, FFBuffers F, const int *gate) {
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the 32 lanes of a warp of 32 values per lane, scattered: lane l
+// ends with the sum of value l (recursive halving: at offset o a lane keeps
+// the half of its values selected by bit o of its index and receives its
+// partner's partial sums of that half; 31 shuffles instead of 160).
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16, n = 32; o > 0; o >>= 1, n >>= 1) {
+        const bool up = lane & o;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            if (i >= n / 2) break;
+            const float send = up ? v[i] : v[i + n / 2];
+            const float keep = up ? v[i + n / 2] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0];
+}
+
+constexpr int kP2MWarps = 4;   // warps of a P2M block, one node each
+
+// Writes the 48 charge sums of a warp (acc[6m + v], summed per lane) as the
+// node's proxy charges: (QF.xyz, QR.x) at float4 16N + m, (QR.y, QR.z) at
+// 16N + 8 + m.
+__device__ __forceinline__ void ff_store_charges(const FFBuffers &F, int N, float (&acc)[48]) {
+    const int lane = threadIdx.x & 31;
+    float lo[32], hi[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) lo[i] = acc[i];
+#pragma unroll
+    for (int i = 0; i < 16; i++) hi[i] = acc[32 + i];
+#pragma unroll
+    for (int i = 16; i < 32; i++) hi[i] = 0.f;
+    const float s_lo = warp_reduce_scatter32(lo);   // value lane
+    const float s_hi = warp_reduce_scatter32(hi);   // value 32 + lane (lanes < 16)
+    float *q = reinterpret_cast<float *>(F.q);
+    auto put = [&](int idx, float val) {
+        const int m = idx / 6, c = idx % 6;
+        q[(size_t)4 * (16 * N + (c < 4 ? m : 8 + m)) + (c < 4 ? c : c - 4)] = val;
+    };
+    put(lane, s_lo);
+    if (lane < 16) put(32 + lane, s_hi);
+}
+
+// Writes the empty slot k of leaf N's pack (far away, zero F and R), or bead
+// values into it.
+__device__ __forceinline__ void ff_pack_slot(const FFBuffers &F, int N, int k, float3 x, float4 Fv, float4 R) {
+    float *pk = reinterpret_cast<float *>(F.pack + (size_t)N * kFFPackF4);
+    const int p = k >> 1, h = k & 1;
+    pk[4 * p + h] = x.x;
+    pk[4 * p + 2 + h] = x.y;
+    pk[4 * (kFFPairSlots + p) + h] = x.z;
+    pk[4 * (kFFPairSlots + p) + 2 + h] = Fv.x;
+    pk[4 * (2 * kFFPairSlots + p) + h] = Fv.y;
+    pk[4 * (2 * kFFPairSlots + p) + 2 + h] = Fv.z;
+    pk[4 * (3 * kFFPairSlots + p) + h] = R.x;
+    pk[4 * (3 * kFFPairSlots + p) + 2 + h] = R.y;
+    pk[4 * 4 * kFFPairSlots + 2 * p + h] = R.z;
+}
+
+// P2M of the leaves, one warp per leaf (lane k: bead k): the bounding box,
+// the proxy charges Q_m = sum_j w_m(x_j) (F_j, R_j), and the leaf's beads in
+// the step kernel's tile layout (leaf nleaf: the padding leaf's pack).
+__global__ void __launch_bounds__(32 * kP2MWarps) k_ff_p2m(KParams P, DevBuffers B, FFBuffers F, const int *gate) {
     if (gate && *gate != 0) return;
-    const int L = blockIdx.x, t = threadIdx.x;
-    const int s = L < F.nleaf ? F.leaf_start[L] : 0, n = L < F.nleaf ? F.leaf_start[L + 1] - s : 0;
-    __shared__ float sw[kFFLeaf][9];
-    __shared__ float sv[kFFLeaf][7];
-    __shared__ float3 slo[kFFLeaf / 32], shi[kFFLeaf / 32];
-    float3 x = make_float3(0.f, 0.f, 0.f), lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f);
-    float3 hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-    float4 Fv = make_float4(0.f, 0.f, 0.f, 0.f), R = Fv;
-    if (t < n) {
-        const int g = F.leaf_bead[s + t];
+    const int N = blockIdx.x * kP2MWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (N > F.nleaf) return;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float3 away = make_float3(kFarAway, kFarAway, kFarAway);
+    if (N == F.nleaf) {
+        ff_pack_slot(F, N, lane, away, zero, zero);
+        return;
+    }
+    const int b0 = F.leaf_start[N], n = F.leaf_start[N + 1] - b0;
+    float3 x = make_float3(0.f, 0.f, 0.f);
+    float4 Fv = zero, R = zero;
+    if (lane < n) {
+        const int g = F.leaf_bead[b0 + lane];
         x = f3(B.frame_in[g]);
         Fv = B.force[g];
         R = B.tea_r[g];
-        lo = hi = x;
     }
-    {   // the leaf's beads in the step kernel's tile layout (block nleaf: the padding leaf)
-        float4 *pk = F.pack + (size_t)L * kFFPackF4;
-        const float3 px = t < n ? x : make_float3(kFarAway, kFarAway, kFarAway);
-        pk[t] = make_float4(px.x, px.x, px.y, px.y);
-        pk[kFFLeaf + t] = make_float4(px.z, px.z, Fv.x, Fv.x);
-        pk[2 * kFFLeaf + t] = make_float4(Fv.y, Fv.y, Fv.z, Fv.z);
-        pk[3 * kFFLeaf + t] = make_float4(R.x, R.x, R.y, R.y);
-        reinterpret_cast<float2 *>(pk + 4 * kFFLeaf)[t] = f2(R.z);
-    }
-    if (L >= F.nleaf) return;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
-        lo.y = fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o));
-        lo.z = fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o));
-        hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
-        hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
-        hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
-    }
-    if ((t & 31) == 0) {
-        slo[t >> 5] = lo;
-        shi[t >> 5] = hi;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < kFFLeaf / 32; k++) {
-        lo = make_float3(fminf(lo.x, slo[k].x), fminf(lo.y, slo[k].y), fminf(lo.z, slo[k].z));
-        hi = make_float3(fmaxf(hi.x, shi[k].x), fmaxf(hi.y, shi[k].y), fmaxf(hi.z, shi[k].z));
-    }
+    const float3 lo = make_float3(warp_min(lane < n ? x.x : 3.4e38f), warp_min(lane < n ? x.y : 3.4e38f),
+                                  warp_min(lane < n ? x.z : 3.4e38f));
+    const float3 hi = make_float3(warp_max(lane < n ? x.x : -3.4e38f), warp_max(lane < n ? x.y : -3.4e38f),
+                                  warp_max(lane < n ? x.z : -3.4e38f));
     const float4 c = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.f);
     const float4 h = make_float4(fmaxf(0.5f * (hi.x - lo.x), 1e-3f), fmaxf(0.5f * (hi.y - lo.y), 1e-3f),
                                  fmaxf(0.5f * (hi.z - lo.z), 1e-3f), 0.f);
+    ff_pack_slot(F, N, lane, lane < n ? x : away, Fv, R);
     float w[8];
     ff_weights(x, c, h, w);
+    const float val[6] = {Fv.x, Fv.y, Fv.z, R.x, R.y, R.z};
+    float acc[48];
 #pragma unroll
-    for (int m = 0; m < 8; m++) sw[t][m] = t < n ? w[m] : 0.f;
-    sv[t][0] = Fv.x;
-    sv[t][1] = Fv.y;
-    sv[t][2] = Fv.z;
-    sv[t][3] = R.x;
-    sv[t][4] = R.y;
-    sv[t][5] = R.z;
-    __syncthreads();
-    if (t < 48) {
-        const int m = t / 6, v = t % 6;
-        float acc = 0.f;
-        for (int j = 0; j < n; j++) acc = fmaf(sw[j][m], sv[j][v], acc);
-        // (QF.xyz, QR.x) at float4 16L + m, (QR.y, QR.z) at 16L + 8 + m
-        float *q = reinterpret_cast<float *>(F.q);
-        q[(size_t)4 * (16 * L + (v < 4 ? m : 8 + m)) + (v < 4 ? v : v - 4)] = acc;
-    }
-    if (t == 0) {
-        F.box[2 * L] = c;
-        F.box[2 * L + 1] = h;
+    for (int m = 0; m < 8; m++)
+#pragma unroll
+        for (int v = 0; v < 6; v++) acc[6 * m + v] = lane < n ? w[m] * val[v] : 0.f;
+    ff_store_charges(F, N, acc);
+    if (lane == 0) {
+        F.box[2 * N] = c;
+        F.box[2 * N + 1] = h;
     }
 }
 
-// M2L: one CTA of 128 threads per target leaf; thread t serves the target
-// proxies t % 4 and t % 4 + 4 (the same x and y, opposite z) as one packed
-// pair over every 32nd far leaf, and the 32 slices meet in shared memory.
-__global__ void __launch_bounds__(128) k_ff_m2l(KParams P, FFBuffers F, const int *gate) {
+// P2M of the inner nodes, one warp per node, from the node's leaves: the
+// bounding box is the union of theirs, and since trilinear interpolation on
+// a leaf's proxies reproduces every trilinear function, the node's weights
+// at the leaf proxies carry the leaf charges over exactly:
+// Q^N_m = sum_leaves sum_k w^N_m(y_k) Q^leaf_k.
+__global__ void __launch_bounds__(32 * kP2MWarps) k_ff_p2m_inner(KParams P, FFBuffers F, const int *gate) {
     if (gate && *gate != 0) return;
-    const int L = blockIdx.x, t = threadIdx.x, np = t & 3, sl = t >> 2;
+    const int k = blockIdx.x * kP2MWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (k >= F.ninner) return;
+    const int N = F.inner[k];
+    const int l0 = F.node_leaves[2 * N], l1 = F.node_leaves[2 * N + 1];
+    float3 lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+    for (int l = l0 + lane; l < l1; l += 32) {
+        const float4 c = F.box[2 * l], h = F.box[2 * l + 1];
+        lo = make_float3(fminf(lo.x, c.x - h.x), fminf(lo.y, c.y - h.y), fminf(lo.z, c.z - h.z));
+        hi = make_float3(fmaxf(hi.x, c.x + h.x), fmaxf(hi.y, c.y + h.y), fmaxf(hi.z, c.z + h.z));
+    }
+    lo = make_float3(warp_min(lo.x), warp_min(lo.y), warp_min(lo.z));
+    hi = make_float3(warp_max(hi.x), warp_max(hi.y), warp_max(hi.z));
+    const float4 c = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.f);
+    const float4 h = make_float4(fmaxf(0.5f * (hi.x - lo.x), 1e-3f), fmaxf(0.5f * (hi.y - lo.y), 1e-3f),
+                                 fmaxf(0.5f * (hi.z - lo.z), 1e-3f), 0.f);
+    float acc[48];
+#pragma unroll
+    for (int i = 0; i < 48; i++) acc[i] = 0.f;
+    // lane t takes proxy t % 8 of every fourth leaf
+    for (int e = l0 * 8 + lane; e < l1 * 8; e += 32) {
+        const int l = e >> 3, m = e & 7;
+        const float3 y = ff_proxy(F.box[2 * l], F.box[2 * l + 1], m);
+        const float4 qa = F.q[16 * l + m], qb = F.q[16 * l + 8 + m];
+        const float val[6] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y};
+        float w[8];
+        ff_weights(y, c, h, w);
+#pragma unroll
+        for (int mm = 0; mm < 8; mm++)
+#pragma unroll
+            for (int v = 0; v < 6; v++) acc[6 * mm + v] = fmaf(w[mm], val[v], acc[6 * mm + v]);
+    }
+    ff_store_charges(F, N, acc);
+    if (lane == 0) {
+        F.box[2 * N] = c;
+        F.box[2 * N + 1] = h;
+    }
+}
+
+// M2L: one warp per target node; lane t serves the target proxies t % 4 and
+// t % 4 + 4 (the same x and y, opposite z) as one packed pair over every 8th
+// far node, and the 8 slices meet by shuffles in a fixed order.
+constexpr int kM2LWarps = 4;
+__global__ void __launch_bounds__(32 * kM2LWarps) k_ff_m2l(KParams P, FFBuffers F, const int *gate) {
+    if (gate && *gate != 0) return;
+    const int wk = blockIdx.x * kM2LWarps + (threadIdx.x >> 5);
+    if (wk >= F.ntgt) return;
+    const int L = F.tgt[wk], t = threadIdx.x & 31, np = t & 3, sl = t >> 2;
     const TeaConst K = tea_const(P.tea_a);
     const float4 cL = F.box[2 * L], hL = F.box[2 * L + 1];
     const float3 x0 = ff_proxy(cL, hL, np), x1 = ff_proxy(cL, hL, np + 4);
@@ -909,7 +1004,7 @@ __global__ void __launch_bounds__(128) k_ff_m2l(KParams P, FFBuffers F, const in
     float2 acc[12];
 #pragma unroll
     for (int c = 0; c < 12; c++) acc[c] = f2(0.f);
-    for (int k = F.far_start[L] + sl; k < F.far_start[L + 1]; k += 32) {
+    for (int k = F.far_start[L] + sl; k < F.far_start[L + 1]; k += 8) {
         const int J = F.far[k];
         const float4 cJ = F.box[2 * J], hJ = F.box[2 * J + 1];
 #pragma unroll 2
@@ -941,127 +1036,101 @@ __global__ void __launch_bounds__(128) k_ff_m2l(KParams P, FFBuffers F, const in
             acc[11] = __ffma2_rn(cii, rz, __ffma2_rn(s2, dz, acc[11]));
         }
     }
-    // red[slice][proxy][component]
-    __shared__ float red[32][8][13];
 #pragma unroll
-    for (int c = 0; c < 12; c++) {
-        red[sl][np][c] = acc[c].x;
-        red[sl][np + 4][c] = acc[c].y;
-    }
-    __syncthreads();
-    if (t < 96) {
-        const int pn = t / 12, c = t % 12;
-        float v = 0.f;
-#pragma unroll 8
-        for (int k = 0; k < 32; k++) v += red[k][pn][c];
-        reinterpret_cast<float *>(F.phi)[(size_t)96 * L + 12 * pn + c] = v;
+    for (int o = 4; o < 32; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < 12; c++) {
+            acc[c].x += __shfl_xor_sync(0xffffffffu, acc[c].x, o);
+            acc[c].y += __shfl_xor_sync(0xffffffffu, acc[c].y, o);
+        }
+    if (sl == 0) {
+        float *phi = reinterpret_cast<float *>(F.phi) + (size_t)96 * L;
+#pragma unroll
+        for (int c = 0; c < 12; c++) {
+            phi[12 * np + c] = acc[c].x;
+            phi[12 * (np + 4) + c] = acc[c].y;
+        }
     }
 }
 
-// Beads i per thread in the far-field step: one packed pair, the 32 lanes of
-// a slice (one warp) spread over the leaf (lane il serves il and il + 32), so
-// that every tile load of a warp is one broadcast.
-constexpr int kFFPairs = 1;
-constexpr int kFFLanes = kFFLeaf / (2 * kFFPairs);
-
-// The packed pass of one tile (self pairs pushed to r^2 = 1e30 when SELF),
-// with TRACK the running minimum of r^2 per packed pair and segment.
+// The packed pass of one tile: the target bead (position -n, weight cb) against
+// the tile's bead pairs; with SELF the target's own slot (pair self_p, lane
+// self_h) is pushed to r^2 = 1e30, with TRACK the running minimum of r^2 per
+// segment of the thread's pairs is kept.
 template <int SLICES, bool SELF, bool TRACK>
-__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_t, const float2 (&nx)[kFFPairs],
-                                             const float2 (&ny)[kFFPairs], const float2 (&nz)[kFFPairs],
-                                             const float2 (&cbx)[kFFPairs], const float2 (&cby)[kFFPairs],
-                                             const float2 (&cbz)[kFFPairs], float2 vkap, float2 vn2a2,
-                                             float2 one, float2 (&ax)[kFFPairs], float2 (&ay)[kFFPairs],
-                                             float2 (&az)[kFFPairs], float (&rmin)[kFFPairs][kTeaSeg]) {
-    constexpr int kLen = kFFTile / SLICES / kTeaSeg;
+__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_p, int self_h, float2 nx, float2 ny,
+                                             float2 nz, float2 cbx, float2 cby, float2 cbz, float2 vkap,
+                                             float2 vn2a2, float2 one, float2 &ax, float2 &ay, float2 &az,
+                                             float (&rmin)[kTeaSeg]) {
+    constexpr int kLen = kFFTileSlots / SLICES / kTeaSeg;
 #pragma unroll
     for (int sg = 0; sg < kTeaSeg; sg++) {
-#pragma unroll(kLen <= 4 ? kLen : 2)
+#pragma unroll(kLen <= 4 ? kLen : 4)
         for (int k = 0; k < kLen; k++) {
             const int t = sl + (sg * kLen + k) * SLICES;
             const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
-            const float2 xj = lo2(a), yj = hi2(a), zj = lo2(b);
-            const float2 fxj = hi2(b), fyj = lo2(c), fzj = hi2(c);
-            const float2 rxj = lo2(d), ryj = hi2(d), rzj = T.rz[t];
-#pragma unroll
-            for (int p = 0; p < kFFPairs; p++) {
-                const float2 dx = __fadd2_rn(xj, nx[p]), dy = __fadd2_rn(yj, ny[p]), dz = __fadd2_rn(zj, nz[p]);
-                const float2 gx = __ffma2_rn(rxj, cbx[p], fxj), gy = __ffma2_rn(ryj, cby[p], fyj),
-                             gz = __ffma2_rn(rzj, cbz[p], fzj);
-                float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-                if (SELF) {
-                    if (t == self_t + kFFLanes * 2 * p) r2.x = 1e30f;
-                    if (t == self_t + kFFLanes * (2 * p + 1)) r2.y = 1e30f;
-                }
-                if (TRACK) rmin[p][sg] = fmin3(rmin[p][sg], r2.x, r2.y);
-                const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-                const float2 q = __fmul2_rn(rinv, rinv);
-                const float2 tq = __fmul2_rn(q, rinv);
-                const float2 cii = __ffma2_rn(vkap, tq, rinv);
-                const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
-                const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
-                ax[p] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax[p]));
-                ay[p] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay[p]));
-                az[p] = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az[p]));
+            const float2 dx = __fadd2_rn(lo2(a), nx), dy = __fadd2_rn(hi2(a), ny), dz = __fadd2_rn(lo2(b), nz);
+            const float2 gx = __ffma2_rn(lo2(d), cbx, hi2(b)), gy = __ffma2_rn(hi2(d), cby, lo2(c)),
+                         gz = __ffma2_rn(T.rz[t], cbz, hi2(c));
+            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            if (SELF && t == self_p) {
+                if (self_h)
+                    r2.y = 1e30f;
+                else
+                    r2.x = 1e30f;
             }
+            if (TRACK) rmin[sg] = fmin3(rmin[sg], r2.x, r2.y);
+            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+            const float2 q = __fmul2_rn(rinv, rinv);
+            const float2 tq = __fmul2_rn(q, rinv);
+            const float2 cii = __ffma2_rn(vkap, tq, rinv);
+            const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
+            const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
+            ax = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax));
+            ay = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay));
+            az = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az));
         }
     }
 }
 
-// Near pairs, far field and update: one CTA of kFFLanes x SLICES threads per
-// target leaf; lane il serves the leaf's beads il + kFFLanes h as packed
-// pairs, the SLICES threads of a lane take interleaved beads of every tile of
-// near leaves (two leaves per tile, copied asynchronously one tile ahead).
-// Overlapping pairs (r <= 2a) get the near formula: with LISTCORR by walking
-// the bead's LJ list once, otherwise by rescanning the tile segments whose
-// running minimum of r^2 flags one, as in k_tea_step.  Then the far field is
-// interpolated from the leaf's proxies and the bead moves (FEFF: its
-// effective force goes to feff instead).
+// Near pairs, far field and update: one CTA of 32 x SLICES threads per
+// target leaf; lane il serves the leaf's bead il, the SLICES warps take
+// interleaved bead pairs of every tile of near leaves (kFFTileLeaves leaves
+// per tile, copied asynchronously one tile ahead), the two lanes of each
+// packed operation being two source beads.  Overlapping pairs (r <= 2a) get
+// the near formula: with LISTCORR by walking the bead's LJ list once,
+// otherwise by rescanning the tile segments whose running minimum of r^2
+// flags one, as in k_tea_step.  Then the far field of the leaf and of each
+// ancestor with a far list is interpolated from that node's proxies and the
+// bead moves (FEFF: its effective force goes to feff instead).
 template <int SLICES, bool FEFF, bool LISTCORR>
-__global__ void __launch_bounds__(kFFLanes *SLICES, 20 / SLICES) k_ff_step(KParams P, DevBuffers B, FFBuffers F, float4 *feff,
-                                                              const int *gate) {
+__global__ void __launch_bounds__(32 * SLICES, 20 / SLICES) k_ff_step(KParams P, DevBuffers B, FFBuffers F,
+                                                                    float4 *feff, const int *gate) {
     if (gate && *gate != 0) return;
-    constexpr int kNI = 2 * kFFPairs;
     const int L = blockIdx.x;
-    const int il = threadIdx.x % kFFLanes, sl = threadIdx.x / kFFLanes;
+    const int il = threadIdx.x & 31, sl = threadIdx.x >> 5;
     const int s0 = F.leaf_start[L], n = F.leaf_start[L + 1] - s0;
     const int traj = F.leaf_traj[L];
     __shared__ FFTile T2[2];
-    __shared__ float4 s_red[kNI * kFFLanes * SLICES];
-    __shared__ float4 s_phi[24];
+    __shared__ float4 s_red[SLICES * 32];
+    __shared__ float4 s_far[kFFMaxAnc * 26];   // per ancestor: box (2), potentials (24)
+    __shared__ int s_near[kFFNearSmem];
     const float beta = B.tea_beta[traj], b2 = beta * beta;
-    // per packed pair p of beads i (2p, 2p+1): -position, beta C_i, sums
-    float2 nx[kFFPairs], ny[kFFPairs], nz[kFFPairs], cbx[kFFPairs], cby[kFFPairs], cbz[kFFPairs];
-    float2 ax[kFFPairs], ay[kFFPairs], az[kFFPairs];
-#pragma unroll
-    for (int h = 0; h < kNI; h++) {
-        const int k = il + h * kFFLanes;
-        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), cb = pi;
-        if (k < n) {
-            const int g = F.leaf_bead[s0 + k];
-            pi = B.frame_in[g];
-            const float4 ci = B.tea_ci[g];
-            cb = make_float4(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
-                             beta / sqrtf(1.0f + b2 * ci.z), 0.f);
-        }
-        float2 *v[6] = {&nx[h >> 1], &ny[h >> 1], &nz[h >> 1], &cbx[h >> 1], &cby[h >> 1], &cbz[h >> 1]};
-        const float val[6] = {-pi.x, -pi.y, -pi.z, cb.x, cb.y, cb.z};
-#pragma unroll
-        for (int c = 0; c < 6; c++) {
-            if (h & 1)
-                v[c]->y = val[c];
-            else
-                v[c]->x = val[c];
-        }
+    const int g = il < n ? F.leaf_bead[s0 + il] : -1;
+    float3 xi = make_float3(0.f, 0.f, 0.f), cbi = make_float3(0.f, 0.f, 0.f);
+    if (g >= 0) {
+        xi = f3(B.frame_in[g]);
+        const float4 ci = B.tea_ci[g];
+        cbi = make_float3(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
+                          beta / sqrtf(1.0f + b2 * ci.z));
     }
-#pragma unroll
-    for (int p = 0; p < kFFPairs; p++) ax[p] = ay[p] = az[p] = f2(0.f);
+    const float2 nx = f2(-xi.x), ny = f2(-xi.y), nz = f2(-xi.z), cbx = f2(cbi.x), cby = f2(cbi.y), cbz = f2(cbi.z);
+    float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f);
     const TeaConst K = tea_const(P.tea_a);
     const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
     // near leaves in tiles of kFFTileLeaves, double-buffered: the copies of
     // tile k + 1 are in flight while tile k is summed
     const int e_beg = F.near_start[L], nnear = F.near_start[L + 1] - e_beg;
-    __shared__ int s_near[kFFNearSmem];
     const int *near = F.near + e_beg;
     if (nnear <= kFFNearSmem) {
         for (int k = threadIdx.x; k < nnear; k += blockDim.x) s_near[k] = near[k];
@@ -1083,29 +1152,22 @@ __global__ void __launch_bounds__(kFFLanes *SLICES, 20 / SLICES) k_ff_step(KPara
             const int e = it * kFFTileLeaves + q;
             if (e < nnear && near[e] == L) self_q = q;
         }
-        float rmin[kFFPairs][kTeaSeg];
+        float rmin[kTeaSeg];
 #pragma unroll
-        for (int p = 0; p < kFFPairs; p++)
-#pragma unroll
-            for (int sg = 0; sg < kTeaSeg; sg++) rmin[p][sg] = 3.4e38f;
+        for (int sg = 0; sg < kTeaSeg; sg++) rmin[sg] = 3.4e38f;
         const bool self = self_q >= 0;
-        const int self_t = il + self_q * kFFLeaf;
+        const int self_p = self_q * kFFPairSlots + (il >> 1), self_h = il & 1;
         if (self)
-            ff_step_tile<SLICES, true, !LISTCORR>(T, sl, self_t, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay,
-                                                  az, rmin);
+            ff_step_tile<SLICES, true, !LISTCORR>(T, sl, self_p, self_h, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one,
+                                                  ax, ay, az, rmin);
         else
-            ff_step_tile<SLICES, false, !LISTCORR>(T, sl, self_t, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one, ax, ay,
-                                                   az, rmin);
-        if (LISTCORR) {   // overlapping pairs are corrected from the pair list below
-            __syncthreads();
-            continue;
-        }
-        constexpr int kLen = kFFTile / SLICES / kTeaSeg;
-#pragma unroll
-        for (int p = 0; p < kFFPairs; p++) {
+            ff_step_tile<SLICES, false, !LISTCORR>(T, sl, self_p, self_h, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2,
+                                                   one, ax, ay, az, rmin);
+        if (!LISTCORR) {
+            constexpr int kLen = kFFTileSlots / SLICES / kTeaSeg;
             unsigned segs = 0;
 #pragma unroll
-            for (int sg = 0; sg < kTeaSeg; sg++) segs |= (rmin[p][sg] <= K.four_a2 ? 1u : 0u) << sg;
+            for (int sg = 0; sg < kTeaSeg; sg++) segs |= (rmin[sg] <= K.four_a2 ? 1u : 0u) << sg;
             while (segs) {  // the segments that hold an overlapping pair
                 const int sg = __ffs(segs) - 1;
                 segs &= segs - 1;
@@ -1113,108 +1175,73 @@ __global__ void __launch_bounds__(kFFLanes *SLICES, 20 / SLICES) k_ff_step(KPara
                     const int t = sl + (sg * kLen + k) * SLICES;
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
-                        if (self && t == self_t + kFFLanes * (2 * p + h)) continue;
-                        const float dx = T.xy[t].x + (h ? nx[p].y : nx[p].x), dy = T.xy[t].z + (h ? ny[p].y : ny[p].x),
-                                    dz = T.zf[t].x + (h ? nz[p].y : nz[p].x);
+                        if (self && t == self_p && h == self_h) continue;
+                        const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
+                        const float dx = (h ? a.y : a.x) - xi.x, dy = (h ? a.w : a.z) - xi.y,
+                                    dz = (h ? b.y : b.x) - xi.z;
                         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                         if (!(r2 <= K.four_a2)) continue;
-                        const float gx = fmaf(T.rxy[t].x, h ? cbx[p].y : cbx[p].x, T.zf[t].z),
-                                    gy = fmaf(T.rxy[t].z, h ? cby[p].y : cby[p].x, T.fyz[t].x),
-                                    gz = fmaf(T.rz[t].x, h ? cbz[p].y : cbz[p].x, T.fyz[t].z);
+                        const float2 rz = T.rz[t];
+                        const float gx = fmaf(h ? d.y : d.x, cbi.x, h ? b.w : b.z),
+                                    gy = fmaf(h ? d.w : d.z, cbi.y, h ? c.y : c.x),
+                                    gz = fmaf(h ? rz.y : rz.x, cbi.z, h ? c.w : c.z);
                         const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
                         const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
-                        if (h) {
-                            ax[p].y += nr.x - fa.x;
-                            ay[p].y += nr.y - fa.y;
-                            az[p].y += nr.z - fa.z;
-                        } else {
-                            ax[p].x += nr.x - fa.x;
-                            ay[p].x += nr.y - fa.y;
-                            az[p].x += nr.z - fa.z;
-                        }
+                        ax.x += nr.x - fa.x;
+                        ay.x += nr.y - fa.y;
+                        az.x += nr.z - fa.z;
                     }
                 }
             }
         }
         __syncthreads();
     }
-    if (LISTCORR) {
+    float3 sum = make_float3(ax.x + ax.y, ay.x + ay.y, az.x + az.y);
+    if (LISTCORR && g >= 0) {
         // overlapping pairs (r <= 2a): every one is within the LJ list cutoff
         // (checked by the launcher), so the far-field term of the tile pass is
         // replaced by the near one while walking the bead's list; the SLICES
         // threads of a bead take interleaved entries
         const int base = B.off[traj], nb = P.nb;
-#pragma unroll
-        for (int h = 0; h < kNI; h++) {
-            const int k = il + h * kFFLanes;
-            if (k >= n) continue;
-            const int g = F.leaf_bead[s0 + k];
-            const int p = h >> 1;
-            const bool hi = h & 1;
-            const float mx = hi ? nx[p].y : nx[p].x, my = hi ? ny[p].y : ny[p].x, mz = hi ? nz[p].y : nz[p].x;
-            const float bx = hi ? cbx[p].y : cbx[p].x, by = hi ? cby[p].y : cby[p].x, bz = hi ? cbz[p].y : cbz[p].x;
-            float3 corr = make_float3(0.f, 0.f, 0.f);
-            const int cnt = B.ljc[g];
-            for (int q = sl; q < cnt; q += SLICES) {
-                const int pj = base + B.lj[q * nb + g];
-                const float4 xj = B.frame_in[pj];
-                const float dx = xj.x + mx, dy = xj.y + my, dz = xj.z + mz;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                if (!(r2 <= K.four_a2) || (B.flags[pj] & kFlagExtra)) continue;
-                const float4 Fj = B.force[pj], Rj = B.tea_r[pj];
-                const float gx = fmaf(Rj.x, bx, Fj.x), gy = fmaf(Rj.y, by, Fj.y), gz = fmaf(Rj.z, bz, Fj.z);
-                const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
-                const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
-                corr.x += nr.x - fa.x;
-                corr.y += nr.y - fa.y;
-                corr.z += nr.z - fa.z;
-            }
-            if (hi) {
-                ax[p].y += corr.x;
-                ay[p].y += corr.y;
-                az[p].y += corr.z;
-            } else {
-                ax[p].x += corr.x;
-                ay[p].x += corr.y;
-                az[p].x += corr.z;
-            }
+        const int cnt = B.ljc[g];
+        for (int q = sl; q < cnt; q += SLICES) {
+            const int pj = base + B.lj[q * nb + g];
+            const float4 xj = B.frame_in[pj];
+            const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (!(r2 <= K.four_a2) || (B.flags[pj] & kFlagExtra)) continue;
+            const float4 Fj = B.force[pj], Rj = B.tea_r[pj];
+            const float gx = fmaf(Rj.x, cbi.x, Fj.x), gy = fmaf(Rj.y, cbi.y, Fj.y), gz = fmaf(Rj.z, cbi.z, Fj.z);
+            const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+            const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
+            sum.x += nr.x - fa.x;
+            sum.y += nr.y - fa.y;
+            sum.z += nr.z - fa.z;
         }
     }
-#pragma unroll
-    for (int h = 0; h < kNI; h++) {
-        const int p = h >> 1;
-        const bool hi = h & 1;
-        s_red[(sl * kNI + h) * kFFLanes + il] =
-            make_float4(hi ? ax[p].y : ax[p].x, hi ? ay[p].y : ay[p].x, hi ? az[p].y : az[p].x, 0.f);
+    s_red[sl * 32 + il] = make_float4(sum.x, sum.y, sum.z, 0.f);
+    // the far fields of the leaf and its ancestors: boxes and potentials
+    const int a0 = F.anc_start[L], na = min(F.anc_start[L + 1] - a0, kFFMaxAnc);
+    for (int k = threadIdx.x; k < 26 * na; k += blockDim.x) {
+        const int N = F.anc[a0 + k / 26], w = k % 26;
+        s_far[k] = w < 2 ? F.box[2 * N + w] : F.phi[24 * N + w - 2];
     }
-    if (threadIdx.x < 24) s_phi[threadIdx.x] = F.phi[24 * L + threadIdx.x];
     __syncthreads();
-    if (sl != 0) return;
-    const float4 c = F.box[2 * L], hb = F.box[2 * L + 1];
-#pragma unroll
-    for (int h = 0; h < kNI; h++) {
-        const int k = il + h * kFFLanes;
-        if (k >= n) continue;
-        const int g = F.leaf_bead[s0 + k];
-        const int p = h >> 1;
-        const bool hi = h & 1;
-        const float3 xi = make_float3(-(hi ? nx[p].y : nx[p].x), -(hi ? ny[p].y : ny[p].x),
-                                      -(hi ? nz[p].y : nz[p].x));
-        const float3 cbi = make_float3(hi ? cbx[p].y : cbx[p].x, hi ? cby[p].y : cby[p].x,
-                                       hi ? cbz[p].y : cbz[p].x);
-        float sx = 0.f, sy = 0.f, sz = 0.f;
-        for (int k = 0; k < SLICES; k++) {
-            const float4 v = s_red[(k * kNI + h) * kFFLanes + il];
-            sx += v.x;
-            sy += v.y;
-            sz += v.z;
-        }
-        // far field interpolated from the leaf's 8 proxies (L2P)
+    if (sl != 0 || g < 0) return;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int k = 0; k < SLICES; k++) {
+        const float4 v = s_red[k * 32 + il];
+        sx += v.x;
+        sy += v.y;
+        sz += v.z;
+    }
+    for (int A = 0; A < na; A++) {   // L2P
+        const float4 *fr = s_far + 26 * A;
         float w[8];
-        ff_weights(xi, c, hb, w);
+        ff_weights(xi, fr[0], fr[1], w);
 #pragma unroll
         for (int m = 0; m < 8; m++) {
-            const float4 p0 = s_phi[3 * m], p1 = s_phi[3 * m + 1], p2 = s_phi[3 * m + 2];
+            const float4 p0 = fr[2 + 3 * m], p1 = fr[3 + 3 * m], p2 = fr[4 + 3 * m];
             // A + beta C_x B_x + beta C_y B_y + beta C_z B_z
             const float ux = p0.x + cbi.x * p0.w + cbi.y * p1.z + cbi.z * p2.y;
             const float uy = p0.y + cbi.x * p1.x + cbi.y * p1.w + cbi.z * p2.z;
@@ -1223,8 +1250,8 @@ __global__ void __launch_bounds__(kFFLanes *SLICES, 20 / SLICES) k_ff_step(KPara
             sy = fmaf(w[m], uy, sy);
             sz = fmaf(w[m], uz, sz);
         }
-        tea_bead_update<FEFF>(P, B, g, sx, sy, sz, b2, K, feff);
     }
+    tea_bead_update<FEFF>(P, B, g, sx, sy, sz, b2, K, feff);
 }
 
 // Beads in no leaf (extra beads): the update draws their angular noise and
@@ -1241,8 +1268,10 @@ __global__ void k_ff_rest(KParams P, DevBuffers B, FFBuffers F, float4 *feff, co
 
 void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s) {
     if (F.nleaf == 0) return;
-    k_ff_p2m<<<F.nleaf + 1, kFFLeaf, 0, s>>>(P, B, F, gate);
-    k_ff_m2l<<<F.nleaf, 128, 0, s>>>(P, F, gate);
+    k_ff_p2m<<<(F.nleaf + kP2MWarps) / kP2MWarps, 32 * kP2MWarps, 0, s>>>(P, B, F, gate);
+    if (F.ninner > 0)
+        k_ff_p2m_inner<<<(F.ninner + kP2MWarps - 1) / kP2MWarps, 32 * kP2MWarps, 0, s>>>(P, F, gate);
+    if (F.ntgt > 0) k_ff_m2l<<<(F.ntgt + kM2LWarps - 1) / kM2LWarps, 32 * kM2LWarps, 0, s>>>(P, F, gate);
 }
 
 // Overlapping pairs can be taken from the LJ list when it holds every pair
@@ -1254,9 +1283,9 @@ static void ff_step_launch(const KParams &P, const DevBuffers &B, const FFBuffer
                            cudaStream_t s) {
     if (F.nleaf > 0) {
         if (ff_list_corr(P))
-            k_ff_step<SL, FEFF, true><<<F.nleaf, kFFLanes * SL, 0, s>>>(P, B, F, feff, gate);
+            k_ff_step<SL, FEFF, true><<<F.nleaf, 32 * SL, 0, s>>>(P, B, F, feff, gate);
         else
-            k_ff_step<SL, FEFF, false><<<F.nleaf, kFFLanes * SL, 0, s>>>(P, B, F, feff, gate);
+            k_ff_step<SL, FEFF, false><<<F.nleaf, 32 * SL, 0, s>>>(P, B, F, feff, gate);
     }
     if (F.nrest > 0) k_ff_rest<FEFF><<<(F.nrest + 127) / 128, 128, 0, s>>>(P, B, F, feff, gate);
 }

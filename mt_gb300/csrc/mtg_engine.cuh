@@ -98,7 +98,7 @@ struct mtg_engine {
     mtg::FFBuffers ffb{};
     long long ff_near_pairs = 0, ff_proxy_pairs = 0;
     std::vector<int> ff_host;        // the partition as built (for mtg_tea_farfield_layout)
-    int ff_sizes[4] = {0, 0, 0, 0};  // leaves, leaf beads, near entries, far entries
+    int ff_sizes[5] = {0, 0, 0, 0, 0};  // leaves, leaf beads, near entries, nodes, far entries
     // device address of the fixed scratch of mtg_energies_noalloc, looked up
     // by this engine's first call (energy_noalloc.cu)
     double *noalloc_scratch = nullptr;

@@ -298,33 +298,45 @@ void launch_set_flags(int nb, const uint8_t *extra, const int *gtp, const int *o
 constexpr int kTile = 128;   // beads per CTA tile of the O(N^2) kernels
 
 // ---------------------------------------------- far field of learned TEA
-// Leaves of at most kFFLeaf beads (a k-d partition of each trajectory,
-// tea_ff.cu), their near / far source leaves, and the per-step proxy data:
-// the 8 points c + h (+-kFFNode, +-kFFNode, +-kFFNode) of a leaf's bounding
-// box (centre c, half extent h; tensor-product Chebyshev nodes of degree 2)
-// carry the leaf's sources (F, R) as interpolation charges and receive the
-// far field of the leaves far from it, interpolated back to its beads.
-constexpr int kFFLeaf = 64;
+// A k-d tree over each trajectory's beads (tea_ff.cu) with leaves of at most
+// kFFLeaf beads; every node is a contiguous range of the leaf bead order.
+// Leaf pairs that are not well separated are summed bead by bead (near
+// lists of the leaves); well-separated node pairs, at the coarsest level
+// where they are, interact through proxies: the 8 points
+// c + h (+-kFFNode, +-kFFNode, +-kFFNode) of a node's bounding box (centre c,
+// half extent h; tensor-product Chebyshev nodes of degree 2) carry the
+// node's sources (F, R) as interpolation charges and receive the far field
+// of the nodes far from it, interpolated to each bead of the node.
+constexpr int kFFLeaf = 32;
 constexpr float kFFNode = 0.70710678f;
+constexpr int kFFMaxAnc = 24;          // nodes with far fields on a leaf's path to the root (tree depth bound)
 struct FFBuffers {
-    int nleaf, nrest;
+    int nleaf, nnode, ntgt, ninner, nrest;
     const int *leaf_start;   // [nleaf+1] into leaf_bead
-    const int *leaf_bead;    // beads of every leaf, leaf after leaf
+    const int *leaf_bead;    // beads of every leaf, leaf after leaf (every node a contiguous range)
     const int *leaf_traj;    // [nleaf]
     const int *near_start;   // [nleaf+1] into near: source leaves summed pair by pair
     const int *near;
-    const int *far_start;    // [nleaf+1] into far: source leaves taken through their proxies
+    const int *node_range;   // [2*nnode] begin, end in leaf_bead; nodes 0 .. nleaf-1 are the leaves, larger nodes first after them
+    const int *node_leaves;  // [2*nnode] first leaf, last leaf + 1 of each node
+    const int *far_start;    // [nnode+1] into far: source nodes taken through their proxies
     const int *far;
+    const int *tgt;          // [ntgt] nodes with a non-empty far list
+    const int *inner;        // [ninner] internal nodes that are far sources or targets, larger first
+    const int *anc_start;    // [nleaf+1] into anc: the leaf and its ancestors with a far list
+    const int *anc;
     const int *rest;         // [nrest] beads in no leaf (extra beads)
-    float4 *box;             // [2*nleaf] centre, half extent (w unused)
-    float4 *q;               // [16*nleaf] proxy m: (QF.xyz, QR.x) at 16L+m, (QR.y, QR.z, 0, 0) at 16L+8+m
-    float4 *phi;             // [24*nleaf] target proxy n: (A.xyz, B0.x), (B0.yz, B1.xy), (B1.z, B2.xyz) at 24L+3n
+    float4 *box;             // [2*nnode] centre, half extent (w unused)
+    float4 *q;               // [16*nnode] proxy m: (QF.xyz, QR.x) at 16N+m, (QR.y, QR.z, 0, 0) at 16N+8+m
+    float4 *phi;             // [24*nnode] target proxy n: (A.xyz, B0.x), (B0.yz, B1.xy), (B1.z, B2.xyz) at 24N+3n
     float4 *pack;            // [(nleaf+1)*kFFPackF4] each leaf's beads in the tile layout of the step kernel
                              // (leaf nleaf: padding, far away with zero F and R), written every step by P2M
 };
-// float4 per leaf of FFBuffers::pack: x x y y | z z Fx Fx | Fy Fy Fz Fz | Rx Rx Ry Ry
-// (kFFLeaf each), then Rz Rz of two slots per float4 (kFFLeaf / 2)
-constexpr int kFFPackF4 = 4 * kFFLeaf + kFFLeaf / 2;
+// float4 per leaf of FFBuffers::pack, for the bead pairs (2p, 2p+1):
+// xa xb ya yb | za zb Fxa Fxb | Fya Fyb Fza Fzb | Rxa Rxb Rya Ryb (kFFLeaf / 2
+// each), then Rza Rzb of two pairs per float4 (kFFLeaf / 4)
+constexpr int kFFPairSlots = kFFLeaf / 2;
+constexpr int kFFPackF4 = 4 * kFFPairSlots + kFFPairSlots / 2;
 // proxies (P2M) and far-field potentials at target proxies (M2L), while *gate == 0
 void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s);
 // near pairs + interpolated far field + update (FEFF: effective forces into feff, no update), while *gate == 0

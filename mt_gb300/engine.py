@@ -88,7 +88,7 @@ EXPORTS = {
     "mtg_set_tea_farfield": (C.c_int, [C.c_void_p, C.c_int, C.c_float, C.c_int]),
     "mtg_tea_farfield_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong),
                                          C.POINTER(C.c_longlong)]),
-    "mtg_tea_farfield_layout": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 7),
+    "mtg_tea_farfield_layout": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 9),
     "mtg_tea_effective_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                            C.POINTER(C.c_float)]),
 }
@@ -463,15 +463,17 @@ class Engine:
         return {"leaves": nl.value, "near_pairs": npairs.value, "proxy_pairs": ppairs.value}
 
     def tea_farfield_layout(self):
-        """(leaf_start, leaf_bead, near_start, near, far_start, far) of the grouping."""
-        sz = np.zeros(4, np.int32)
+        """(leaf_start, leaf_bead, near_start, near, node_range, node_parent, far_start, far) of the tree
+        (nodes 0 .. nleaf-1 are the leaves)."""
+        sz = np.zeros(5, np.int32)
         nul = C.cast(None, C.POINTER(C.c_int))
-        check(self.lib.mtg_tea_farfield_layout(self.h, ptr(sz, C.c_int), nul, nul, nul, nul, nul, nul))
-        nl = int(sz[0])
-        a = [np.zeros(nl + 1, np.int32), np.zeros(int(sz[1]), np.int32), np.zeros(nl + 1, np.int32),
-             np.zeros(max(int(sz[2]), 1), np.int32), np.zeros(nl + 1, np.int32), np.zeros(max(int(sz[3]), 1), np.int32)]
+        check(self.lib.mtg_tea_farfield_layout(self.h, ptr(sz, C.c_int), *([nul] * 8)))
+        nl, nbl, nnear, nn, nfar = (int(v) for v in sz)
+        a = [np.zeros(nl + 1, np.int32), np.zeros(max(nbl, 1), np.int32), np.zeros(nl + 1, np.int32),
+             np.zeros(max(nnear, 1), np.int32), np.zeros(max(2 * nn, 1), np.int32), np.zeros(max(nn, 1), np.int32),
+             np.zeros(nn + 1, np.int32), np.zeros(max(nfar, 1), np.int32)]
         check(self.lib.mtg_tea_farfield_layout(self.h, ptr(sz, C.c_int), *[ptr(x, C.c_int) for x in a]))
-        return a[0], a[1], a[2], a[3][:int(sz[2])], a[4], a[5][:int(sz[3])]
+        return (a[0], a[1][:nbl], a[2], a[3][:nnear], a[4][:2 * nn], a[5][:nn], a[6], a[7][:nfar])
 
     def tea_effective_forces(self, exact: bool = True, farfield: bool = True):
         """(feff_exact, feff_ff, rforce) [nb, 4] of the current state from one draw of random forces."""

@@ -1,6 +1,6 @@
 """The far field of the learned TEA mobility product on the GPU
 (mtg_set_tea_farfield): its kernels against the FP64 restatement
-(oracle/tea_ff_oracle.py) on the engine's own grouping, its approximation
+(oracle/tea_ff_oracle.py) on the engine's own tree, its approximation
 error against the exact all-pairs product at the learned comparison's
 trajectory size (5600 beads), and the learned mode running with it: re-checks
 against exact TEA, the fall-back to the exact product bit for bit, and the
@@ -44,10 +44,14 @@ def test_farfield_kernels_match_fp64_restatement(engine_mod):
     e.set_tea_farfield(True, THETA)
     st = e.tea_farfield_stats()
     layout = e.tea_farfield_layout()
-    leaf_start, leaf_bead = layout[0], layout[1]
-    assert np.all(np.diff(leaf_start) <= 64) and np.all(np.diff(leaf_start) > 0)
+    leaf_start, leaf_bead, _, _, node_range, node_parent, far_start, _ = layout
+    nleaf = len(leaf_start) - 1
+    assert np.all(np.diff(leaf_start) <= 32) and np.all(np.diff(leaf_start) > 0)
     act = b.extra == 0
     assert sorted(leaf_bead.tolist()) == np.nonzero(act)[0].tolist()   # every active bead in one leaf
+    assert np.array_equal(node_range[0:2 * nleaf:2], leaf_start[:-1])
+    assert np.all(node_parent[nleaf:] < np.arange(nleaf, len(node_parent)))   # larger nodes first
+    assert (np.diff(far_start)[nleaf:] > 0).any()                      # internal nodes take part
     fe, ff, rf = e.tea_effective_forces()
     _, F = e.download_state(forces=True)
     betab = beta[bead_traj(b)]
