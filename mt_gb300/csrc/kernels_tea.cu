@@ -805,10 +805,11 @@ __device__ __forceinline__ void ff_tile_issue(FFTile &T, const FFBuffers &F, con
 
 // Trilinear Lagrange weights of the 8 proxies (bit 0: x, bit 1: y, bit 2: z;
 // a clear bit is the node at -h/sqrt(2), a set bit the one at +h/sqrt(2)) at
-// position x of a box (c, h).
+// position x of a box (c, h); the fast division's 2-ulp error is far below
+// the interpolation's own.
 __device__ __forceinline__ void ff_weights(float3 x, float4 c, float4 h, float w[8]) {
-    const float tx = (x.x - c.x) / (h.x * kFFNode), ty = (x.y - c.y) / (h.y * kFFNode),
-                tz = (x.z - c.z) / (h.z * kFFNode);
+    const float tx = __fdividef(x.x - c.x, h.x * kFFNode), ty = __fdividef(x.y - c.y, h.y * kFFNode),
+                tz = __fdividef(x.z - c.z, h.z * kFFNode);
     const float lx[2] = {0.5f * (1.0f - tx), 0.5f * (1.0f + tx)};
     const float ly[2] = {0.5f * (1.0f - ty), 0.5f * (1.0f + ty)};
     const float lz[2] = {0.5f * (1.0f - tz), 0.5f * (1.0f + tz)};
@@ -1053,15 +1054,22 @@ __global__ void __launch_bounds__(32 * kM2LWarps) k_ff_m2l(KParams P, FFBuffers 
     }
 }
 
-// The packed pass of one tile: the target bead (position -n, weight cb) against
-// the tile's bead pairs; with SELF the target's own slot (pair self_p, lane
-// self_h) is pushed to r^2 = 1e30, with TRACK the running minimum of r^2 per
-// segment of the thread's pairs is kept.
-template <int SLICES, bool SELF, bool TRACK>
-__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_p, int self_h, float2 nx, float2 ny,
-                                             float2 nz, float2 cbx, float2 cby, float2 cbz, float2 vkap,
-                                             float2 vn2a2, float2 one, float2 &ax, float2 &ay, float2 &az,
-                                             float (&rmin)[kTeaSeg]) {
+// Targets of one thread of the far-field step: TPT beads of the leaf, each
+// with its negated position, its weights beta C_i (both duplicated into the
+// two lanes of a packed pair), its packed sums, its own pair slot and lane.
+template <int TPT>
+struct FFTargets {
+    float2 nx[TPT], ny[TPT], nz[TPT], cbx[TPT], cby[TPT], cbz[TPT];
+    float2 ax[TPT], ay[TPT], az[TPT];
+    int self_p[TPT], self_h[TPT];
+};
+
+// The packed pass of one tile: the thread's targets against the tile's bead
+// pairs; with SELF a target's own slot is pushed to r^2 = 1e30, with TRACK
+// the running minimum of r^2 per segment of the thread's pairs is kept.
+template <int SLICES, int TPT, bool SELF, bool TRACK>
+__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, FFTargets<TPT> &X, float2 vkap, float2 vn2a2,
+                                             float2 one, float (&rmin)[kTeaSeg]) {
     constexpr int kLen = kFFTileSlots / SLICES / kTeaSeg;
 #pragma unroll
     for (int sg = 0; sg < kTeaSeg; sg++) {
@@ -1069,77 +1077,137 @@ __device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int self_p
         for (int k = 0; k < kLen; k++) {
             const int t = sl + (sg * kLen + k) * SLICES;
             const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
-            const float2 dx = __fadd2_rn(lo2(a), nx), dy = __fadd2_rn(hi2(a), ny), dz = __fadd2_rn(lo2(b), nz);
-            const float2 gx = __ffma2_rn(lo2(d), cbx, hi2(b)), gy = __ffma2_rn(hi2(d), cby, lo2(c)),
-                         gz = __ffma2_rn(T.rz[t], cbz, hi2(c));
-            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-            if (SELF && t == self_p) {
-                if (self_h)
-                    r2.y = 1e30f;
-                else
-                    r2.x = 1e30f;
+            const float2 rz = T.rz[t];
+#pragma unroll
+            for (int h = 0; h < TPT; h++) {
+                const float2 dx = __fadd2_rn(lo2(a), X.nx[h]), dy = __fadd2_rn(hi2(a), X.ny[h]),
+                             dz = __fadd2_rn(lo2(b), X.nz[h]);
+                const float2 gx = __ffma2_rn(lo2(d), X.cbx[h], hi2(b)), gy = __ffma2_rn(hi2(d), X.cby[h], lo2(c)),
+                             gz = __ffma2_rn(rz, X.cbz[h], hi2(c));
+                float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                if (SELF && t == X.self_p[h]) {
+                    if (X.self_h[h])
+                        r2.y = 1e30f;
+                    else
+                        r2.x = 1e30f;
+                }
+                if (TRACK) rmin[sg] = fmin3(rmin[sg], r2.x, r2.y);
+                const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
+                const float2 q = __fmul2_rn(rinv, rinv);
+                const float2 tq = __fmul2_rn(q, rinv);
+                const float2 cii = __ffma2_rn(vkap, tq, rinv);
+                const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
+                const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
+                X.ax[h] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, X.ax[h]));
+                X.ay[h] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, X.ay[h]));
+                X.az[h] = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, X.az[h]));
             }
-            if (TRACK) rmin[sg] = fmin3(rmin[sg], r2.x, r2.y);
-            const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-            const float2 q = __fmul2_rn(rinv, rinv);
-            const float2 tq = __fmul2_rn(q, rinv);
-            const float2 cii = __ffma2_rn(vkap, tq, rinv);
-            const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
-            const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
-            ax = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, ax));
-            ay = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, ay));
-            az = __ffma2_rn(cii, gz, __ffma2_rn(s, dz, az));
         }
     }
 }
 
-// Near pairs, far field and update: one CTA of 32 x SLICES threads per
-// target leaf; lane il serves the leaf's bead il, the SLICES warps take
-// interleaved bead pairs of every tile of near leaves (kFFTileLeaves leaves
-// per tile, copied asynchronously one tile ahead), the two lanes of each
-// packed operation being two source beads.  Overlapping pairs (r <= 2a) get
-// the near formula: with LISTCORR by walking the bead's LJ list once,
-// otherwise by rescanning the tile segments whose running minimum of r^2
-// flags one, as in k_tea_step.  Then the far field of the leaf and of each
-// ancestor with a far list is interpolated from that node's proxies and the
-// bead moves (FEFF: its effective force goes to feff instead).
-template <int SLICES, bool FEFF, bool LISTCORR>
-__global__ void __launch_bounds__(32 * SLICES, 20 / SLICES) k_ff_step(KParams P, DevBuffers B, FFBuffers F,
-                                                                    float4 *feff, const int *gate) {
+// Near pairs, far field and update: one CTA of (32 / TPT) x SLICES threads
+// per target leaf; thread lane il serves the leaf's beads il + h 32 / TPT
+// (h < TPT), the SLICES groups of lanes take interleaved bead pairs of every
+// tile of near leaves (kFFTileLeaves leaves per tile, copied asynchronously
+// one tile ahead), the two lanes of each packed operation being two source
+// beads.  Overlapping pairs (r <= 2a) get the near formula: with LISTCORR by
+// walking the bead's LJ list once, otherwise by rescanning the tile segments
+// whose running minimum of r^2 flags one, as in k_tea_step.  Then the far
+// fields of the leaf and of each ancestor with a far list are brought to the
+// leaf's proxies (L2L), summed, interpolated to the bead (L2P), and the bead
+// moves (FEFF: its effective force goes to feff instead).
+template <int SLICES, int TPT, bool FEFF, bool LISTCORR>
+__global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_step(KParams P, DevBuffers B,
+                                                                                FFBuffers F, float4 *feff,
+                                                                                const int *gate) {
     if (gate && *gate != 0) return;
+    constexpr int kLanes = 32 / TPT;
     const int L = blockIdx.x;
-    const int il = threadIdx.x & 31, sl = threadIdx.x >> 5;
+    const int il = threadIdx.x % kLanes, sl = threadIdx.x / kLanes;
     const int s0 = F.leaf_start[L], n = F.leaf_start[L + 1] - s0;
     const int traj = F.leaf_traj[L];
     __shared__ FFTile T2[2];
     __shared__ float4 s_red[SLICES * 32];
     __shared__ float4 s_far[kFFMaxAnc * 26];   // per ancestor: box (2), potentials (24)
+    __shared__ float s_pl[8 * 12];             // the far field at the leaf's proxies
+    __shared__ float4 s_lbox[2];
+    __shared__ float4 s_x[32], s_cb[32];       // the leaf's beads: position, beta C_i
     __shared__ int s_near[kFFNearSmem];
     const float beta = B.tea_beta[traj], b2 = beta * beta;
-    const int g = il < n ? F.leaf_bead[s0 + il] : -1;
-    float3 xi = make_float3(0.f, 0.f, 0.f), cbi = make_float3(0.f, 0.f, 0.f);
-    if (g >= 0) {
-        xi = f3(B.frame_in[g]);
-        const float4 ci = B.tea_ci[g];
-        cbi = make_float3(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
-                          beta / sqrtf(1.0f + b2 * ci.z));
+    if (threadIdx.x < 32) {
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f), cb = x;
+        if (threadIdx.x < n) {
+            const int g = F.leaf_bead[s0 + threadIdx.x];
+            x = B.frame_in[g];
+            const float4 ci = B.tea_ci[g];
+            cb = make_float4(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
+                             beta / sqrtf(1.0f + b2 * ci.z), 0.f);
+        }
+        s_x[threadIdx.x] = x;
+        s_cb[threadIdx.x] = cb;
     }
-    const float2 nx = f2(-xi.x), ny = f2(-xi.y), nz = f2(-xi.z), cbx = f2(cbi.x), cby = f2(cbi.y), cbz = f2(cbi.z);
-    float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f);
-    const TeaConst K = tea_const(P.tea_a);
-    const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
     // near leaves in tiles of kFFTileLeaves, double-buffered: the copies of
     // tile k + 1 are in flight while tile k is summed
     const int e_beg = F.near_start[L], nnear = F.near_start[L + 1] - e_beg;
     const int *near = F.near + e_beg;
-    if (nnear <= kFFNearSmem) {
+    const bool near_smem = nnear <= kFFNearSmem;
+    if (near_smem)
         for (int k = threadIdx.x; k < nnear; k += blockDim.x) s_near[k] = near[k];
-        near = s_near;
-        __syncthreads();
-    }
+    if (threadIdx.x < 2) s_lbox[threadIdx.x] = F.box[2 * L + threadIdx.x];
+    __syncthreads();
+    if (near_smem) near = s_near;
+    const TeaConst K = tea_const(P.tea_a);
+    const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
     const int ntiles = (nnear + kFFTileLeaves - 1) / kFFTileLeaves;
     ff_tile_issue(T2[0], F, near, 0, nnear);
+    // the far fields of the leaf and its ancestors (boxes, potentials) travel
+    // with the first tile
+    const int a0 = F.anc_start[L], na = min(F.anc_start[L + 1] - a0, kFFMaxAnc);
+    for (int k = threadIdx.x; k < 26 * na; k += blockDim.x) {
+        const int N = F.anc[a0 + k / 26], w = k % 26;
+        cp_async16(&s_far[k], w < 2 ? &F.box[2 * N + w] : &F.phi[24 * N + w - 2]);
+    }
     cp_async_commit();
+    FFTargets<TPT> X;
+    float3 corr[TPT];
+#pragma unroll
+    for (int h = 0; h < TPT; h++) {
+        const int bi = il + h * kLanes;
+        const float4 x = s_x[bi], cb = s_cb[bi];
+        X.nx[h] = f2(-x.x);
+        X.ny[h] = f2(-x.y);
+        X.nz[h] = f2(-x.z);
+        X.cbx[h] = f2(cb.x);
+        X.cby[h] = f2(cb.y);
+        X.cbz[h] = f2(cb.z);
+        X.ax[h] = X.ay[h] = X.az[h] = f2(0.f);
+        corr[h] = make_float3(0.f, 0.f, 0.f);
+        if (LISTCORR && bi < n) {
+            // overlapping pairs (r <= 2a): every one is within the LJ list
+            // cutoff (checked by the launcher), so the far-field term of the
+            // tile pass is replaced by the near one while walking the bead's
+            // list, the SLICES threads of a bead taking interleaved entries;
+            // done while the first tile is in flight
+            const int g = F.leaf_bead[s0 + bi];
+            const int base = B.off[traj], nb = P.nb;
+            const int cnt = B.ljc[g];
+            for (int q = sl; q < cnt; q += SLICES) {
+                const int pj = base + B.lj[q * nb + g];
+                const float4 xj = B.frame_in[pj];
+                const float dx = xj.x - x.x, dy = xj.y - x.y, dz = xj.z - x.z;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (!(r2 <= K.four_a2) || (B.flags[pj] & kFlagExtra)) continue;
+                const float4 Fj = B.force[pj], Rj = B.tea_r[pj];
+                const float gx = fmaf(Rj.x, cb.x, Fj.x), gy = fmaf(Rj.y, cb.y, Fj.y), gz = fmaf(Rj.z, cb.z, Fj.z);
+                const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+                const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
+                corr[h].x += nr.x - fa.x;
+                corr[h].y += nr.y - fa.y;
+                corr[h].z += nr.z - fa.z;
+            }
+        }
+    }
     for (int it = 0; it < ntiles; it++) {
         if (it + 1 < ntiles) ff_tile_issue(T2[(it + 1) & 1], F, near, (it + 1) * kFFTileLeaves, nnear);
         cp_async_commit();
@@ -1156,13 +1224,16 @@ __global__ void __launch_bounds__(32 * SLICES, 20 / SLICES) k_ff_step(KParams P,
 #pragma unroll
         for (int sg = 0; sg < kTeaSeg; sg++) rmin[sg] = 3.4e38f;
         const bool self = self_q >= 0;
-        const int self_p = self_q * kFFPairSlots + (il >> 1), self_h = il & 1;
+#pragma unroll
+        for (int h = 0; h < TPT; h++) {
+            const int bi = il + h * kLanes;
+            X.self_p[h] = self_q * kFFPairSlots + (bi >> 1);
+            X.self_h[h] = bi & 1;
+        }
         if (self)
-            ff_step_tile<SLICES, true, !LISTCORR>(T, sl, self_p, self_h, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2, one,
-                                                  ax, ay, az, rmin);
+            ff_step_tile<SLICES, TPT, true, !LISTCORR>(T, sl, X, vkap, vn2a2, one, rmin);
         else
-            ff_step_tile<SLICES, false, !LISTCORR>(T, sl, self_p, self_h, nx, ny, nz, cbx, cby, cbz, vkap, vn2a2,
-                                                   one, ax, ay, az, rmin);
+            ff_step_tile<SLICES, TPT, false, !LISTCORR>(T, sl, X, vkap, vn2a2, one, rmin);
         if (!LISTCORR) {
             constexpr int kLen = kFFTileSlots / SLICES / kTeaSeg;
             unsigned segs = 0;
@@ -1173,79 +1244,85 @@ __global__ void __launch_bounds__(32 * SLICES, 20 / SLICES) k_ff_step(KParams P,
                 segs &= segs - 1;
                 for (int k = 0; k < kLen; k++) {
                     const int t = sl + (sg * kLen + k) * SLICES;
+                    const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
+                    const float2 rz = T.rz[t];
 #pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        if (self && t == self_p && h == self_h) continue;
-                        const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
-                        const float dx = (h ? a.y : a.x) - xi.x, dy = (h ? a.w : a.z) - xi.y,
-                                    dz = (h ? b.y : b.x) - xi.z;
-                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        if (!(r2 <= K.four_a2)) continue;
-                        const float2 rz = T.rz[t];
-                        const float gx = fmaf(h ? d.y : d.x, cbi.x, h ? b.w : b.z),
-                                    gy = fmaf(h ? d.w : d.z, cbi.y, h ? c.y : c.x),
-                                    gz = fmaf(h ? rz.y : rz.x, cbi.z, h ? c.w : c.z);
-                        const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
-                        const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
-                        ax.x += nr.x - fa.x;
-                        ay.x += nr.y - fa.y;
-                        az.x += nr.z - fa.z;
-                    }
+                    for (int h = 0; h < TPT; h++)
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            if (self && t == X.self_p[h] && e == X.self_h[h]) continue;
+                            const float dx = (e ? a.y : a.x) + X.nx[h].x, dy = (e ? a.w : a.z) + X.ny[h].x,
+                                        dz = (e ? b.y : b.x) + X.nz[h].x;
+                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                            if (!(r2 <= K.four_a2)) continue;
+                            const float gx = fmaf(e ? d.y : d.x, X.cbx[h].x, e ? b.w : b.z),
+                                        gy = fmaf(e ? d.w : d.z, X.cby[h].x, e ? c.y : c.x),
+                                        gz = fmaf(e ? rz.y : rz.x, X.cbz[h].x, e ? c.w : c.z);
+                            const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
+                            const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
+                            corr[h].x += nr.x - fa.x;
+                            corr[h].y += nr.y - fa.y;
+                            corr[h].z += nr.z - fa.z;
+                        }
                 }
             }
         }
         __syncthreads();
     }
-    float3 sum = make_float3(ax.x + ax.y, ay.x + ay.y, az.x + az.y);
-    if (LISTCORR && g >= 0) {
-        // overlapping pairs (r <= 2a): every one is within the LJ list cutoff
-        // (checked by the launcher), so the far-field term of the tile pass is
-        // replaced by the near one while walking the bead's list; the SLICES
-        // threads of a bead take interleaved entries
-        const int base = B.off[traj], nb = P.nb;
-        const int cnt = B.ljc[g];
-        for (int q = sl; q < cnt; q += SLICES) {
-            const int pj = base + B.lj[q * nb + g];
-            const float4 xj = B.frame_in[pj];
-            const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (!(r2 <= K.four_a2) || (B.flags[pj] & kFlagExtra)) continue;
-            const float4 Fj = B.force[pj], Rj = B.tea_r[pj];
-            const float gx = fmaf(Rj.x, cbi.x, Fj.x), gy = fmaf(Rj.y, cbi.y, Fj.y), gz = fmaf(Rj.z, cbi.z, Fj.z);
-            const float3 fa = tea_far1(K, dx, dy, dz, gx, gy, gz);
-            const float3 nr = tea_pair1(K, dx, dy, dz, gx, gy, gz);
-            sum.x += nr.x - fa.x;
-            sum.y += nr.y - fa.y;
-            sum.z += nr.z - fa.z;
+#pragma unroll
+    for (int h = 0; h < TPT; h++) {
+        const int bi = il + h * kLanes;
+        s_red[sl * 32 + bi] = make_float4(X.ax[h].x + X.ax[h].y + corr[h].x, X.ay[h].x + X.ay[h].y + corr[h].y,
+                                          X.az[h].x + X.az[h].y + corr[h].z, 0.f);
+    }
+    // L2L: every ancestor's far field (trilinear over its box) at the leaf's 8
+    // proxies, one (ancestor, proxy) per thread; interpolating those on the
+    // leaf reproduces it exactly.  Then the sum over the ancestors, in order.
+    // (The tile buffers are free now: the loop ended with a barrier.)
+    static_assert(sizeof(float) * kFFMaxAnc * 96 <= sizeof(T2), "L2L partials fit in the tile buffers");
+    float *s_l2l = reinterpret_cast<float *>(T2);
+    for (int t = threadIdx.x; t < 8 * na; t += blockDim.x) {
+        const int A = t >> 3, pn = t & 7;
+        const float4 *fr = s_far + 26 * A;
+        const float *ph = reinterpret_cast<const float *>(fr + 2);
+        float w[8];
+        ff_weights(ff_proxy(s_lbox[0], s_lbox[1], pn), fr[0], fr[1], w);
+#pragma unroll
+        for (int c = 0; c < 12; c++) {
+            float v = 0.f;
+#pragma unroll
+            for (int m = 0; m < 8; m++) v = fmaf(w[m], ph[12 * m + c], v);
+            s_l2l[96 * A + 12 * pn + c] = v;
         }
     }
-    s_red[sl * 32 + il] = make_float4(sum.x, sum.y, sum.z, 0.f);
-    // the far fields of the leaf and its ancestors: boxes and potentials
-    const int a0 = F.anc_start[L], na = min(F.anc_start[L + 1] - a0, kFFMaxAnc);
-    for (int k = threadIdx.x; k < 26 * na; k += blockDim.x) {
-        const int N = F.anc[a0 + k / 26], w = k % 26;
-        s_far[k] = w < 2 ? F.box[2 * N + w] : F.phi[24 * N + w - 2];
+    __syncthreads();
+    for (int t = threadIdx.x; t < 96 && na > 0; t += blockDim.x) {
+        float v = 0.f;
+        for (int A = 0; A < na; A++) v += s_l2l[96 * A + t];
+        s_pl[t] = v;
     }
     __syncthreads();
-    if (sl != 0 || g < 0) return;
+    const int bi = threadIdx.x;
+    if (bi >= n) return;
+    const int g = F.leaf_bead[s0 + bi];
+    const float3 xi = f3(s_x[bi]), cbi = f3(s_cb[bi]);
     float sx = 0.f, sy = 0.f, sz = 0.f;
     for (int k = 0; k < SLICES; k++) {
-        const float4 v = s_red[k * 32 + il];
+        const float4 v = s_red[k * 32 + bi];
         sx += v.x;
         sy += v.y;
         sz += v.z;
     }
-    for (int A = 0; A < na; A++) {   // L2P
-        const float4 *fr = s_far + 26 * A;
+    if (na > 0) {   // L2P from the leaf's proxies
         float w[8];
-        ff_weights(xi, fr[0], fr[1], w);
+        ff_weights(xi, s_lbox[0], s_lbox[1], w);
 #pragma unroll
         for (int m = 0; m < 8; m++) {
-            const float4 p0 = fr[2 + 3 * m], p1 = fr[3 + 3 * m], p2 = fr[4 + 3 * m];
+            const float *p = s_pl + 12 * m;   // A.xyz, B_x.xyz, B_y.xyz, B_z.xyz
             // A + beta C_x B_x + beta C_y B_y + beta C_z B_z
-            const float ux = p0.x + cbi.x * p0.w + cbi.y * p1.z + cbi.z * p2.y;
-            const float uy = p0.y + cbi.x * p1.x + cbi.y * p1.w + cbi.z * p2.z;
-            const float uz = p0.z + cbi.x * p1.y + cbi.y * p2.x + cbi.z * p2.w;
+            const float ux = p[0] + cbi.x * p[3] + cbi.y * p[6] + cbi.z * p[9];
+            const float uy = p[1] + cbi.x * p[4] + cbi.y * p[7] + cbi.z * p[10];
+            const float uz = p[2] + cbi.x * p[5] + cbi.y * p[8] + cbi.z * p[11];
             sx = fmaf(w[m], ux, sx);
             sy = fmaf(w[m], uy, sy);
             sz = fmaf(w[m], uz, sz);
@@ -1278,14 +1355,19 @@ void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F
 // within 2a (plus 2 nm for the motion since its rebuild).
 static bool ff_list_corr(const KParams &P) { return P.lj_on && P.ljcut >= 2.0f * P.tea_a + 2.0f; }
 
+#ifndef FF_TPT
+#define FF_TPT 1
+#endif
+constexpr int kFFTPT = FF_TPT;   // target beads per thread of the far-field step
 template <int SL, bool FEFF>
 static void ff_step_launch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff, const int *gate,
                            cudaStream_t s) {
+    constexpr int threads = 32 / kFFTPT * SL;
     if (F.nleaf > 0) {
         if (ff_list_corr(P))
-            k_ff_step<SL, FEFF, true><<<F.nleaf, 32 * SL, 0, s>>>(P, B, F, feff, gate);
+            k_ff_step<SL, kFFTPT, FEFF, true><<<F.nleaf, threads, 0, s>>>(P, B, F, feff, gate);
         else
-            k_ff_step<SL, FEFF, false><<<F.nleaf, 32 * SL, 0, s>>>(P, B, F, feff, gate);
+            k_ff_step<SL, kFFTPT, FEFF, false><<<F.nleaf, threads, 0, s>>>(P, B, F, feff, gate);
     }
     if (F.nrest > 0) k_ff_rest<FEFF><<<(F.nrest + 127) / 128, 128, 0, s>>>(P, B, F, feff, gate);
 }

@@ -309,7 +309,7 @@ constexpr int kTile = 128;   // beads per CTA tile of the O(N^2) kernels
 // of the nodes far from it, interpolated to each bead of the node.
 constexpr int kFFLeaf = 32;
 constexpr float kFFNode = 0.70710678f;
-constexpr int kFFMaxAnc = 24;          // nodes with far fields on a leaf's path to the root (tree depth bound)
+constexpr int kFFMaxAnc = 16;          // nodes with far fields on a leaf's path to the root (tree depth bound)
 struct FFBuffers {
     int nleaf, nnode, ntgt, ninner, nrest;
     const int *leaf_start;   // [nleaf+1] into leaf_bead
