@@ -386,6 +386,27 @@ def run_reference(args, spec, dist):
 
 
 # ------------------------------------------------------------------ main
+def kernel_time_pass(e, step: int, period: int, nsteps: int, flush):
+    """Per-kernel CUDA-event times from a second pass of the same steps (the
+    timed pass runs without the per-kernel events, which would add gaps)."""
+    import torch
+    e.set_kernel_timing(True)
+    e.step(step, period)          # captures the instrumented graph
+    step += period
+    e.kernel_times(reset=True)
+    for _ in range(nsteps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e.step_timed(step, period)
+        step += period
+    torch.cuda.synchronize()
+    kt = e.kernel_times(reset=True)
+    e.set_kernel_timing(False)
+    e.step(step, period)          # the uninstrumented graph again
+    step += period
+    return step, kt
+
+
 def run_gpu(args, spec, dist, cpu_seconds: float = 20.0):
     import torch
 
@@ -408,10 +429,6 @@ def run_gpu(args, spec, dist, cpu_seconds: float = 20.0):
     for _ in range(args.warmup):
         e.step(step, period)
         step += period
-    e.set_kernel_timing(True)
-    e.step(step, period)          # capture the timed graph outside the timed region
-    step += period
-    e.kernel_times(reset=True)
     e.graph_kernel_launches(reset=True)
 
     clocks = ClockSampler(dist.local)
@@ -426,9 +443,8 @@ def run_gpu(args, spec, dist, cpu_seconds: float = 20.0):
     torch.cuda.synchronize()
     dist.barrier()
     clk = clocks.stop()
-    kt = e.kernel_times(reset=True)
     graph_kernels = e.graph_kernel_launches(reset=True)   # every timed step is a graph replay
-    e.set_kernel_timing(False)
+    step, kt = kernel_time_pass(e, step, period, args.steps, flush)
     total_ms = sum(ms)
     t_max = dist.max(total_ms)
     total_units = dist.sum(active * period * args.steps)
@@ -722,10 +738,6 @@ def run_tea_compare(args, spec, dist):
         for _ in range(args.warmup):
             e.step(step, period)
             step += period
-        e.set_kernel_timing(True)
-        e.step(step, period)
-        step += period
-        e.kernel_times(reset=True)
         e.graph_kernel_launches(reset=True)
         clocks = ClockSampler(dist.local)
         clocks.start()
@@ -738,9 +750,8 @@ def run_tea_compare(args, spec, dist):
             step += period
         dist.barrier()
         clk = clocks.stop()
-        kt = e.kernel_times(reset=True)
         graph_kernels = e.graph_kernel_launches(reset=True)   # every timed step is a graph replay
-        e.set_kernel_timing(False)
+        step, kt = kernel_time_pass(e, step, period, args.steps, flush)
         t_max = dist.max(sum(ms))
         value = dist.sum(active * period * args.steps) / (t_max / 1e3)
         res = {"value": value, "ms_per_step": t_max / args.steps, "clocks": clk,

@@ -745,17 +745,17 @@ void launch_tea_feff(const KParams &P, const DevBuffers &B, const int2 *work, in
 }
 
 // ---------------------------------------------- far field of learned TEA
-// The learned mode's approximation of sum_j T_ij (F_j + beta C_i o R_j):
-// pairs of beads in near leaves are summed exactly (the packed pair loop of
-// k_tea_step over one source leaf per tile), and every far leaf J acts on a
-// target leaf I through proxies: J's sources are spread onto the 8 corners
-// of a Chebyshev grid in its bounding box (P2M, trilinear Lagrange weights at
-// nodes +-h/sqrt(2)), the RPY far field of those 8 charges is evaluated at
-// the 8 grid points of I (M2L) and interpolated back to I's beads (L2P).
+// The learned mode's approximation of sum_j T_ij (F_j + beta C_i o R_j) on a
+// k-d tree per trajectory (tea_ff.cu): pairs of beads in near leaves are
+// summed exactly (the packed pair loop of k_tea_step, source beads in the two
+// lanes), and every far node J acts on a target node N through proxies: J's
+// sources are spread onto the 8 points of a Chebyshev grid in its bounding box
+// (P2M, trilinear Lagrange weights at nodes +-h/sqrt(2)), the RPY far field
+// of those 8 charges is evaluated at the 8 grid points of N (M2L), brought
+// down to the leaves under N (L2L) and interpolated to their beads (L2P).
 // Because C_i weights R_j per component and per target, the proxies carry F
 // and R separately and the targets receive A = T Q_F and B_k = T e_k Q_R,k
-// (k = x, y, z); a bead adds A + sum_k beta C_ik B_k.  Far means the leaves'
-// centres are farther apart than (r_I + r_J + margin) / theta (tea_ff.cu).
+// (k = x, y, z); a bead adds A + sum_k beta C_ik B_k.
 
 // Tile of kFFTileLeaves source leaves (kFFPairSlots bead pairs each), in the
 // layout of FFBuffers::pack: the two lanes of a packed pair are two source
@@ -782,15 +782,16 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // from global memory).
 constexpr int kFFNearSmem = 256;
 
-// Issues the copies of near-list entries e0 .. e0 + kFFTileLeaves - 1 (the
-// padding leaf past e1; entries relative to the list's start) into tile T:
-// each leaf is kFFPackF4 contiguous float4 of pack.
+// Issues the copies of near-list entries e0 .. min(e0 + kFFTileLeaves, e1) - 1
+// (entries relative to the list's start) into tile T: each leaf is kFFPackF4
+// contiguous float4 of pack.
 __device__ __forceinline__ void ff_tile_issue(FFTile &T, const FFBuffers &F, const int *near, int e0, int e1) {
     constexpr int kPer = kFFPackF4;
     for (int c = threadIdx.x; c < kFFTileLeaves * kPer; c += blockDim.x) {
         const int q = c / kPer, w = c % kPer;
         const int e = e0 + q;
-        const int J = e < e1 ? near[e] : F.nleaf;
+        if (e >= e1) continue;   // past the list: the tile pass skips the slot
+        const int J = near[e];
         const float4 *src = F.pack + (size_t)J * kPer + w;
         float4 *dst;
         if (w < 4 * kFFPairSlots) {
@@ -882,20 +883,36 @@ __device__ __forceinline__ void ff_store_charges(const FFBuffers &F, int N, floa
     if (lane < 16) put(32 + lane, s_hi);
 }
 
-// Writes the empty slot k of leaf N's pack (far away, zero F and R), or bead
-// values into it.
-__device__ __forceinline__ void ff_pack_slot(const FFBuffers &F, int N, int k, float3 x, float4 Fv, float4 R) {
-    float *pk = reinterpret_cast<float *>(F.pack + (size_t)N * kFFPackF4);
-    const int p = k >> 1, h = k & 1;
-    pk[4 * p + h] = x.x;
-    pk[4 * p + 2 + h] = x.y;
-    pk[4 * (kFFPairSlots + p) + h] = x.z;
-    pk[4 * (kFFPairSlots + p) + 2 + h] = Fv.x;
-    pk[4 * (2 * kFFPairSlots + p) + h] = Fv.y;
-    pk[4 * (2 * kFFPairSlots + p) + 2 + h] = Fv.z;
-    pk[4 * (3 * kFFPairSlots + p) + h] = R.x;
-    pk[4 * (3 * kFFPairSlots + p) + 2 + h] = R.y;
-    pk[4 * 4 * kFFPairSlots + 2 * p + h] = R.z;
+// Writes lane k's bead (or an empty slot: far away, zero F and R) into leaf
+// N's pack: lanes 2p and 2p + 1 swap their values and write bead pair p as
+// whole 16-byte words (the even lane the position words, the odd lane the
+// force and random-force words, the even lane Rz with its neighbour pair's).
+// Called by all 32 lanes of the warp.
+__device__ __forceinline__ void ff_pack_warp(const FFBuffers &F, int N, float3 x, float4 Fv, float4 R) {
+    const int lane = threadIdx.x & 31, p = lane >> 1;
+    const bool odd = lane & 1;
+    const float v[9] = {x.x, x.y, x.z, Fv.x, Fv.y, Fv.z, R.x, R.y, R.z};
+    float o[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) o[i] = __shfl_xor_sync(0xffffffffu, v[i], 1);
+    // (a, b) = (even lane's bead, odd lane's bead)
+    float a[9], b[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        a[i] = odd ? o[i] : v[i];
+        b[i] = odd ? v[i] : o[i];
+    }
+    float4 *pk = F.pack + (size_t)N * kFFPackF4;
+    if (!odd) {
+        pk[p] = make_float4(a[0], b[0], a[1], b[1]);                      // xa xb ya yb
+        pk[kFFPairSlots + p] = make_float4(a[2], b[2], a[3], b[3]);       // za zb Fxa Fxb
+    } else {
+        pk[2 * kFFPairSlots + p] = make_float4(a[4], b[4], a[5], b[5]);   // Fya Fyb Fza Fzb
+        pk[3 * kFFPairSlots + p] = make_float4(a[6], b[6], a[7], b[7]);   // Rxa Rxb Rya Ryb
+    }
+    // Rz of pairs p (lanes 4w, 4w+1) and p + 1 (lanes 4w+2, 4w+3) in one word
+    const float rz2a = __shfl_down_sync(0xffffffffu, a[8], 2), rz2b = __shfl_down_sync(0xffffffffu, b[8], 2);
+    if ((lane & 3) == 0) pk[4 * kFFPairSlots + (p >> 1)] = make_float4(a[8], b[8], rz2a, rz2b);
 }
 
 // P2M of the leaves, one warp per leaf (lane k: bead k): the bounding box,
@@ -908,7 +925,7 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_ff_p2m(KParams P, DevBuffers
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 away = make_float3(kFarAway, kFarAway, kFarAway);
     if (N == F.nleaf) {
-        ff_pack_slot(F, N, lane, away, zero, zero);
+        ff_pack_warp(F, N, away, zero, zero);
         return;
     }
     const int b0 = F.leaf_start[N], n = F.leaf_start[N + 1] - b0;
@@ -927,7 +944,7 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_ff_p2m(KParams P, DevBuffers
     const float4 c = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.f);
     const float4 h = make_float4(fmaxf(0.5f * (hi.x - lo.x), 1e-3f), fmaxf(0.5f * (hi.y - lo.y), 1e-3f),
                                  fmaxf(0.5f * (hi.z - lo.z), 1e-3f), 0.f);
-    ff_pack_slot(F, N, lane, lane < n ? x : away, Fv, R);
+    ff_pack_warp(F, N, lane < n ? x : away, Fv, R);
     float w[8];
     ff_weights(x, c, h, w);
     const float val[6] = {Fv.x, Fv.y, Fv.z, R.x, R.y, R.z};
@@ -988,15 +1005,21 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_ff_p2m_inner(KParams P, FFBu
     }
 }
 
-// M2L: one warp per target node; lane t serves the target proxies t % 4 and
-// t % 4 + 4 (the same x and y, opposite z) as one packed pair over every 8th
-// far node, and the 8 slices meet by shuffles in a fixed order.
+// M2L: 4 x kM2LSlices lanes per target node; lane t serves the target
+// proxies t % 4 and t % 4 + 4 (the same x and y, opposite z) as one packed
+// pair over every kM2LSlices-th far node, and the slices meet by shuffles in
+// a fixed order.
 constexpr int kM2LWarps = 4;
+#ifndef FF_M2L_SLICES
+#define FF_M2L_SLICES 8
+#endif
+constexpr int kM2LSlices = FF_M2L_SLICES, kM2LLanes = 4 * kM2LSlices;
 __global__ void __launch_bounds__(32 * kM2LWarps) k_ff_m2l(KParams P, FFBuffers F, const int *gate) {
     if (gate && *gate != 0) return;
-    const int wk = blockIdx.x * kM2LWarps + (threadIdx.x >> 5);
-    if (wk >= F.ntgt) return;
-    const int L = F.tgt[wk], t = threadIdx.x & 31, np = t & 3, sl = t >> 2;
+    const int lane = threadIdx.x & 31;
+    const int wk = (blockIdx.x * kM2LWarps + (threadIdx.x >> 5)) * (32 / kM2LLanes) + lane / kM2LLanes;
+    const bool active = wk < F.ntgt;
+    const int L = active ? F.tgt[wk] : 0, t = lane % kM2LLanes, np = t & 3, sl = t >> 2;
     const TeaConst K = tea_const(P.tea_a);
     const float4 cL = F.box[2 * L], hL = F.box[2 * L + 1];
     const float3 x0 = ff_proxy(cL, hL, np), x1 = ff_proxy(cL, hL, np + 4);
@@ -1005,10 +1028,10 @@ __global__ void __launch_bounds__(32 * kM2LWarps) k_ff_m2l(KParams P, FFBuffers 
     float2 acc[12];
 #pragma unroll
     for (int c = 0; c < 12; c++) acc[c] = f2(0.f);
-    for (int k = F.far_start[L] + sl; k < F.far_start[L + 1]; k += 8) {
+    for (int k = F.far_start[L] + sl; active && k < F.far_start[L + 1]; k += kM2LSlices) {
         const int J = F.far[k];
         const float4 cJ = F.box[2 * J], hJ = F.box[2 * J + 1];
-#pragma unroll 2
+#pragma unroll
         for (int m = 0; m < 8; m++) {
             const float3 y = ff_proxy(cJ, hJ, m);
             const float2 dx = __fadd2_rn(f2(y.x), nxx), dy = __fadd2_rn(f2(y.y), nxy), dz = __fadd2_rn(f2(y.z), nxz);
@@ -1038,13 +1061,13 @@ __global__ void __launch_bounds__(32 * kM2LWarps) k_ff_m2l(KParams P, FFBuffers 
         }
     }
 #pragma unroll
-    for (int o = 4; o < 32; o <<= 1)
+    for (int o = 4; o < kM2LLanes; o <<= 1)
 #pragma unroll
         for (int c = 0; c < 12; c++) {
             acc[c].x += __shfl_xor_sync(0xffffffffu, acc[c].x, o);
             acc[c].y += __shfl_xor_sync(0xffffffffu, acc[c].y, o);
         }
-    if (sl == 0) {
+    if (active && sl == 0) {
         float *phi = reinterpret_cast<float *>(F.phi) + (size_t)96 * L;
 #pragma unroll
         for (int c = 0; c < 12; c++) {
@@ -1067,12 +1090,16 @@ struct FFTargets {
 // The packed pass of one tile: the thread's targets against the tile's bead
 // pairs; with SELF a target's own slot is pushed to r^2 = 1e30, with TRACK
 // the running minimum of r^2 per segment of the thread's pairs is kept.
+// Segment sg of a thread's pairs is exactly the tile's leaf sg, so the
+// padding leaves of a list's last tile (nleaves < kFFTileLeaves) are skipped.
+static_assert(kTeaSeg == kFFTileLeaves, "one segment per tile leaf");
 template <int SLICES, int TPT, bool SELF, bool TRACK>
-__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, FFTargets<TPT> &X, float2 vkap, float2 vn2a2,
-                                             float2 one, float (&rmin)[kTeaSeg]) {
+__device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int nleaves, FFTargets<TPT> &X, float2 vkap,
+                                             float2 vn2a2, float2 one, float (&rmin)[kTeaSeg]) {
     constexpr int kLen = kFFTileSlots / SLICES / kTeaSeg;
 #pragma unroll
     for (int sg = 0; sg < kTeaSeg; sg++) {
+        if (sg >= nleaves) break;
 #pragma unroll(kLen <= 4 ? kLen : 4)
         for (int k = 0; k < kLen; k++) {
             const int t = sl + (sg * kLen + k) * SLICES;
@@ -1106,21 +1133,19 @@ __device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, FFTargets<
     }
 }
 
-// Near pairs, far field and update: one CTA of (32 / TPT) x SLICES threads
-// per target leaf; thread lane il serves the leaf's beads il + h 32 / TPT
-// (h < TPT), the SLICES groups of lanes take interleaved bead pairs of every
-// tile of near leaves (kFFTileLeaves leaves per tile, copied asynchronously
-// one tile ahead), the two lanes of each packed operation being two source
-// beads.  Overlapping pairs (r <= 2a) get the near formula: with LISTCORR by
-// walking the bead's LJ list once, otherwise by rescanning the tile segments
-// whose running minimum of r^2 flags one, as in k_tea_step.  Then the far
-// fields of the leaf and of each ancestor with a far list are brought to the
-// leaf's proxies (L2L), summed, interpolated to the bead (L2P), and the bead
-// moves (FEFF: its effective force goes to feff instead).
-template <int SLICES, int TPT, bool FEFF, bool LISTCORR>
-__global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_step(KParams P, DevBuffers B,
-                                                                                FFBuffers F, float4 *feff,
-                                                                                const int *gate) {
+// Near pairs: one CTA of (32 / TPT) x SLICES threads per target leaf; thread
+// lane il serves the leaf's beads il + h 32 / TPT (h < TPT), the SLICES
+// groups of lanes take interleaved bead pairs of every tile of near leaves
+// (kFFTileLeaves leaves per tile, copied asynchronously one tile ahead), the
+// two lanes of each packed operation being two source beads.  Overlapping
+// pairs (r <= 2a) get the near formula: with LISTCORR by walking the bead's
+// LJ list once (while the first tile is in flight), otherwise by rescanning
+// the tile segments whose running minimum of r^2 flags one, as in
+// k_tea_step.  The bead's sum goes to FFBuffers::nearsum (k_ff_far adds the
+// far field and moves it).
+template <int SLICES, int TPT, bool LISTCORR>
+__global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_near(KParams P, DevBuffers B,
+                                                                                FFBuffers F, const int *gate) {
     if (gate && *gate != 0) return;
     constexpr int kLanes = 32 / TPT;
     const int L = blockIdx.x;
@@ -1129,9 +1154,6 @@ __global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_ste
     const int traj = F.leaf_traj[L];
     __shared__ FFTile T2[2];
     __shared__ float4 s_red[SLICES * 32];
-    __shared__ float4 s_far[kFFMaxAnc * 26];   // per ancestor: box (2), potentials (24)
-    __shared__ float s_pl[8 * 12];             // the far field at the leaf's proxies
-    __shared__ float4 s_lbox[2];
     __shared__ float4 s_x[32], s_cb[32];       // the leaf's beads: position, beta C_i
     __shared__ int s_near[kFFNearSmem];
     const float beta = B.tea_beta[traj], b2 = beta * beta;
@@ -1154,20 +1176,12 @@ __global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_ste
     const bool near_smem = nnear <= kFFNearSmem;
     if (near_smem)
         for (int k = threadIdx.x; k < nnear; k += blockDim.x) s_near[k] = near[k];
-    if (threadIdx.x < 2) s_lbox[threadIdx.x] = F.box[2 * L + threadIdx.x];
     __syncthreads();
     if (near_smem) near = s_near;
     const TeaConst K = tea_const(P.tea_a);
     const float2 vkap = f2(K.kap), vn2a2 = f2(-K.two_a2), one = f2(1.0f);
     const int ntiles = (nnear + kFFTileLeaves - 1) / kFFTileLeaves;
     ff_tile_issue(T2[0], F, near, 0, nnear);
-    // the far fields of the leaf and its ancestors (boxes, potentials) travel
-    // with the first tile
-    const int a0 = F.anc_start[L], na = min(F.anc_start[L + 1] - a0, kFFMaxAnc);
-    for (int k = threadIdx.x; k < 26 * na; k += blockDim.x) {
-        const int N = F.anc[a0 + k / 26], w = k % 26;
-        cp_async16(&s_far[k], w < 2 ? &F.box[2 * N + w] : &F.phi[24 * N + w - 2]);
-    }
     cp_async_commit();
     FFTargets<TPT> X;
     float3 corr[TPT];
@@ -1230,10 +1244,11 @@ __global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_ste
             X.self_p[h] = self_q * kFFPairSlots + (bi >> 1);
             X.self_h[h] = bi & 1;
         }
+        const int nleaves = min(kFFTileLeaves, nnear - it * kFFTileLeaves);
         if (self)
-            ff_step_tile<SLICES, TPT, true, !LISTCORR>(T, sl, X, vkap, vn2a2, one, rmin);
+            ff_step_tile<SLICES, TPT, true, !LISTCORR>(T, sl, nleaves, X, vkap, vn2a2, one, rmin);
         else
-            ff_step_tile<SLICES, TPT, false, !LISTCORR>(T, sl, X, vkap, vn2a2, one, rmin);
+            ff_step_tile<SLICES, TPT, false, !LISTCORR>(T, sl, nleaves, X, vkap, vn2a2, one, rmin);
         if (!LISTCORR) {
             constexpr int kLen = kFFTileSlots / SLICES / kTeaSeg;
             unsigned segs = 0;
@@ -1275,13 +1290,42 @@ __global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_ste
         s_red[sl * 32 + bi] = make_float4(X.ax[h].x + X.ax[h].y + corr[h].x, X.ay[h].x + X.ay[h].y + corr[h].y,
                                           X.az[h].x + X.az[h].y + corr[h].z, 0.f);
     }
-    // L2L: every ancestor's far field (trilinear over its box) at the leaf's 8
-    // proxies, one (ancestor, proxy) per thread; interpolating those on the
-    // leaf reproduces it exactly.  Then the sum over the ancestors, in order.
-    // (The tile buffers are free now: the loop ended with a barrier.)
-    static_assert(sizeof(float) * kFFMaxAnc * 96 <= sizeof(T2), "L2L partials fit in the tile buffers");
-    float *s_l2l = reinterpret_cast<float *>(T2);
-    for (int t = threadIdx.x; t < 8 * na; t += blockDim.x) {
+    __syncthreads();
+    if (threadIdx.x < n) {
+        float4 v = s_red[threadIdx.x];
+        for (int k = 1; k < SLICES; k++) {
+            const float4 u = s_red[k * 32 + threadIdx.x];
+            v.x += u.x;
+            v.y += u.y;
+            v.z += u.z;
+        }
+        F.nearsum[s0 + threadIdx.x] = v;
+    }
+}
+
+// Far field and update: one warp per leaf.  The far fields of the leaf and
+// of each ancestor with a far list are brought to the leaf's 8 proxies (L2L:
+// one (ancestor, proxy) per lane, exact because interpolating on the leaf
+// reproduces any trilinear field), summed in ancestor order, interpolated to
+// each bead (L2P), added to its near sum, and the bead moves (FEFF: its
+// effective force goes to feff instead).
+template <bool FEFF>
+__global__ void __launch_bounds__(32) k_ff_far(KParams P, DevBuffers B, FFBuffers F, float4 *feff, const int *gate) {
+    if (gate && *gate != 0) return;
+    const int L = blockIdx.x, lane = threadIdx.x;
+    const int s0 = F.leaf_start[L], n = F.leaf_start[L + 1] - s0;
+    __shared__ float4 s_far[kFFMaxAnc * 26];   // per ancestor: box (2), potentials (24)
+    __shared__ float s_l2l[kFFMaxAnc * 96];    // per ancestor: its far field at the leaf's proxies
+    __shared__ float s_pl[8 * 12];             // the far field at the leaf's proxies
+    __shared__ float4 s_lbox[2];
+    const int a0 = F.anc_start[L], na = min(F.anc_start[L + 1] - a0, kFFMaxAnc);
+    for (int k = lane; k < 26 * na; k += 32) {
+        const int N = F.anc[a0 + k / 26], w = k % 26;
+        s_far[k] = w < 2 ? F.box[2 * N + w] : F.phi[24 * N + w - 2];
+    }
+    if (lane < 2) s_lbox[lane] = F.box[2 * L + lane];
+    __syncwarp();
+    for (int t = lane; t < 8 * na; t += 32) {
         const int A = t >> 3, pn = t & 7;
         const float4 *fr = s_far + 26 * A;
         const float *ph = reinterpret_cast<const float *>(fr + 2);
@@ -1295,24 +1339,23 @@ __global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_ste
             s_l2l[96 * A + 12 * pn + c] = v;
         }
     }
-    __syncthreads();
-    for (int t = threadIdx.x; t < 96 && na > 0; t += blockDim.x) {
+    __syncwarp();
+    for (int t = lane; t < 96; t += 32) {
         float v = 0.f;
         for (int A = 0; A < na; A++) v += s_l2l[96 * A + t];
         s_pl[t] = v;
     }
-    __syncthreads();
-    const int bi = threadIdx.x;
-    if (bi >= n) return;
-    const int g = F.leaf_bead[s0 + bi];
-    const float3 xi = f3(s_x[bi]), cbi = f3(s_cb[bi]);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    for (int k = 0; k < SLICES; k++) {
-        const float4 v = s_red[k * 32 + bi];
-        sx += v.x;
-        sy += v.y;
-        sz += v.z;
-    }
+    __syncwarp();
+    if (lane >= n) return;
+    const int g = F.leaf_bead[s0 + lane];
+    const int traj = F.leaf_traj[L];
+    const float beta = B.tea_beta[traj], b2 = beta * beta;
+    const float3 xi = f3(B.frame_in[g]);
+    const float4 ci = B.tea_ci[g];
+    const float3 cbi = make_float3(beta / sqrtf(1.0f + b2 * ci.x), beta / sqrtf(1.0f + b2 * ci.y),
+                                   beta / sqrtf(1.0f + b2 * ci.z));
+    const float4 ns = F.nearsum[s0 + lane];
+    float sx = ns.x, sy = ns.y, sz = ns.z;
     if (na > 0) {   // L2P from the leaf's proxies
         float w[8];
         ff_weights(xi, s_lbox[0], s_lbox[1], w);
@@ -1328,7 +1371,7 @@ __global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_ste
             sz = fmaf(w[m], uz, sz);
         }
     }
-    tea_bead_update<FEFF>(P, B, g, sx, sy, sz, b2, K, feff);
+    tea_bead_update<FEFF>(P, B, g, sx, sy, sz, b2, tea_const(P.tea_a), feff);
 }
 
 // Beads in no leaf (extra beads): the update draws their angular noise and
@@ -1343,12 +1386,21 @@ __global__ void k_ff_rest(KParams P, DevBuffers B, FFBuffers F, float4 *feff, co
     tea_bead_update<FEFF>(P, B, g, 0.f, 0.f, 0.f, beta * beta, tea_const(P.tea_a), feff);
 }
 
-void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s) {
+void launch_ff_p2m_leaves(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate,
+                          cudaStream_t s) {
     if (F.nleaf == 0) return;
     k_ff_p2m<<<(F.nleaf + kP2MWarps) / kP2MWarps, 32 * kP2MWarps, 0, s>>>(P, B, F, gate);
+}
+void launch_ff_m2l(const KParams &P, const FFBuffers &F, const int *gate, cudaStream_t s) {
+    if (F.nleaf == 0) return;
     if (F.ninner > 0)
         k_ff_p2m_inner<<<(F.ninner + kP2MWarps - 1) / kP2MWarps, 32 * kP2MWarps, 0, s>>>(P, F, gate);
-    if (F.ntgt > 0) k_ff_m2l<<<(F.ntgt + kM2LWarps - 1) / kM2LWarps, 32 * kM2LWarps, 0, s>>>(P, F, gate);
+    constexpr int per_block = kM2LWarps * (32 / kM2LLanes);
+    if (F.ntgt > 0) k_ff_m2l<<<(F.ntgt + per_block - 1) / per_block, 32 * kM2LWarps, 0, s>>>(P, F, gate);
+}
+void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s) {
+    launch_ff_p2m_leaves(P, B, F, gate, s);
+    launch_ff_m2l(P, F, gate, s);
 }
 
 // Overlapping pairs can be taken from the LJ list when it holds every pair
@@ -1359,34 +1411,43 @@ static bool ff_list_corr(const KParams &P) { return P.lj_on && P.ljcut >= 2.0f *
 #define FF_TPT 1
 #endif
 constexpr int kFFTPT = FF_TPT;   // target beads per thread of the far-field step
-template <int SL, bool FEFF>
-static void ff_step_launch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff, const int *gate,
+template <int SL>
+static void ff_near_launch(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate,
                            cudaStream_t s) {
     constexpr int threads = 32 / kFFTPT * SL;
-    if (F.nleaf > 0) {
-        if (ff_list_corr(P))
-            k_ff_step<SL, kFFTPT, FEFF, true><<<F.nleaf, threads, 0, s>>>(P, B, F, feff, gate);
-        else
-            k_ff_step<SL, kFFTPT, FEFF, false><<<F.nleaf, threads, 0, s>>>(P, B, F, feff, gate);
-    }
-    if (F.nrest > 0) k_ff_rest<FEFF><<<(F.nrest + 127) / 128, 128, 0, s>>>(P, B, F, feff, gate);
+    if (F.nleaf == 0) return;
+    if (ff_list_corr(P))
+        k_ff_near<SL, kFFTPT, true><<<F.nleaf, threads, 0, s>>>(P, B, F, gate);
+    else
+        k_ff_near<SL, kFFTPT, false><<<F.nleaf, threads, 0, s>>>(P, B, F, gate);
 }
-template <bool FEFF>
-static void ff_step_dispatch(const KParams &P, const DevBuffers &B, const FFBuffers &F, float4 *feff,
-                             const int *gate, cudaStream_t s) {
+void launch_ff_near(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s) {
     switch (P.tea_slices) {
         case 1:
-        case 2: ff_step_launch<2, FEFF>(P, B, F, feff, gate, s); break;
-        case 4: ff_step_launch<4, FEFF>(P, B, F, feff, gate, s); break;
-        default: ff_step_launch<8, FEFF>(P, B, F, feff, gate, s); break;
+        case 2: ff_near_launch<2>(P, B, F, gate, s); break;
+        case 4: ff_near_launch<4>(P, B, F, gate, s); break;
+        default: ff_near_launch<8>(P, B, F, gate, s); break;
+    }
+}
+void launch_ff_far(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,
+                   const int *gate, cudaStream_t s) {
+    if (F.nleaf > 0) {
+        if (feff_only)
+            k_ff_far<true><<<F.nleaf, 32, 0, s>>>(P, B, F, feff, gate);
+        else
+            k_ff_far<false><<<F.nleaf, 32, 0, s>>>(P, B, F, feff, gate);
+    }
+    if (F.nrest > 0) {
+        if (feff_only)
+            k_ff_rest<true><<<(F.nrest + 127) / 128, 128, 0, s>>>(P, B, F, feff, gate);
+        else
+            k_ff_rest<false><<<(F.nrest + 127) / 128, 128, 0, s>>>(P, B, F, feff, gate);
     }
 }
 void launch_ff_step(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,
                     const int *gate, cudaStream_t s) {
-    if (feff_only)
-        ff_step_dispatch<true>(P, B, F, feff, gate, s);
-    else
-        ff_step_dispatch<false>(P, B, F, feff, gate, s);
+    launch_ff_near(P, B, F, gate, s);
+    launch_ff_far(P, B, F, feff_only, feff, gate, s);
 }
 
 }  // namespace mtg

@@ -276,6 +276,52 @@ void timed_launch(mtg_engine *e, int kind, F &&launch) {
 
 // Enqueues one step of the loop of compute() (src/compute_cuda.cu:1137-1238)
 // minus its host I/O.
+// Sets the condition of a graph's conditional node from the fall-back flag.
+__global__ void k_gate_condition(cudaGraphConditionalHandle h, const int *gate) {
+    cudaGraphSetConditional(h, *gate == 1 ? 1u : 0u);
+}
+
+// Inside the capture of a step graph: the exact mobility product as the body
+// of a conditional node that runs only after a fall-back (the flag is read
+// on the device by a one-thread kernel), in place of a full-grid launch whose
+// blocks read the flag and return.  Returns false, with nothing added to the
+// graph, when the node cannot be set up (the caller then uses the gated
+// launch).
+static bool capture_exact_fallback(mtg_engine *e) {
+    if (!e->body) return false;
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *ed = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(e->stream, &st, nullptr, &g, &deps, &ed, &nd) != cudaSuccess ||
+        st != cudaStreamCaptureStatusActive)
+        return false;
+    cudaGraphConditionalHandle h;
+    if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return false;
+    k_gate_condition<<<1, 1, 0, e->stream>>>(h, e->surr_gate);
+    if (cudaStreamGetCaptureInfo(e->stream, &st, nullptr, &g, &deps, &ed, &nd) != cudaSuccess) return false;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, deps, ed, nd, &np) != cudaSuccess) return false;
+    // from here on a failure leaves the capture invalid; it is reported when
+    // the capture ends
+    cudaStreamUpdateCaptureDependencies(e->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    if (cudaStreamBeginCaptureToGraph(e->body, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+        cudaSuccess) {
+        e->capture_failed = true;   // an empty body would skip the exact product: fail the capture
+        return true;
+    }
+    launch_tea_step(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->body);
+    if (cudaStreamEndCapture(e->body, &body) != cudaSuccess) e->capture_failed = true;
+    return true;
+}
+
 void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
     const mtg_params &p = e->p;
     if (allow_rebuild && step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
@@ -284,15 +330,37 @@ void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
     }
     if (p.hdi_on) {
         timed_launch(e, 2, [&] { launch_forces(e->kp, e->bufs(), true, e->stream); });
-        // learned TEA with the far field: proxies of this step's F and R
+        // learned TEA with the far field: proxies of this step's F and R.
+        // Without per-kernel timing the inner proxies and M2L run on the
+        // second stream beside the network and the near pairs, and join
+        // before the first kernel that reads the far potentials.
         const bool ff = e->surr && e->ff_on;
-        if (ff) timed_launch(e, 8, [&] { launch_ff_proxies(e->kp, e->bufs(), e->ffb, e->surr_gate, e->stream); });
+        const bool fork = ff && !e->timing && e->side;
+        bool joined = true;
+        auto join = [&] {
+            if (!joined) {
+                cudaEventRecord(e->ev_join, e->side);
+                cudaStreamWaitEvent(e->stream, e->ev_join, 0);
+                joined = true;
+            }
+        };
+        if (fork) {
+            launch_ff_p2m_leaves(e->kp, e->bufs(), e->ffb, e->surr_gate, e->stream);
+            cudaEventRecord(e->ev_fork, e->stream);
+            cudaStreamWaitEvent(e->side, e->ev_fork, 0);
+            launch_ff_m2l(e->kp, e->ffb, e->surr_gate, e->side);
+            joined = false;
+        } else if (ff) {
+            timed_launch(e, 8, [&] { launch_ff_proxies(e->kp, e->bufs(), e->ffb, e->surr_gate, e->stream); });
+        }
         if (e->surr) {
             // learned TEA: the network replaces the epsilon pass; the exact
             // re-check decides whether it stays in charge
             if (step % p.tea_epsilon_freq == 0) timed_launch(e, 6, [&] { enqueue_surrogate_eps(e); });
-            if (e->surr_recheck > 0 && step % e->surr_recheck == 0)
+            if (e->surr_recheck > 0 && step % e->surr_recheck == 0) {
+                join();
                 timed_launch(e, 7, [&] { enqueue_surrogate_recheck(e); });
+            }
         } else if (step % p.tea_epsilon_freq == 0) {
             timed_launch(e, 3, [&] { launch_tea_eps(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
             timed_launch(e, 4, [&] { launch_tea_beta(e->kp, e->bufs(), p.tea_capricious, p.tea_epsmax, e->stream); });
@@ -301,11 +369,14 @@ void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
             // the far-field product while the surrogate is in charge, the exact
             // one after a fall-back (each gated on the fall-back flag)
             timed_launch(e, 9, [&] {
-                launch_ff_step(e->kp, e->bufs(), e->ffb, false, nullptr, e->surr_gate, e->stream);
+                launch_ff_near(e->kp, e->bufs(), e->ffb, e->surr_gate, e->stream);
+                join();
+                launch_ff_far(e->kp, e->bufs(), e->ffb, false, nullptr, e->surr_gate, e->stream);
             });
-            timed_launch(e, 5, [&] {
-                launch_tea_step_gated(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->surr_gate, e->stream);
-            });
+            if (!(e->capturing && !e->timing && capture_exact_fallback(e)))
+                timed_launch(e, 5, [&] {
+                    launch_tea_step_gated(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->surr_gate, e->stream);
+                });
         } else {
             timed_launch(e, 5, [&] { launch_tea_step(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
         }
@@ -683,6 +754,10 @@ int mtg_destroy(mtg_engine *e) {
     if (e->call_a) cudaEventDestroy(e->call_a);
     if (e->call_b) cudaEventDestroy(e->call_b);
     if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->side) cudaStreamDestroy(e->side);
+    if (e->body) cudaStreamDestroy(e->body);
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
     delete e;
     return MTG_OK;
 }
@@ -896,6 +971,7 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
                 }
                 cudaGraph_t g;
                 e->capturing = true;
+                e->capture_failed = false;
                 cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
                 if (ce == cudaSuccess) {
                     if (period_active(e)) {
@@ -913,6 +989,10 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
                 }
                 e->capturing = false;
                 if (ce != cudaSuccess) return fail(MTG_E_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+                if (e->capture_failed) {
+                    cudaGraphDestroy(g);
+                    return fail(MTG_E_CUDA, "graph capture failed: a conditional node body could not be recorded");
+                }
                 if (e->timing) e->graph_slot_count[cur0] = e->capture_next - e->graph_slot_base[cur0];
                 e->cur = cur0;
                 e->graph_kernels[cur0] = count_kernel_nodes(g);

@@ -331,15 +331,27 @@ struct FFBuffers {
     float4 *phi;             // [24*nnode] target proxy n: (A.xyz, B0.x), (B0.yz, B1.xy), (B1.z, B2.xyz) at 24N+3n
     float4 *pack;            // [(nleaf+1)*kFFPackF4] each leaf's beads in the tile layout of the step kernel
                              // (leaf nleaf: padding, far away with zero F and R), written every step by P2M
+    float4 *nearsum;         // [leaf beads] each bead's near-pair sum, in leaf bead order
 };
 // float4 per leaf of FFBuffers::pack, for the bead pairs (2p, 2p+1):
 // xa xb ya yb | za zb Fxa Fxb | Fya Fyb Fza Fzb | Rxa Rxb Rya Ryb (kFFLeaf / 2
 // each), then Rza Rzb of two pairs per float4 (kFFLeaf / 4)
 constexpr int kFFPairSlots = kFFLeaf / 2;
 constexpr int kFFPackF4 = 4 * kFFPairSlots + kFFPairSlots / 2;
-// proxies (P2M) and far-field potentials at target proxies (M2L), while *gate == 0
+// All of the kernels below run while *gate == 0.
+// leaf proxies (P2M of the leaves, and their packed beads)
+void launch_ff_p2m_leaves(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate,
+                          cudaStream_t s);
+// inner-node proxies and far-field potentials at target proxies (M2L); needs the leaf proxies
+void launch_ff_m2l(const KParams &P, const FFBuffers &F, const int *gate, cudaStream_t s);
+// both of the above
 void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s);
-// near pairs + interpolated far field + update (FEFF: effective forces into feff, no update), while *gate == 0
+// near-pair sums; needs the leaf proxies' packed beads
+void launch_ff_near(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate, cudaStream_t s);
+// far field + update (FEFF: effective forces into feff, no update); needs the near sums and M2L
+void launch_ff_far(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,
+                   const int *gate, cudaStream_t s);
+// near + far
 void launch_ff_step(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,
                     const int *gate, cudaStream_t s);
 // the exact mobility product + update, only while *gate == 1 (after a fall-back to exact TEA)

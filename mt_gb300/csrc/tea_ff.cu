@@ -284,7 +284,7 @@ static int ff_build(mtg_engine *e) {
     size_t nints = 0;
     for (auto *v : parts) nints += v->size() + 1;
     const size_t nn1 = (size_t)std::max(nnode, 1);
-    const size_t nf4 = (size_t)(2 + 16 + 24) * nn1 + (size_t)kFFPackF4 * (nleaf + 1);
+    const size_t nf4 = (size_t)(2 + 16 + 24) * nn1 + (size_t)kFFPackF4 * (nleaf + 1) + P.leaf_bead.size();
     if (nints > e->ff_ints_cap) {
         if (e->ff_ints) cudaFree(e->ff_ints);
         e->ff_ints = nullptr;
@@ -332,6 +332,7 @@ static int ff_build(mtg_engine *e) {
     F.q = e->ff_f4 + 2 * nn1;
     F.phi = e->ff_f4 + 18 * nn1;
     F.pack = e->ff_f4 + 42 * nn1;
+    F.nearsum = F.pack + (size_t)kFFPackF4 * (nleaf + 1);
     e->ff_near_pairs = P.near_pairs;
     e->ff_proxy_pairs = P.proxy_pairs;
     e->ff_sizes[0] = nleaf;
@@ -368,6 +369,10 @@ int mtg_set_tea_farfield(mtg_engine *e, int on, float theta, int refresh_every) 
     if (!e->ff_on) return MTG_OK;
     e->ff_theta = theta;
     e->ff_refresh = refresh_every;
+    if (!e->side) FCK(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
+    if (!e->body) FCK(cudaStreamCreateWithFlags(&e->body, cudaStreamNonBlocking));
+    if (!e->ev_fork) FCK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+    if (!e->ev_join) FCK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
     return ff_build(e);
 }
 
