@@ -172,6 +172,12 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the first sample before the timed region starts (nvidia-smi takes
+            # a moment to come up), so that short regions are covered too
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.first = len(self.lines)
         except (OSError, FileNotFoundError):
             self.proc = None
 
@@ -182,6 +188,10 @@ class ClockSampler:
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        # one sample at or after the end of the timed region (200 ms period)
+        n0, t0 = len(self.lines), time.time()
+        while len(self.lines) == n0 and time.time() - t0 < 0.5 and self.proc.poll() is None:
+            time.sleep(0.01)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)

@@ -276,52 +276,6 @@ void timed_launch(mtg_engine *e, int kind, F &&launch) {
 
 // Enqueues one step of the loop of compute() (src/compute_cuda.cu:1137-1238)
 // minus its host I/O.
-// Sets the condition of a graph's conditional node from the fall-back flag.
-__global__ void k_gate_condition(cudaGraphConditionalHandle h, const int *gate) {
-    cudaGraphSetConditional(h, *gate == 1 ? 1u : 0u);
-}
-
-// Inside the capture of a step graph: the exact mobility product as the body
-// of a conditional node that runs only after a fall-back (the flag is read
-// on the device by a one-thread kernel), in place of a full-grid launch whose
-// blocks read the flag and return.  Returns false, with nothing added to the
-// graph, when the node cannot be set up (the caller then uses the gated
-// launch).
-static bool capture_exact_fallback(mtg_engine *e) {
-    if (!e->body) return false;
-    cudaStreamCaptureStatus st;
-    cudaGraph_t g;
-    const cudaGraphNode_t *deps = nullptr;
-    const cudaGraphEdgeData *ed = nullptr;
-    size_t nd = 0;
-    if (cudaStreamGetCaptureInfo(e->stream, &st, nullptr, &g, &deps, &ed, &nd) != cudaSuccess ||
-        st != cudaStreamCaptureStatusActive)
-        return false;
-    cudaGraphConditionalHandle h;
-    if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return false;
-    k_gate_condition<<<1, 1, 0, e->stream>>>(h, e->surr_gate);
-    if (cudaStreamGetCaptureInfo(e->stream, &st, nullptr, &g, &deps, &ed, &nd) != cudaSuccess) return false;
-    cudaGraphNodeParams np = {};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeIf;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    if (cudaGraphAddNode(&node, g, deps, ed, nd, &np) != cudaSuccess) return false;
-    // from here on a failure leaves the capture invalid; it is reported when
-    // the capture ends
-    cudaStreamUpdateCaptureDependencies(e->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-    cudaGraph_t body = np.conditional.phGraph_out[0];
-    if (cudaStreamBeginCaptureToGraph(e->body, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
-        cudaSuccess) {
-        e->capture_failed = true;   // an empty body would skip the exact product: fail the capture
-        return true;
-    }
-    launch_tea_step(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->body);
-    if (cudaStreamEndCapture(e->body, &body) != cudaSuccess) e->capture_failed = true;
-    return true;
-}
-
 void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
     const mtg_params &p = e->p;
     if (allow_rebuild && step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
@@ -373,10 +327,9 @@ void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
                 join();
                 launch_ff_far(e->kp, e->bufs(), e->ffb, false, nullptr, e->surr_gate, e->stream);
             });
-            if (!(e->capturing && !e->timing && capture_exact_fallback(e)))
-                timed_launch(e, 5, [&] {
-                    launch_tea_step_gated(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->surr_gate, e->stream);
-                });
+            timed_launch(e, 5, [&] {
+                launch_tea_step_gated(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->surr_gate, e->stream);
+            });
         } else {
             timed_launch(e, 5, [&] { launch_tea_step(e->kp, e->bufs(), e->tea_work, e->tea_nwork, e->stream); });
         }
@@ -755,7 +708,6 @@ int mtg_destroy(mtg_engine *e) {
     if (e->call_b) cudaEventDestroy(e->call_b);
     if (e->stream) cudaStreamDestroy(e->stream);
     if (e->side) cudaStreamDestroy(e->side);
-    if (e->body) cudaStreamDestroy(e->body);
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     delete e;
@@ -971,7 +923,6 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
                 }
                 cudaGraph_t g;
                 e->capturing = true;
-                e->capture_failed = false;
                 cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
                 if (ce == cudaSuccess) {
                     if (period_active(e)) {
@@ -989,10 +940,6 @@ static int enqueue_range(mtg_engine *e, long long first_step, int nsteps) {
                 }
                 e->capturing = false;
                 if (ce != cudaSuccess) return fail(MTG_E_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
-                if (e->capture_failed) {
-                    cudaGraphDestroy(g);
-                    return fail(MTG_E_CUDA, "graph capture failed: a conditional node body could not be recorded");
-                }
                 if (e->timing) e->graph_slot_count[cur0] = e->capture_next - e->graph_slot_base[cur0];
                 e->cur = cur0;
                 e->graph_kernels[cur0] = count_kernel_nodes(g);

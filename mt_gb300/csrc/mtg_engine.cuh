@@ -20,7 +20,6 @@ struct mtg_engine {
     bool lists_fresh = false;   // mtg_rebuild_pairs ran after the last step
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;   // second stream of the learned step (M2L)
-    cudaStream_t body = nullptr;   // captures the bodies of conditional graph nodes
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<int> h_off;
     // device
@@ -58,7 +57,6 @@ struct mtg_engine {
     int graph_slot_base[2] = {0, 0}, graph_slot_count[2] = {0, 0};
     int direct_base = 0, direct_next = 0, capture_next = 0;
     bool capturing = false;
-    bool capture_failed = false;   // a part of the graph under capture could not be recorded
     std::vector<int> used_slots;
     double kt_total[MTG_KERNEL_KINDS] = {0};
     long long kt_count[MTG_KERNEL_KINDS] = {0};

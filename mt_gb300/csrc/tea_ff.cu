@@ -370,7 +370,6 @@ int mtg_set_tea_farfield(mtg_engine *e, int on, float theta, int refresh_every) 
     e->ff_theta = theta;
     e->ff_refresh = refresh_every;
     if (!e->side) FCK(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
-    if (!e->body) FCK(cudaStreamCreateWithFlags(&e->body, cudaStreamNonBlocking));
     if (!e->ev_fork) FCK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
     if (!e->ev_join) FCK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
     return ff_build(e);
