@@ -816,8 +816,8 @@ def run_tea_compare(args, spec, dist):
     learned_ok = not L["status"]["fell_back"]
     ffs = L["farfield"]
     roof_exact = fp32_roof(X["kt"], "tea_step", "k_tea_step", 45.0 * tea_pairs(b), "45 FLOP per ordered pair")
-    roof_ff = fp32_roof(L["kt"], "ff_step", "k_ff_step", 45.0 * ffs["near_pairs"],
-                        "45 FLOP per ordered near pair (the pair loop; interpolation and update not counted)")
+    roof_ff = fp32_roof(L["kt"], "ff_near", "k_ff_near", 45.0 * ffs["near_pairs"],
+                        "45 FLOP per ordered near pair (the pair loop of k_ff_near; its list walk not counted)")
     out = None
     if dist.rank == 0:
         cpu = cpu_sample(dict(spec, kind="tea"), seed, single_core=True) if dist.ws == 1 and not args.no_cpu_baseline else None
@@ -956,16 +956,16 @@ def run_stride(args, spec, dist):
 # Small cases of the hot kernels for one-kernel ncu captures (`--profile-case`):
 # each builds its system, runs a few warm-up launches and then `launches`
 # launches of the kernel named, and prints one JSON line.  The command that
-# captures one launch of, e.g., k_ff_step:
-#   ncu --set full --clock-control none -k regex:k_ff_step -s 4 -c 1 -o prof \
-#       python bench.py --profile-case ff_step
+# captures one launch of, e.g., k_ff_near:
+#   ncu --set full --clock-control none -k regex:k_ff_near -s 4 -c 1 -o prof \
+#       python bench.py --profile-case ff_near
 # Sizes are those of the workloads (one list period of steps, trajectories
 # cut to keep a case at a few hundred MB on the device).
 PROFILE_CASES = {
     # 16 of the 64 x 5600 learned-workload trajectories; untrained network
     # (the kernels' work does not depend on the weights), far field at the
     # workload's theta, no re-check
-    "ff_step": dict(workload="tea_learned_vs_exact_64x5600", ntraj=16, steps=10),
+    "ff_near": dict(workload="tea_learned_vs_exact_64x5600", ntraj=16, steps=10),
     "tea_step": dict(workload="tea_exact_64x5600", ntraj=16, steps=10),
     "step_plain": dict(workload="ragged_1024", ntraj=None, steps=10),
     "step_period": dict(workload="single_156", ntraj=None, steps=100),
@@ -987,7 +987,7 @@ def run_profile_case(name: str):
     out = {"profile_case": name, "workload": c["workload"], "trajectories": b.ntraj, "beads": b.nbeads}
     with eng.Engine(b) as e:
         e.upload_state(b.coords)
-        if name in ("ff_step", "mlp_infer", "mlp_backward"):
+        if name in ("ff_near", "mlp_infer", "mlp_backward"):
             X, T = e.tea_training_data()
             s = eng.Surrogate(seed=1)
             if name == "mlp_backward":

@@ -468,10 +468,11 @@ int mtg_step_timed(mtg_engine *e, long long first_step, int nsteps, float *devic
  * Kinds: 0 pair-list rebuild, 1 fused plain step, 2 forces (+ TEA random
  * forces), 3 TEA epsilon pass, 4 TEA beta reduction, 5 TEA mobility step,
  * 6 learned-TEA descriptors + network + C_i/beta, 7 learned-TEA re-check,
- * 8 far-field proxies (charges and far potentials), 9 far-field mobility step,
+ * 8 far-field proxies (charges and far potentials), 9 far-field near pairs,
  * 10 persistent run of plain steps (one launch covers the steps between two
- * pair-list rebuilds). */
-#define MTG_KERNEL_KINDS 11
+ * pair-list rebuilds), 11 far-field interpolation + update.  With timing on,
+ * the learned step's kernels run on one stream, one after another. */
+#define MTG_KERNEL_KINDS 12
 int mtg_set_kernel_timing(mtg_engine *e, int on);
 int mtg_kernel_times(mtg_engine *e, double *total_ms, long long *launches, int reset);
 /* Kernel launches replayed from the engine's step graphs since the last

@@ -322,9 +322,9 @@ void enqueue_step(mtg_engine *e, long long step, bool allow_rebuild = true) {
         if (ff) {
             // the far-field product while the surrogate is in charge, the exact
             // one after a fall-back (each gated on the fall-back flag)
-            timed_launch(e, 9, [&] {
-                launch_ff_near(e->kp, e->bufs(), e->ffb, e->surr_gate, e->stream);
-                join();
+            timed_launch(e, 9, [&] { launch_ff_near(e->kp, e->bufs(), e->ffb, e->surr_gate, e->stream); });
+            join();
+            timed_launch(e, 11, [&] {
                 launch_ff_far(e->kp, e->bufs(), e->ffb, false, nullptr, e->surr_gate, e->stream);
             });
             timed_launch(e, 5, [&] {

@@ -98,7 +98,7 @@ SURROGATE_OUTPUTS = 4
 SURROGATE_PARAMS = 37764
 
 KERNEL_KINDS = ("rebuild", "step_plain", "forces", "tea_eps", "tea_beta", "tea_step", "surrogate", "recheck",
-                "ff_proxies", "ff_step", "step_period")
+                "ff_proxies", "ff_near", "step_period", "ff_far")
 
 _lib = None
 

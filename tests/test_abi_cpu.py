@@ -81,3 +81,11 @@ def test_empty_trajectory_rejected(engine_mod):
     b = synth.batch_from_trajectories(p, trajs)
     with pytest.raises(engine_mod.MtgError, match="MTG_E_CONFIG"):
         engine_mod.Engine(b)
+
+
+def test_kernel_kinds_match_header(engine_mod):
+    """The Python names of the per-kernel timing kinds cover MTG_KERNEL_KINDS."""
+    src = open(os.path.join(ROOT, "include", "mtg.h")).read()
+    n = int(re.search(r"#define\s+MTG_KERNEL_KINDS\s+(\d+)", src).group(1))
+    assert len(engine_mod.KERNEL_KINDS) == n
+    assert len(set(engine_mod.KERNEL_KINDS)) == n

@@ -101,7 +101,8 @@ def test_learned_mode_with_farfield_runs_and_rechecks(engine_mod):
     # a network trained on 20-monomer systems, run on 60-monomer ones: the
     # bench measures the accuracy of a network trained for its workload
     assert np.isfinite(st["last_error"]) and st["last_error"] < 0.1, st
-    assert kt["ff_step"][1] >= 10 and kt["ff_proxies"][1] >= 10 and kt["tea_step"][0] < kt["ff_step"][0]
+    assert kt["ff_near"][1] >= 10 and kt["ff_far"][1] >= 10 and kt["ff_proxies"][1] >= 10
+    assert kt["tea_step"][0] < kt["ff_near"][0]
     x = e.download_state()
     assert np.all(np.isfinite(x))
     extra = b.extra.astype(bool)
