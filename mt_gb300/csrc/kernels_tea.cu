@@ -1314,11 +1314,14 @@ __global__ void __launch_bounds__(32) k_ff_far(KParams P, DevBuffers B, FFBuffer
     if (gate && *gate != 0) return;
     const int L = blockIdx.x, lane = threadIdx.x;
     const int s0 = F.leaf_start[L], n = F.leaf_start[L + 1] - s0;
-    __shared__ float4 s_far[kFFMaxAnc * 26];   // per ancestor: box (2), potentials (24)
-    __shared__ float s_l2l[kFFMaxAnc * 96];    // per ancestor: its far field at the leaf's proxies
+    // per ancestor: box (2) and potentials (24), then its far field at the
+    // leaf's proxies; sized for the tree's longest ancestor list (max_anc)
+    extern __shared__ float4 s_dyn[];
+    float4 *s_far = s_dyn;
+    float *s_l2l = reinterpret_cast<float *>(s_dyn + 26 * F.max_anc);
     __shared__ float s_pl[8 * 12];             // the far field at the leaf's proxies
     __shared__ float4 s_lbox[2];
-    const int a0 = F.anc_start[L], na = min(F.anc_start[L + 1] - a0, kFFMaxAnc);
+    const int a0 = F.anc_start[L], na = min(F.anc_start[L + 1] - a0, F.max_anc);
     for (int k = lane; k < 26 * na; k += 32) {
         const int N = F.anc[a0 + k / 26], w = k % 26;
         s_far[k] = w < 2 ? F.box[2 * N + w] : F.phi[24 * N + w - 2];
@@ -1432,10 +1435,11 @@ void launch_ff_near(const KParams &P, const DevBuffers &B, const FFBuffers &F, c
 void launch_ff_far(const KParams &P, const DevBuffers &B, const FFBuffers &F, bool feff_only, float4 *feff,
                    const int *gate, cudaStream_t s) {
     if (F.nleaf > 0) {
+        const size_t smem = (size_t)F.max_anc * (26 * sizeof(float4) + 96 * sizeof(float));
         if (feff_only)
-            k_ff_far<true><<<F.nleaf, 32, 0, s>>>(P, B, F, feff, gate);
+            k_ff_far<true><<<F.nleaf, 32, smem, s>>>(P, B, F, feff, gate);
         else
-            k_ff_far<false><<<F.nleaf, 32, 0, s>>>(P, B, F, feff, gate);
+            k_ff_far<false><<<F.nleaf, 32, smem, s>>>(P, B, F, feff, gate);
     }
     if (F.nrest > 0) {
         if (feff_only)

@@ -312,6 +312,7 @@ constexpr float kFFNode = 0.70710678f;
 constexpr int kFFMaxAnc = 16;          // nodes with far fields on a leaf's path to the root (tree depth bound)
 struct FFBuffers {
     int nleaf, nnode, ntgt, ninner, nrest;
+    int max_anc;             // the longest ancestor list of a leaf (at most kFFMaxAnc)
     const int *leaf_start;   // [nleaf+1] into leaf_bead
     const int *leaf_bead;    // beads of every leaf, leaf after leaf (every node a contiguous range)
     const int *leaf_traj;    // [nleaf]

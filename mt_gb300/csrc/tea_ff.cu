@@ -273,9 +273,10 @@ static int ff_build(mtg_engine *e) {
     std::vector<int> inner;
     for (int N = nleaf; N < nnode; N++)
         if (used[N]) inner.push_back(N);
-    for (int L = 0; L < nleaf; L++)
-        if (P.anc_start[L + 1] - P.anc_start[L] > kFFMaxAnc)
-            return mtg_internal_fail(MTG_E_CONFIG, "far-field tree deeper than the step kernel's ancestor limit");
+    int max_anc = 0;
+    for (int L = 0; L < nleaf; L++) max_anc = std::max(max_anc, P.anc_start[L + 1] - P.anc_start[L]);
+    if (max_anc > kFFMaxAnc)
+        return mtg_internal_fail(MTG_E_CONFIG, "far-field tree deeper than the step kernel's ancestor limit");
     enum { kLeafStart, kLeafBead, kLeafTraj, kNearStart, kNear, kNodeRange, kNodeLeaves, kFarStart, kFar, kTgt,
            kInner, kAncStart, kAnc, kRest, kParts };
     const std::vector<int> *parts[kParts] = {&P.leaf_start, &P.leaf_bead, &P.leaf_traj, &P.near_start, &P.near,
@@ -314,6 +315,7 @@ static int ff_build(mtg_engine *e) {
     F.ntgt = (int)P.tgt.size();
     F.ninner = (int)inner.size();
     F.nrest = (int)P.rest.size();
+    F.max_anc = max_anc;
     F.leaf_start = dev[kLeafStart];
     F.leaf_bead = dev[kLeafBead];
     F.leaf_traj = dev[kLeafTraj];
