@@ -11,11 +11,6 @@
 
 namespace mtg {
 
-// Site offsets are at most |p1| ~ 2 nm from the centre, so a site distance
-// below 2.5 nm needs a centre distance below 2.5 + 2 + 2 = 6.5 nm; 6.6 nm
-// leaves room for rounding.
-constexpr float kPairPrefilter = 6.6f;
-
 __device__ __forceinline__ void block_box(float3 p, bool valid, float *sbox /*[6]*/, float *scratch /*[2*6*warps]*/) {
     float v[6] = {valid ? p.x : 3.0e38f, valid ? p.y : 3.0e38f, valid ? p.z : 3.0e38f,
                   valid ? p.x : -3.0e38f, valid ? p.y : -3.0e38f, valid ? p.z : -3.0e38f};
@@ -67,15 +62,8 @@ __global__ void __launch_bounds__(kTile) k_rebuild(KParams P, DevBuffers B, cons
         flags = B.flags[g];
         h0 = B.harm[g * P.maxH];
     }
-    const bool extra_i = (flags & kFlagExtra) != 0;
-    const int il = g - base;
-    // pairs_kernel reads harmonic[max*i] even without a partner (-1 fill):
-    // < 0 -> R_MON = -r_mon and |.| is excluded (src/compute_cuda.cu:548,565,599)
-    const float rmon = h0 < 0 ? -2.0f : 2.0f;
-    const int hpart = h0 < 0 ? -h0 : h0;
-    const float3 wi = make_float3(ui.x * rmon, ui.y * rmon, ui.z * rmon);
-    const bool do_pairs = P.is_assembly && valid && !extra_i;
-    const bool do_lj = P.lj_on && valid && !extra_i;
+    const ListSite I = list_site(P, pi, ui, li1, li2, flags, g - base, h0);
+    const bool do_lj = valid && I.do_lj, do_pairs = valid && I.do_pairs;
     const float reach = fmaxf(P.lj_on ? P.ljcut : 0.f, P.is_assembly ? kPairPrefilter : 0.f);
 
     block_box(f3(pi), valid, s_box_i, s_scr);
@@ -102,47 +90,8 @@ __global__ void __launch_bounds__(kTile) k_rebuild(KParams P, DevBuffers B, cons
             const int n = min(kTile, end - j0);
             for (int t = 0; t < n; t++) {
                 const int jl = j0 + t - base;
-                const float4 q = s_pos[t];
-                const float cd = centre_dist(pi, q);
-                if (do_lj && jl != il && cd < P.ljcut) {
-                    if (nlj < P.maxLJ)
-                        B.lj[nlj * nb + g] = jl;
-                    else
-                        overflow = true;
-                    nlj++;
-                }
-                if (do_pairs && cd < kPairPrefilter && jl != hpart) {
-                    const int fj = s_flags[t];
-                    if (((flags ^ fj) & kFlagBeta) != 0) {
-                        const float4 uj = s_uz[t];
-                        const float3 d = site_delta(pi, q, wi, make_float3(-uj.x * rmon, -uj.y * rmon, -uj.z * rmon));
-                        if (norm3_rn(d) < 2.5f) {
-                            if (nlo < P.maxLong)
-                                B.lon[nlo * nb + g] = h0 < 0 ? jl : -jl;
-                            else
-                                overflow = true;
-                            nlo++;
-                        }
-                    }
-                    if (jl != il) {
-                        const int code = jl != 0 ? jl : kZeroCode;
-                        // orientation 0: i site p1, j site p2 -> -j; orientation 1: p2 / p1 -> +j
-                        if (norm3_rn(site_delta(pi, q, f3(li1), f3(s_l2[t]))) < 2.5f) {
-                            if (nla < P.maxLat)
-                                B.lat[nla * nb + g] = -code;
-                            else
-                                overflow = true;
-                            nla++;
-                        }
-                        if (norm3_rn(site_delta(pi, q, f3(li2), f3(s_l1[t]))) < 2.5f) {
-                            if (nla < P.maxLat)
-                                B.lat[nla * nb + g] = code;
-                            else
-                                overflow = true;
-                            nla++;
-                        }
-                    }
-                }
+                const unsigned bits = list_bits(P, I, jl, s_pos[t], s_uz[t], s_l1[t], s_l2[t], s_flags[t]);
+                list_append(P, B, g, I, bits, jl, nlj, nlo, nla, overflow);
             }
         }
         __syncthreads();

@@ -267,7 +267,8 @@ __global__ void __launch_bounds__(256) k_step_plain(KParams P, DevBuffers B) {
 // for bit.  At the end the frames go to the buffer the engine's step parity
 // expects (frame_out for an odd number of steps, frame_in otherwise).
 template <bool KEEP_FORCES>
-__global__ void __launch_bounds__(kPeriodThreads, 2) k_step_period(KParams P, DevBuffers B, int nsteps, int nmax) {
+__global__ void __launch_bounds__(kPeriodThreads, 2) k_step_period(KParams P, DevBuffers B, int nsteps, int nmax,
+                                                                   int rebuild) {
     extern __shared__ float4 s_dyn[];
     const int traj = blockIdx.x;
     const int base = B.off[traj], n = B.off[traj + 1] - base;
@@ -283,6 +284,37 @@ __global__ void __launch_bounds__(kPeriodThreads, 2) k_step_period(KParams P, De
         sfl[j] = B.flags[g];
     }
     __syncthreads();
+    if (rebuild) {
+        // the pair lists of this state first, from the frames in shared
+        // memory: every bead against the trajectory in ascending j, the
+        // decisions of k_rebuild (the same lists)
+        // beads farther apart than every cutoff (plus a margin over the
+        // rounding of the distance) are skipped before the full decisions
+        const float reach = fmaxf(P.lj_on ? P.ljcut : 0.f, P.is_assembly ? kPairPrefilter : 0.f) + 0.05f;
+        const float reach2 = reach * reach;
+        for (int il = threadIdx.x; il < n; il += nt) {
+            const int g = base + il;
+            const ListSite I = list_site(P, sf[il], sf[n + il], sf[2 * n + il], sf[3 * n + il], sfl[il], il,
+                                         B.harm[g * P.maxH]);
+            int nlj = 0, nlo = 0, nla = 0;
+            bool overflow = false;
+            if (I.do_lj || I.do_pairs)
+                for (int jl = 0; jl < n; jl++) {
+                    const float4 q = sf[jl];
+                    const float dx = q.x - I.p.x, dy = q.y - I.p.y, dz = q.z - I.p.z;
+                    if (dx * dx + dy * dy + dz * dz > reach2) continue;
+                    const unsigned bits = list_bits(P, I, jl, q, sf[n + jl], sf[2 * n + jl], sf[3 * n + jl], sfl[jl]);
+                    list_append(P, B, g, I, bits, jl, nlj, nlo, nla, overflow);
+                }
+            if (P.lj_on) B.ljc[g] = min(nlj, P.maxLJ);
+            if (P.is_assembly) {
+                B.lonc[g] = min(nlo, P.maxLong);
+                B.latc[g] = min(nla, P.maxLat);
+            }
+            if (overflow) atomicOr(B.err, kErrOverflow);
+        }
+        __syncthreads();
+    }
     const NbrView V = {sf, sfl, n, 0};
     float f[kPeriodBeads][6];
     for (int step = 0; step < nsteps; step++) {
@@ -560,15 +592,16 @@ int period_prepare(int nmax) {
         return -1;
     return 0;
 }
-void launch_step_period(const KParams &P, const DevBuffers &B, bool keep_forces, int nsteps, int nmax,
+bool period_rebuilds(int nmax) { return nmax <= kPeriodRebuildMax; }
+void launch_step_period(const KParams &P, const DevBuffers &B, bool keep_forces, int nsteps, int nmax, bool rebuild,
                         cudaStream_t s) {
     int t = ((nmax + 31) / 32) * 32;
     if (t > kPeriodThreads) t = kPeriodThreads;
     const size_t bytes = period_smem_bytes(nmax);
     if (keep_forces)
-        k_step_period<true><<<P.nt, t, bytes, s>>>(P, B, nsteps, nmax);
+        k_step_period<true><<<P.nt, t, bytes, s>>>(P, B, nsteps, nmax, rebuild ? 1 : 0);
     else
-        k_step_period<false><<<P.nt, t, bytes, s>>>(P, B, nsteps, nmax);
+        k_step_period<false><<<P.nt, t, bytes, s>>>(P, B, nsteps, nmax, rebuild ? 1 : 0);
 }
 
 void launch_forces(const KParams &P, const DevBuffers &B, bool tea_prepare, cudaStream_t s) {

@@ -346,12 +346,15 @@ bool period_active(const mtg_engine *e) { return e->persistent && !e->p.hdi_on &
 // after the pair-list rebuild due at `step`; run never crosses a rebuild.
 void enqueue_period_run(mtg_engine *e, long long step, int run, bool allow_rebuild = true) {
     const mtg_params &p = e->p;
+    bool in_kernel = false;
     if (allow_rebuild && step % p.ljpairsupdatefreq == 0 && (p.lj_on || p.is_assembly)) {
-        timed_launch(e, 0, [&] { launch_lists(e); });
+        // small trajectories rebuild inside the persistent launch (the same lists)
+        in_kernel = period_rebuilds(e->max_traj_beads);
+        if (!in_kernel) timed_launch(e, 0, [&] { launch_lists(e); });
         e->lists_valid = true;
     }
     timed_launch(e, 10, [&] {
-        launch_step_period(e->kp, e->bufs(), e->keep_forces, run, e->max_traj_beads, e->stream);
+        launch_step_period(e->kp, e->bufs(), e->keep_forces, run, e->max_traj_beads, in_kernel, e->stream);
     });
     if (run & 1) e->cur ^= 1;
 }

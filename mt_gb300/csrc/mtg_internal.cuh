@@ -206,6 +206,97 @@ __device__ __forceinline__ float norm3_rn(float3 d) {
     return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z)));
 }
 
+// --------------------------------------------------------- list decisions
+// Site offsets are at most |p1| ~ 2 nm from the centre, so a site distance
+// below 2.5 nm needs a centre distance below 2.5 + 2 + 2 = 6.5 nm; 6.6 nm
+// leaves room for rounding.
+constexpr float kPairPrefilter = 6.6f;
+
+// Bead i's side of the pair-list decisions (LJ_kernel,
+// src/compute_cuda.cu:913-940; pairs_kernel, :527-674).
+struct ListSite {
+    float4 p, l1, l2;
+    float3 wi;        // R_MON * e_z, R_MON = -r_mon without a harmonic partner
+    float rmon;
+    int flags, il, hpart, h0;
+    bool do_lj, do_pairs;
+};
+__device__ __forceinline__ ListSite list_site(const KParams &P, float4 p, float4 uz, float4 l1, float4 l2, int flags,
+                                              int il, int h0) {
+    ListSite I;
+    I.p = p;
+    I.l1 = l1;
+    I.l2 = l2;
+    // pairs_kernel reads harmonic[max*i] even without a partner (-1 fill):
+    // < 0 -> R_MON = -r_mon and |.| is excluded (src/compute_cuda.cu:548,565,599)
+    I.rmon = h0 < 0 ? -2.0f : 2.0f;
+    I.hpart = h0 < 0 ? -h0 : h0;
+    I.h0 = h0;
+    I.wi = make_float3(uz.x * I.rmon, uz.y * I.rmon, uz.z * I.rmon);
+    I.flags = flags;
+    I.il = il;
+    const bool extra = (flags & kFlagExtra) != 0;
+    I.do_lj = P.lj_on && !extra;
+    I.do_pairs = P.is_assembly && !extra;
+    return I;
+}
+// The lists bead j (index jl in its trajectory) enters for bead i: bit 0 LJ,
+// bit 1 longitudinal, bit 2 lateral with i's site p1 against j's p2 (code
+// -j), bit 3 lateral with i's p2 against j's p1 (code +j); appended in that
+// order for ascending j, as the reference's loops do.
+__device__ __forceinline__ unsigned list_bits(const KParams &P, const ListSite &I, int jl, float4 q, float4 uj,
+                                              float4 l1j, float4 l2j, int fj) {
+    unsigned bits = 0;
+    const float cd = centre_dist(I.p, q);
+    if (I.do_lj && jl != I.il && cd < P.ljcut) bits |= 1u;
+    if (I.do_pairs && cd < kPairPrefilter && jl != I.hpart) {
+        if (((I.flags ^ fj) & kFlagBeta) != 0) {
+            const float3 d = site_delta(I.p, q, I.wi, make_float3(-uj.x * I.rmon, -uj.y * I.rmon, -uj.z * I.rmon));
+            if (norm3_rn(d) < 2.5f) bits |= 2u;
+        }
+        if (jl != I.il) {
+            if (norm3_rn(site_delta(I.p, q, f3(I.l1), f3(l2j))) < 2.5f) bits |= 4u;
+            if (norm3_rn(site_delta(I.p, q, f3(I.l2), f3(l1j))) < 2.5f) bits |= 8u;
+        }
+    }
+    return bits;
+}
+// Appends bead j's entries to bead g's lists (k-major, capacity-checked).
+__device__ __forceinline__ void list_append(const KParams &P, const DevBuffers &B, int g, const ListSite &I,
+                                            unsigned bits, int jl, int &nlj, int &nlo, int &nla, bool &overflow) {
+    const int nb = P.nb;
+    if (bits & 1u) {
+        if (nlj < P.maxLJ)
+            B.lj[nlj * nb + g] = jl;
+        else
+            overflow = true;
+        nlj++;
+    }
+    if (bits & 2u) {
+        if (nlo < P.maxLong)
+            B.lon[nlo * nb + g] = I.h0 < 0 ? jl : -jl;
+        else
+            overflow = true;
+        nlo++;
+    }
+    const int code = jl != 0 ? jl : kZeroCode;
+    // orientation 0: i site p1, j site p2 -> -j; orientation 1: p2 / p1 -> +j
+    if (bits & 4u) {
+        if (nla < P.maxLat)
+            B.lat[nla * nb + g] = -code;
+        else
+            overflow = true;
+        nla++;
+    }
+    if (bits & 8u) {
+        if (nla < P.maxLat)
+            B.lat[nla * nb + g] = code;
+        else
+            overflow = true;
+        nla++;
+    }
+}
+
 // 1/sqrt(x) as the single hardware approximation instruction (a few ulp);
 // pair distances are never subnormal, so the flush-to-zero form gives the
 // same value for them without a subnormal fix-up.
@@ -272,7 +363,11 @@ constexpr size_t kPeriodMaxSmem = 227 * 1024;     // bytes of dynamic shared mem
 size_t period_smem_bytes(int nmax);
 bool period_fits(int nmax);
 int period_prepare(int nmax);                     // opts the kernel into its shared memory (outside captures)
-void launch_step_period(const KParams &P, const DevBuffers &B, bool keep_forces, int nsteps, int nmax,
+// trajectories this small rebuild their pair lists inside the persistent
+// kernel (every bead against the whole trajectory) instead of by launch_lists
+constexpr int kPeriodRebuildMax = 512;
+bool period_rebuilds(int nmax);
+void launch_step_period(const KParams &P, const DevBuffers &B, bool keep_forces, int nsteps, int nmax, bool rebuild,
                         cudaStream_t s);
 void launch_energy(const KParams &P, const DevBuffers &B, double *per_bead, double *partials,
                    const int2 *work, int nwork, cudaStream_t s);

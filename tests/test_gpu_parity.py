@@ -482,17 +482,21 @@ def test_assembly_lists_without_lj_prefilter(engine_mod, oracle_lib, over, metho
     e.close()
 
 
-@pytest.mark.parametrize("keep", [False, True])
-def test_persistent_period_equals_per_step_kernels(engine_mod, keep):
+@pytest.mark.parametrize("keep,small", [(False, False), (True, False), (False, True), (True, True)])
+def test_persistent_period_equals_per_step_kernels(engine_mod, keep, small):
     """The persistent plain path (one launch per pair-list period, one CTA per
     trajectory with its frames in shared memory) gives the per-step kernels'
     result bit for bit, on an uneven batch with extra and fixed beads, with
-    and without stored forces."""
+    and without stored forces; with trajectories of at most 512 beads (small)
+    the pair lists are rebuilt inside the persistent launch, otherwise by the
+    list kernels before it."""
     from mt_gb300 import synth
     p = synth.default_params(seed=61)
     trajs = [synth.make_trajectory(14, 120, seed=61, radius=8.12, psi_mode="make_mt", cube=50.0, thermal=0.05,
                                    n_extra_dimers=2),
              synth.make_trajectory(4, 0, seed=62, radius=8.12, psi_mode="make_mt", cube=50.0, thermal=0.05),
+             synth.make_trajectory(20, 150, seed=63, radius=8.12, psi_mode="make_mt", cube=50.0, thermal=0.05)
+             if small else
              synth.make_trajectory(30, 400, seed=63, radius=8.12, psi_mode="make_mt", cube=60.0, thermal=0.05)]
     b = synth.batch_from_trajectories(p, trajs)
     runs = []
@@ -505,6 +509,8 @@ def test_persistent_period_equals_per_step_kernels(engine_mod, keep):
         e.step(0, 35)                      # three periods from graphs + a direct tail
         kt = e.kernel_times()
         assert (kt["step_period"][1] > 0) == bool(persistent)
+        if persistent:
+            assert (kt["rebuild"][1] == 0) == small, kt["rebuild"]   # lists rebuilt in the launch
         runs.append((e.download_state(forces=True), e.download_rng(), e.lists()))
         e.close()
     (x0, f0), r0, l0 = runs[0]
