@@ -760,7 +760,7 @@ void launch_tea_feff(const KParams &P, const DevBuffers &B, const int2 *work, in
 // Tile of kFFTileLeaves source leaves (kFFPairSlots bead pairs each), in the
 // layout of FFBuffers::pack: the two lanes of a packed pair are two source
 // beads.  Filled from pack by asynchronous 16-byte copies.
-constexpr int kFFTileLeaves = 4;
+constexpr int kFFTileLeaves = 4;   // 128 beads; tiles of 8 leaves measured slower (0.288 against 0.246 ms)
 constexpr int kFFTileSlots = kFFPairSlots * kFFTileLeaves;
 struct FFTile {
     float4 xy[kFFTileSlots];   // xa xb ya yb
@@ -1005,10 +1005,9 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_ff_p2m_inner(KParams P, FFBu
 // pair over every kM2LSlices-th far node, and the slices meet by shuffles in
 // a fixed order.
 constexpr int kM2LWarps = 4;
-#ifndef FF_M2L_SLICES
-#define FF_M2L_SLICES 8
-#endif
-constexpr int kM2LSlices = FF_M2L_SLICES, kM2LLanes = 4 * kM2LSlices;
+// 8 slices (a warp per target); 4 and 2 (two and four targets per warp)
+// measured the same and slower
+constexpr int kM2LSlices = 8, kM2LLanes = 4 * kM2LSlices;
 __global__ void __launch_bounds__(32 * kM2LWarps) k_ff_m2l(KParams P, FFBuffers F, const int *gate) {
     if (gate && *gate != 0) return;
     const int lane = threadIdx.x & 31;
@@ -1085,19 +1084,19 @@ struct FFTargets {
 // The packed pass of one tile: the thread's targets against the tile's bead
 // pairs; with SELF a target's own slot is pushed to r^2 = 1e30, with TRACK
 // the running minimum of r^2 per segment of the thread's pairs is kept.
-// Segment sg of a thread's pairs is exactly the tile's leaf sg, so the
-// padding leaves of a list's last tile (nleaves < kFFTileLeaves) are skipped.
-static_assert(kTeaSeg == kFFTileLeaves, "one segment per tile leaf");
+// A thread takes the pair slots sl, sl + SLICES, ... of every leaf of the
+// tile, leaf after leaf (so the order of its sums does not depend on the tile
+// size); the padding leaves of a list's last tile (q >= nleaves) are skipped.
 template <int SLICES, int TPT, bool SELF, bool TRACK>
 __device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int nleaves, FFTargets<TPT> &X, float2 vkap,
-                                             float2 vn2a2, float2 one, float (&rmin)[kTeaSeg]) {
-    constexpr int kLen = kFFTileSlots / SLICES / kTeaSeg;
+                                             float2 vn2a2, float2 one, float (&rmin)[kFFTileLeaves]) {
+    constexpr int kLen = kFFPairSlots / SLICES;
 #pragma unroll
-    for (int sg = 0; sg < kTeaSeg; sg++) {
-        if (sg >= nleaves) break;
+    for (int q = 0; q < kFFTileLeaves; q++) {
+        if (q >= nleaves) break;
 #pragma unroll(kLen <= 4 ? kLen : 4)
         for (int k = 0; k < kLen; k++) {
-            const int t = sl + (sg * kLen + k) * SLICES;
+            const int t = q * kFFPairSlots + sl + k * SLICES;
             const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
             const float2 rz = T.rz[t];
 #pragma unroll
@@ -1113,12 +1112,12 @@ __device__ __forceinline__ void ff_step_tile(const FFTile &T, int sl, int nleave
                     else
                         r2.x = 1e30f;
                 }
-                if (TRACK) rmin[sg] = fmin3(rmin[sg], r2.x, r2.y);
+                if (TRACK) rmin[q] = fmin3(rmin[q], r2.x, r2.y);
                 const float2 rinv = make_float2(rsqrt_hw(r2.x), rsqrt_hw(r2.y));
-                const float2 q = __fmul2_rn(rinv, rinv);
-                const float2 tq = __fmul2_rn(q, rinv);
+                const float2 q2 = __fmul2_rn(rinv, rinv);
+                const float2 tq = __fmul2_rn(q2, rinv);
                 const float2 cii = __ffma2_rn(vkap, tq, rinv);
-                const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q, one));
+                const float2 cr = __fmul2_rn(tq, __ffma2_rn(vn2a2, q2, one));
                 const float2 s = __fmul2_rn(cr, __ffma2_rn(dx, gx, __ffma2_rn(dy, gy, __fmul2_rn(dz, gz))));
                 X.ax[h] = __ffma2_rn(cii, gx, __ffma2_rn(s, dx, X.ax[h]));
                 X.ay[h] = __ffma2_rn(cii, gy, __ffma2_rn(s, dy, X.ay[h]));
@@ -1229,9 +1228,9 @@ __global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_nea
             const int e = it * kFFTileLeaves + q;
             if (e < nnear && near[e] == L) self_q = q;
         }
-        float rmin[kTeaSeg];
+        float rmin[kFFTileLeaves];
 #pragma unroll
-        for (int sg = 0; sg < kTeaSeg; sg++) rmin[sg] = 3.4e38f;
+        for (int q = 0; q < kFFTileLeaves; q++) rmin[q] = 3.4e38f;
         const bool self = self_q >= 0;
 #pragma unroll
         for (int h = 0; h < TPT; h++) {
@@ -1245,15 +1244,15 @@ __global__ void __launch_bounds__(32 / TPT * SLICES, 32 * TPT / SLICES) k_ff_nea
         else
             ff_step_tile<SLICES, TPT, false, !LISTCORR>(T, sl, nleaves, X, vkap, vn2a2, one, rmin);
         if (!LISTCORR) {
-            constexpr int kLen = kFFTileSlots / SLICES / kTeaSeg;
+            constexpr int kLen = kFFPairSlots / SLICES;
             unsigned segs = 0;
 #pragma unroll
-            for (int sg = 0; sg < kTeaSeg; sg++) segs |= (rmin[sg] <= K.four_a2 ? 1u : 0u) << sg;
-            while (segs) {  // the segments that hold an overlapping pair
+            for (int q = 0; q < kFFTileLeaves; q++) segs |= (rmin[q] <= K.four_a2 ? 1u : 0u) << q;
+            while (segs) {  // the tile leaves that hold an overlapping pair
                 const int sg = __ffs(segs) - 1;
                 segs &= segs - 1;
                 for (int k = 0; k < kLen; k++) {
-                    const int t = sl + (sg * kLen + k) * SLICES;
+                    const int t = sg * kFFPairSlots + sl + k * SLICES;
                     const float4 a = T.xy[t], b = T.zf[t], c = T.fyz[t], d = T.rxy[t];
                     const float2 rz = T.rz[t];
 #pragma unroll
@@ -1405,10 +1404,9 @@ void launch_ff_proxies(const KParams &P, const DevBuffers &B, const FFBuffers &F
 // within 2a (plus 2 nm for the motion since its rebuild).
 static bool ff_list_corr(const KParams &P) { return P.lj_on && P.ljcut >= 2.0f * P.tea_a + 2.0f; }
 
-#ifndef FF_TPT
-#define FF_TPT 1
-#endif
-constexpr int kFFTPT = FF_TPT;   // target beads per thread of the far-field step
+// target beads per thread of the near-pair kernel (two, with 16 lanes per
+// slice, measured slower)
+constexpr int kFFTPT = 1;
 template <int SL>
 static void ff_near_launch(const KParams &P, const DevBuffers &B, const FFBuffers &F, const int *gate,
                            cudaStream_t s) {
